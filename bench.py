@@ -1,0 +1,330 @@
+#!/usr/bin/env python3
+"""Spin-trials/s of the Metropolis anneal on one GB300.
+
+Workload (the headline configuration): a 256x256x1 film, dx = dy = 1 nm,
+dz = 0.8 nm, Ms = 1.6e6 A/m, Aex = 16 pJ/m, Dind = 6 mJ/m^2, Ku1 = 2 MJ/m^3
+along z, Bext = 0.3 T along z, 20 periodic images in x and y, open in z, demag
+on, random unit-vector start from seed 256, anneal 1400 K -> 40 K by x0.90 per
+stage with 10000 Metropolis sweeps per stage.  One bench step is one
+temperature stage (10000 sweeps of 65536 trials), taken in anneal order.  The
+lattice state is resident in HBM between steps; an L2 flush (a 512 MB write)
+separates the timed steps.  FP32 bulk arithmetic ("f32"); the plain FP64 path
+is timed on the same workload as well.
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
+
+N > 1 runs one independent replica per GPU (seeds 256 + rank); rank 0 prints
+one JSON line.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "micromagnetic-gpu-monte-carlo_gb300")
+for p in (PKG, os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "spin-trials/s, 256^2x1 demag on"
+UNIT = "spin-trials/s"
+WORKLOAD = dict(nx=256, ny=256, nz=1, dx=1e-9, dy=1e-9, dz=0.8e-9, ms=1.6e6, Aex=16e-12, Dind=6e-3, Ku1=2e6,
+                anisUx=0.0, anisUy=0.0, anisUz=1.0, Bextx=0.0, Bexty=0.0, Bextz=0.3, pbc_x=20, pbc_y=20, pbc_z=0,
+                cal_demag_flag=1, randomseed=256, use_random_init=1, Temperature_start=1400.0,
+                Temperature_end=40.0, Temperature_step=0.9, Temperature_use_exp=1, circle_per_stage=10000,
+                rand_block_size=40)
+SWEEPS_PER_STAGE = 10000
+CACHE_DIR = os.environ.get("MMC_BENCH_CACHE", "/tmp/mmc_bench_tensor_cache")
+
+
+def stage_temperature(k):
+    t = np.float32(1400.0)
+    for _ in range(k):
+        t = np.float32(t * np.float32(0.9))
+    return float(t)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def l2_flush(torch, dev, buf=[]):
+    if not buf:
+        buf.append(torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev))
+    buf[0].fill_(1.0)
+    torch.cuda.synchronize(dev)
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return dist, rank, local, world
+    return None, rank, local, world
+
+
+def reduce_max(dist, v):
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t[0])
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_sample(M, O, k6, seconds=12.0, threads=0):
+    """FP64 oracle sweeps of the same lattice on the host cores."""
+    cfg = M.Config.defaults(precision=64, **WORKLOAD)
+    m = O.init_random(cfg, 256)
+    n = m.shape[1]
+    t0 = time.perf_counter()
+    O.sweeps(cfg, k6, stage_temperature(0), 0, 0, 1, m, demag_mode=1, nthreads=threads)
+    one = time.perf_counter() - t0
+    ns = max(1, int(seconds / max(one, 1e-3)))
+    t0 = time.perf_counter()
+    O.sweeps(cfg, k6, stage_temperature(0), 0, 1, ns, m, demag_mode=1, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return ns * n / dt, ns
+
+
+def run_reference(args):
+    """The reference's CPU path on the host cores.  The reference cannot be
+    built (its Metropolis, energy and tensor-image kernel bodies are not
+    published), so this arm runs the project's FP64 C++ restatement of the same
+    sweep (the oracle) on every host core."""
+    dist, rank, local, world = dist_setup()
+    if rank != 0:
+        return
+    import mmc_ctypes as M
+    import oracle_ctypes as O
+    cores = os.cpu_count() or 1
+    # The sweep cost does not depend on the tensor values, so the sample uses the
+    # 256x256 tensor with 2 images (20 images take ~40 core-minutes to build on
+    # the CPU).
+    tcfg = M.Config.defaults(precision=64, **dict(WORKLOAD, pbc_x=2, pbc_y=2))
+    k6 = O.tensor(tcfg)
+    vals = []
+    n_sw = 0
+    for i in range(args.warmup + args.steps):
+        v, ns = cpu_sample(M, O, k6, seconds=args.ref_seconds, threads=cores)
+        if i >= args.warmup:
+            vals.append(v)
+            n_sw += ns
+    value = statistics.mean(vals)
+    sample = f"{n_sw} FP64 sweeps of the 256x256x1 lattice with FFT demag over {args.steps} steps"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "anneal stage 256x256x1, demag, PBC 20 images (x,y), 10000 sweeps/stage",
+                   "cache": "lattice resident in host memory"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference not buildable (kernel bodies unpublished); FP64 C++ port of the sweep on all host cores",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    dist, rank, local, world = dist_setup()
+    import torch
+    import mmc_ctypes as M
+    import oracle_ctypes as O  # CPU-baseline leg only
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    os.makedirs(CACHE_DIR, exist_ok=True)
+    seed = 256 + rank
+    cfg = M.Config.defaults(precision=32, **dict(WORKLOAD, randomseed=seed))
+    lat = M.Lattice(cfg, device=local)
+    t0 = time.perf_counter()
+    lat.build_demag(CACHE_DIR)
+    setup_s = time.perf_counter() - t0
+    n = lat.n
+    S = args.sweeps
+
+    # warm-up stages
+    for k in range(args.warmup):
+        lat.run_sweeps(stage_temperature(k), k, 0, S)
+    barrier(dist)
+    torch.cuda.synchronize(dev)
+    times = []
+    with ClockSampler(local) as clk:
+        for j in range(args.steps):
+            k = args.warmup + j
+            l2_flush(torch, dev)
+            lat.run_sweeps(stage_temperature(k), k, 0, S)
+            times.append(lat.last_run_ms() / 1e3)
+    torch.cuda.synchronize(dev)
+    barrier(dist)
+    total = reduce_max(dist, sum(times))
+    value = world * args.steps * S * n / total
+
+    # end to end through the public API with host buffers
+    pin_in = torch.empty((3, n), dtype=torch.float64).pin_memory()
+    pin_out = torch.empty((3, n), dtype=torch.float64).pin_memory()
+    pin_in.numpy()[:] = lat.get_m()
+    e2e_t = 0.0
+    for j in range(args.steps):
+        k = args.warmup + args.steps + j
+        l2_flush(torch, dev)
+        t0 = time.perf_counter()
+        lat.set_m(pin_in.numpy())
+        lat.run_sweeps(stage_temperature(k), k, 0, S)
+        mo = pin_out.numpy()
+        M.check(M.lib().mmc_get_m(lat.h, M.dptr(mo[0]), M.dptr(mo[1]), M.dptr(mo[2])))
+        e2e_t += time.perf_counter() - t0
+    e2e_t = reduce_max(dist, e2e_t)
+    e2e = world * args.steps * S * n / e2e_t
+
+    # per-family attribution with CUDA events on the library's stream
+    prof_sweeps = 500
+    prof = lat.profile_sweeps(stage_temperature(args.warmup), args.warmup, 0, prof_sweeps)
+    fam = {"demag_conv": prof[0] / prof_sweeps, "metropolis_sweep": prof[1] / prof_sweeps}
+    s = 4
+    nh = (256 // 2 + 1) * 256
+    bytes_fam = {"demag_conv": 6 * s * n + 12 * s * nh, "metropolis_sweep": 9 * s * n}
+    dom = max(fam, key=fam.get)
+    peak, peak_kind = measured_peaks()
+    achieved = bytes_fam[dom] / (fam[dom] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": bytes_fam[dom], "avg_ms_per_launch": fam[dom],
+                "family_ms_per_sweep": fam}
+
+    # plain FP64 path on the same workload (fewer sweeps per step)
+    cfg64 = cfg.copy(precision=64)
+    lat64 = M.Lattice(cfg64, device=local)
+    lat64.build_demag(CACHE_DIR)
+    s64 = max(100, S // 10)
+    lat64.run_sweeps(stage_temperature(0), 0, 0, s64)
+    t64 = 0.0
+    for j in range(2):
+        lat64.run_sweeps(stage_temperature(1 + j), 1 + j, 0, s64)
+        t64 += lat64.last_run_ms() / 1e3
+    fp64 = 2 * s64 * n / t64
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "anneal stage 256x256x1, demag, PBC 20 images (x,y), 10000 sweeps/stage",
+                   "sweeps_per_step": S, "cells": n, "precision": "fp32 bulk, fp64 tensor and energy",
+                   "l2": "512 MB flush between timed steps", "replicas": world},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * n * 8, "d2h_bytes_per_step": 3 * n * 8},
+        "roofline": roofline,
+        "clocks": clk.summary(),
+        "gpu_launches": args.steps * S * (3 + 2 + 1),
+        "fp64_plain": {"value": fp64, "unit": UNIT, "sweeps_timed": 2 * s64,
+                       "fp32_over_fp64": value / world / fp64},
+        "setup_s": setup_s,
+    }
+    if rank == 0 and not args.no_cpu:
+        k6 = lat.tensor()
+        v1, ns1 = cpu_sample(M, O, k6, seconds=args.cpu_seconds, threads=1)
+        cores = os.cpu_count() or 1
+        vN, nsN = cpu_sample(M, O, k6, seconds=args.cpu_seconds, threads=cores)
+        line["cpu_baseline"] = {"value": vN, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{nsN} FP64 sweeps of the same 256x256x1 lattice (FFT demag)",
+                                "single_thread": v1}
+    lat.close()
+    lat64.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sweeps", type=int, default=SWEEPS_PER_STAGE)
+    ap.add_argument("--cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--ref-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

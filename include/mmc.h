@@ -1,0 +1,230 @@
+/*
+ * mmc.h -- C ABI of the GB300 micromagnetic Monte Carlo annealer.
+ *
+ * The reference program (chg-hou/Micromagnetic-GPU-Monte-Carlo) is a single
+ * CUDA executable whose only public surface is its command line, its ini file
+ * and its output files; its GPU work is done by file-scope kernels.  Each entry
+ * point below replaces one of those pieces and cites the reference interface
+ * it stands in for (paths are relative to the reference project).
+ *
+ * Conventions
+ *  - Every function that can fail returns an int status (MMC_OK == 0) and never
+ *    calls exit(); mmc_last_error() gives a message for the calling thread.
+ *  - Host arrays are caller-owned and copied; device memory is owned by the
+ *    handle.  One handle per host thread; the library starts no threads.
+ *  - Lattice arrays on the host are indexed x fastest, then y, then z:
+ *    i = x + nx*(y + ny*z) (the OVF data order).  The reference's own host
+ *    arrays were z fastest (src/mx_init.h:98-153); callers holding that order
+ *    transpose before calling.
+ *  - Fields are in A/m, energies in J, temperatures in K, lengths in m.
+ */
+#ifndef MMC_H_
+#define MMC_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MMC_ABI_VERSION 1
+
+enum mmc_status {
+  MMC_OK = 0,
+  MMC_ERR_INVALID = 1,      /* bad argument or config value */
+  MMC_ERR_CONFIG = 2,       /* ini syntax error or missing key */
+  MMC_ERR_IO = 3,           /* file could not be opened / read / written, malformed OVF */
+  MMC_ERR_CUDA = 4,         /* CUDA runtime error */
+  MMC_ERR_NO_DEVICE = 5,    /* no usable CUDA device */
+  MMC_ERR_UNSUPPORTED = 6,  /* e.g. an FFT length with a prime factor above 31 */
+  MMC_ERR_INTERRUPTED = 7,  /* mmc_request_stop() was called */
+  MMC_ERR_TIMEOUT = 8,      /* a device-side wait ran out of its iteration budget */
+  MMC_ERR_STATE = 9,        /* call made in the wrong order (e.g. demag not built) */
+  MMC_ERR_OOM = 10          /* device allocation failed */
+};
+
+/* Field / energy terms for mmc_get_field(). */
+enum mmc_term {
+  MMC_TERM_EXCHANGE = 0,
+  MMC_TERM_DMI = 1,
+  MMC_TERM_ANISOTROPY = 2,
+  MMC_TERM_ZEEMAN = 3,
+  MMC_TERM_DEMAG = 4,
+  MMC_TERM_TOTAL = 5
+};
+
+enum mmc_ovf_format { MMC_OVF_BINARY4 = 0, MMC_OVF_BINARY8 = 1, MMC_OVF_TEXT = 2 };
+
+/*
+ * Simulation parameters.  The first block holds exactly the 26 ini keys of the
+ * reference (src/parse_input_ini.h:15-41, example README.md:44-86) with the
+ * same names and meaning; bools are ints (0/1).  The second block holds
+ * optional keys added by this library; their defaults reproduce the reference
+ * behaviour.
+ */
+typedef struct mmc_config {
+  int nx, ny, nz;
+  double dx, dy, dz;
+  double Bextx, Bexty, Bextz;              /* applied field, T */
+  int pbc_x, pbc_y, pbc_z;                 /* 0: open (zero-padded), >0: periodic with that many images, <0: periodic, no images */
+  double ms, Aex, Dind;                    /* A/m, J/m, J/m^2 */
+  double anisUx, anisUy, anisUz, Ku1;      /* axis (normalised internally), J/m^3 */
+  int use_random_init;
+  long long randomseed;                    /* < 0: time(NULL) (src/main.cu:246-250) */
+  char ovf_filename[1024];
+  double Temperature_start, Temperature_end, Temperature_step;
+  long long circle_per_stage;              /* sweeps per temperature stage */
+  long long terminal_output_period;
+  long long energy_output_period;
+  long long ms_output_period;
+  int rand_block_size;                     /* accepted for compatibility; see DESIGN */
+  int cal_demag_flag;
+  int Temperature_use_exp;                 /* 1: T *= step, 0: T -= step */
+
+  /* ---- optional keys (not in the reference) ---- */
+  int precision;                           /* 32 (default, the reference's FLOAT_=float) or 64 */
+  int ovf_format;                          /* enum mmc_ovf_format, default MMC_OVF_BINARY4 */
+  int use_reference_pi;                    /* 1: pi = 3.14159265358 as src/constant.h:21 */
+  char tensor_cache[1024];                 /* directory for the demag tensor cache ("" = off) */
+} mmc_config;
+
+typedef struct mmc_observables {
+  double e_total;                          /* J, sum of the five terms */
+  double e_exchange, e_dmi, e_anisotropy, e_zeeman, e_demag;
+  double m[3];                             /* average reduced magnetisation */
+  double q;                                /* topological charge per layer (Berg-Luescher) */
+  unsigned long long accepted, proposed;   /* Metropolis counts since the last mmc_energy() */
+} mmc_observables;
+
+typedef struct mmc_handle mmc_handle;
+
+int mmc_abi_version(void);
+/* sizeof(mmc_config) as compiled into the library (binding sanity check). */
+size_t mmc_config_size(void);
+const char* mmc_status_string(int status);
+/* Message of the last failing call on this thread ("" if none). */
+const char* mmc_last_error(void);
+
+/* Fill every field with the reference's README example values and the optional defaults. */
+void mmc_config_defaults(mmc_config* cfg);
+
+/* Replaces parse_input_ini (src/parse_input_ini.h:15-47).  All 26 reference
+ * keys are required; unknown keys are an error; the optional keys above may be
+ * given as well. */
+int mmc_config_load_ini(const char* path, mmc_config* cfg);
+
+/* Replaces cout_input_ini (src/parse_input_ini.h:49-114): writes the
+ * "key: value" echo into buf (NUL-terminated, truncated to len). */
+int mmc_config_format(const mmc_config* cfg, char* buf, size_t len);
+
+/* Padded FFT dimensions (src/main.cu:254-263): n -> 2n-1 on open axes. */
+int mmc_padded_dims(const mmc_config* cfg, int out[3]);
+
+/* Allocates the device state for one lattice on CUDA device `device`
+ * (the -gpu= flag, src/GPU_selector.h:35-76).  m starts at +z. */
+int mmc_create(const mmc_config* cfg, int device, mmc_handle** out);
+void mmc_destroy(mmc_handle* h);
+
+/* Replaces randInitMx (src/mx_init.h:21-97): every cell gets an independent
+ * direction uniform on the sphere, from Philox4x32-10 keyed on the seed. */
+int mmc_init_random(mmc_handle* h, long long seed);
+
+/* Host <-> device copies of m (replace copyMxtoMxpadded / copyMxpaddedtoMx,
+ * src/mx_init.h:98-153).  Arrays hold nx*ny*nz values, x fastest. */
+int mmc_set_m(mmc_handle* h, const double* mx, const double* my, const double* mz);
+int mmc_get_m(mmc_handle* h, double* mx, double* my, double* mz);
+
+/* Newell demag tensor with periodic images (ktensorCPU / ktensorKernel2_*,
+ * src/demag_cu.cu:119-248, src/main.cu:419-573) and its FFT (src/main.cu:589-675).
+ * With a non-empty cache_dir (the -tensorcache= flag) the tensor is read from /
+ * written to cache_<nxp>_<nyp>_<nzp>-<dx>_<dy>_<dz>-<pbcx>_<pbcy>_<pbcz>.ovf
+ * in the reference's raw layout.  Called implicitly by the first call that
+ * needs it when cal_demag_flag is set. */
+int mmc_build_demag(mmc_handle* h, const char* cache_dir);
+
+/* The real-space tensor: 6 blocks (xx,xy,xz,yy,yz,zz) of nxp*nyp*nzp doubles,
+ * x fastest within a block. */
+int mmc_get_tensor(mmc_handle* h, double* k6);
+
+/* Replaces calDemagMirrorTensor (src/demag_mirror.h:18-24): the tensor at zero
+ * offset including periodic images, order xx,xy,xz,yy,yz,zz. */
+int mmc_self_tensor(mmc_handle* h, double k6[6]);
+
+/* One demag convolution of the current m (src/main.cu:868-884 plus the
+ * inverse transform and crop that the reference never executed). */
+int mmc_compute_demag(mmc_handle* h);
+
+/* Device-pointer form of the demag convolution, the kernel-level contract of
+ * calHexchangeKernel + the cuFFT calls around it (src/demag_cu.h:36-39,
+ * src/main.cu:868-884): hdev = K * mdev for this handle's lattice, using the
+ * handle's tensor spectrum.  mdev and hdev hold 3*nx*ny*nz values of the
+ * handle's precision (float for precision 32, double for 64), SoA, x fastest;
+ * hdev is dimensionless (H_demag = ms * hdev).  scratch is a caller-owned
+ * device buffer of at least mmc_demag_scratch_bytes() bytes.  The work is
+ * enqueued on `stream` (a cudaStream_t; NULL means the handle's stream) and
+ * the call returns without synchronising. */
+int mmc_demag_scratch_bytes(mmc_handle* h, size_t* bytes);
+int mmc_demag_apply(mmc_handle* h, const void* mdev, void* hdev, void* scratch, size_t scratch_bytes,
+                    void* stream);
+
+/* Per-term effective field in A/m for the current m, the DEBUG_H_FIELD dumps of
+ * src/main.cu:965-1086.  MMC_TERM_DEMAG and MMC_TERM_TOTAL use the demag field
+ * of the last mmc_compute_demag() / sweep. */
+int mmc_get_field(mmc_handle* h, int term, double* hx, double* hy, double* hz);
+
+/* Energy and observables of the current m (calEnergyKernel + thrust::reduce,
+ * src/effective_H.h:35-43, src/main.cu:902-956).  Recomputes the demag field
+ * first.  Resets the acceptance counters. */
+int mmc_energy(mmc_handle* h, mmc_observables* out);
+
+/* nsweeps Metropolis sweeps at `temperature` (mcKernel2, src/mc_sampling.h:27-41,
+ * launched src/main.cu:1101-1120), each preceded by a demag refresh when
+ * cal_demag_flag is set.  Random numbers are keyed on (seed, stage, sweep, cell),
+ * so splitting a stage into several calls gives the same result. */
+int mmc_run_sweeps(mmc_handle* h, double temperature, long long stage, long long sweep0,
+                   long long nsweeps);
+
+/* Device time, in ms, of the last mmc_run_sweeps() call: CUDA events recorded
+ * on the handle's stream around the enqueued sweeps. */
+int mmc_last_run_ms(mmc_handle* h, double* ms);
+
+/* Runs nsweeps sweeps like mmc_run_sweeps() but without graphs, timing each
+ * group of kernels with CUDA events: out_ms[0] = total of the demag
+ * convolutions, out_ms[1] = total of the sweep (Metropolis) kernels,
+ * out_ms[2] = whole run.  Used to attribute time per kernel family. */
+int mmc_profile_sweeps(mmc_handle* h, double temperature, long long stage, long long sweep0, long long nsweeps,
+                       double out_ms[3]);
+
+/* The whole temperature-stage loop of src/main.cu:801-1139 with its outputs
+ * (energy.txt, %06ld_%.2fK_%ld.ovf snapshots) written into output_dir.
+ * verbose != 0 prints progress lines to stdout. */
+int mmc_run_anneal(mmc_handle* h, const char* output_dir, int verbose);
+
+/* Asks a running call on another thread (or a signal handler) to stop at the
+ * next sweep boundary; that call returns MMC_ERR_INTERRUPTED. */
+void mmc_request_stop(mmc_handle* h);
+
+/* OVF 1.0/2.0 reader (parseOvfFile, src/ovf_io.h:88-91): text, binary 4 and
+ * binary 8 data; dimensions must match and step sizes agree within 1e-5
+ * relative (src/ovf_io.h:35-64). */
+int mmc_ovf_read(const char* path, int nx, int ny, int nz, double dx, double dy, double dz,
+                 double* mx, double* my, double* mz);
+
+/* OVF 2.0 writer (writetoOvfFile, src/ovf_io.h:93-98). */
+int mmc_ovf_write(const char* path, int nx, int ny, int nz, double dx, double dy, double dz,
+                  const double* mx, const double* my, const double* mz, int format,
+                  const char* title);
+
+/* Test hook (no counterpart in the reference, whose random pools came from
+ * cuRAND's host API, src/main.cu:351-385): evaluates Philox4x32-10 on device
+ * `device` for n counters ctr[4*i..4*i+3] and key (k0, k1).  out receives this
+ * library's result and out_curand cuRAND's curand_Philox4x32_10; either may be
+ * NULL.  Both arrays hold 4*n words. */
+int mmc_selftest_philox(int device, long long n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out,
+                        uint32_t* out_curand);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MMC_H_ */

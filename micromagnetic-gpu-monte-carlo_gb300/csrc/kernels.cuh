@@ -1,0 +1,748 @@
+// kernels.cuh -- demag convolution passes, Metropolis sweep, energy and field
+// kernels, templated on the working precision T (float or double).
+//
+// Included by kernels_f32.cu (built with multiply-add contraction) and
+// kernels_f64.cu (built with -fmad=false so that FP64 results match the CPU
+// oracle bit for bit where the operation order is the same).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fft.cuh"
+#include "mmc_internal.h"
+#include "mmc_math.h"
+
+namespace mmc {
+
+// =========================================================== demag passes
+//
+// The reference computes H^ = K^ . M^ / N with three cuFFT R2C transforms and
+// calHexchangeKernel (src/main.cu:868-884, src/demag_cu.cu:68-116) and never
+// runs the inverse.  Here the convolution is complete and split into
+//   x_forward : real rows -> half spectrum along x (two real rows per complex FFT)
+//   col_pass  : complex FFT along y or z over tiles of kx columns, optionally
+//               fused with the 3x3 tensor product and the inverse FFT
+//   x_inverse : half spectrum -> real rows, cropped to the lattice
+// Rows that are pure zero padding are never loaded (pruned transform).
+
+// Real rows in[c][row][x] (x < xdata, zero up to p.n) -> S[c][z][y][kx], kx < hx.
+template <typename T>
+__global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrows, const T* __restrict__ in,
+                            long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, int hx,
+                            int rows_per_cta) {
+  using V = C<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* tw = reinterpret_cast<V*>(smem_raw);
+  const int L = p.n;
+  const int npairs = (ncomp + 1) / 2;
+  const int row0 = blockIdx.x * rows_per_cta;
+  const int nr = min(rows_per_cta, nrows - row0);
+  V* bufA = tw + ((p.tw_total + 1) & ~1);
+  V* bufB = bufA + (long long)rows_per_cta * npairs * L;
+  load_twiddles<T>(p, tw);
+  for (int idx = threadIdx.x; idx < nr * L; idx += blockDim.x) {
+    const int rr = idx / L, x = idx - rr * L;
+    const long long rbase = (long long)(row0 + rr) * xdata + x;
+    for (int pr = 0; pr < npairs; ++pr) {
+      const int ca = 2 * pr, cb = 2 * pr + 1;
+      T va = 0, vb = 0;
+      if (x < xdata) {
+        va = in[ca * in_cstride + rbase];
+        if (cb < ncomp) vb = in[cb * in_cstride + rbase];
+      }
+      bufA[(long long)(rr * npairs + pr) * L + x] = cmk<V>(va, vb);
+    }
+  }
+  __syncthreads();
+  V* res = fft_lines<T, false>(bufA, bufB, nr * npairs, L, p, tw);
+  for (int idx = threadIdx.x; idx < nr * npairs * hx; idx += blockDim.x) {
+    const int k = idx % hx;
+    const int rest = idx / hx;
+    const int pr = rest % npairs, rr = rest / npairs;
+    const V* line = res + (long long)(rr * npairs + pr) * L;
+    const V A = line[k];
+    const V B = line[k == 0 ? 0 : L - k];
+    const int row = row0 + rr;
+    const int y = row % ydata, z = row / ydata;
+    const long long off = ((long long)z * nyp + y) * hx + k;
+    const int ca = 2 * pr, cb = 2 * pr + 1;
+    S[ca * nspec + off] = cmk<V>((T)0.5 * (A.x + B.x), (T)0.5 * (A.y - B.y));
+    if (cb < ncomp) S[cb * nspec + off] = cmk<V>((T)0.5 * (A.y + B.y), (T)-0.5 * (A.x - B.x));
+  }
+}
+
+// Half spectra S[0..2][z][y][kx] -> real rows out[c][row][x], x < xout.
+template <typename T>
+__global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int xout,
+                            int yout, int nrows, T* __restrict__ out, long long out_cstride, int rows_per_cta) {
+  using V = C<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* tw = reinterpret_cast<V*>(smem_raw);
+  const int L = p.n;
+  const int row0 = blockIdx.x * rows_per_cta;
+  const int nr = min(rows_per_cta, nrows - row0);
+  V* bufA = tw + ((p.tw_total + 1) & ~1);
+  V* bufB = bufA + (long long)rows_per_cta * 2 * L;
+  load_twiddles<T>(p, tw);
+  for (int idx = threadIdx.x; idx < nr * L; idx += blockDim.x) {
+    const int rr = idx / L, k = idx - rr * L;
+    const int row = row0 + rr;
+    const int y = row % yout, z = row / yout;
+    const long long base = ((long long)z * nyp + y) * hx;
+    V v[3];
+    const bool lo = k < hx;
+    const long long kk = lo ? k : L - k;
+    for (int c = 0; c < 3; ++c) {
+      V s = S[c * nspec + base + kk];
+      if (!lo) s.y = -s.y;
+      if (k == 0 || 2 * k == L) s.y = 0;  // bins that are real for a real output
+      v[c] = s;
+    }
+    bufA[(long long)(rr * 2) * L + k] = cmk<V>(v[0].x - v[1].y, v[0].y + v[1].x);
+    bufA[(long long)(rr * 2 + 1) * L + k] = v[2];
+  }
+  __syncthreads();
+  V* res = fft_lines<T, true>(bufA, bufB, nr * 2, L, p, tw);
+  for (int idx = threadIdx.x; idx < nr * xout; idx += blockDim.x) {
+    const int rr = idx / xout, x = idx - rr * xout;
+    const long long o = (long long)(row0 + rr) * xout + x;
+    const V a = res[(long long)(rr * 2) * L + x];
+    const V b = res[(long long)(rr * 2 + 1) * L + x];
+    out[o] = a.x;
+    out[out_cstride + o] = a.y;
+    out[2 * out_cstride + o] = b.x;
+  }
+}
+
+enum : int { PASS_FWD = 1, PASS_MUL = 2, PASS_INV = 4 };
+
+// Complex FFT along a strided axis (y or z) of tiles of `tx` consecutive kx
+// columns.  Element (c, pos, col) lives at S[c*nspec + plane*plane_stride +
+// pos*pos_stride + kx0 + col].  Loads pos < load_lim (zero above), stores
+// pos < store_lim.  With PASS_MUL the tile is multiplied by the symmetric
+// tensor spectrum (K^ . M^ / N, calHexchangeKernel) between the transforms.
+template <typename T>
+__global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long nspec, const C<T>* __restrict__ khat,
+                           int hx, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
+                           int flags, T inv_n, int tx) {
+  using V = C<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* tw = reinterpret_cast<V*>(smem_raw);
+  const int L = p.n;
+  const int stride = L + 1;
+  const int kx0 = blockIdx.x * tx;
+  const int ntx = min(tx, hx - kx0);
+  const long long pbase = (long long)blockIdx.y * plane_stride + kx0;
+  const int nlines = ncomp * ntx;
+  V* bufA = tw + ((p.tw_total + 1) & ~1);
+  V* bufB = bufA + (long long)ncomp * tx * stride;
+  load_twiddles<T>(p, tw);
+  for (int idx = threadIdx.x; idx < ncomp * L * ntx; idx += blockDim.x) {
+    const int t = idx % ntx;
+    const int rest = idx / ntx;
+    const int pos = rest % L, c = rest / L;
+    V val = cmk<V>(0, 0);
+    if (pos < load_lim) val = S[c * nspec + pbase + pos * pos_stride + t];
+    bufA[(long long)(c * ntx + t) * stride + pos] = val;
+  }
+  __syncthreads();
+  V* cur = bufA;
+  V* oth = bufB;
+  if (flags & PASS_FWD) {
+    V* r = fft_lines<T, false>(cur, oth, nlines, stride, p, tw);
+    if (r != cur) {
+      oth = cur;
+      cur = r;
+    }
+  }
+  if (flags & PASS_MUL) {
+    for (int idx = threadIdx.x; idx < L * ntx; idx += blockDim.x) {
+      const int t = idx % ntx, pos = idx / ntx;
+      const long long ka = pbase + pos * pos_stride + t;
+      const V kxx = khat[ka], kxy = khat[nspec + ka], kxz = khat[2 * nspec + ka];
+      const V kyy = khat[3 * nspec + ka], kyz = khat[4 * nspec + ka], kzz = khat[5 * nspec + ka];
+      V* px = cur + (long long)(0 * ntx + t) * stride + pos;
+      V* py = cur + (long long)(1 * ntx + t) * stride + pos;
+      V* pz = cur + (long long)(2 * ntx + t) * stride + pos;
+      const V mx = *px, my = *py, mz = *pz;
+      // src/demag_cu.cu:98-111: real and imaginary parts of sum_b K_ab M_b, divided by N
+      T hxr = (mx.x * kxx.x - mx.y * kxx.y) + (my.x * kxy.x - my.y * kxy.y) + (mz.x * kxz.x - mz.y * kxz.y);
+      T hxi = (mx.x * kxx.y + mx.y * kxx.x) + (my.x * kxy.y + my.y * kxy.x) + (mz.x * kxz.y + mz.y * kxz.x);
+      T hyr = (mx.x * kxy.x - mx.y * kxy.y) + (my.x * kyy.x - my.y * kyy.y) + (mz.x * kyz.x - mz.y * kyz.y);
+      T hyi = (mx.x * kxy.y + mx.y * kxy.x) + (my.x * kyy.y + my.y * kyy.x) + (mz.x * kyz.y + mz.y * kyz.x);
+      T hzr = (mx.x * kxz.x - mx.y * kxz.y) + (my.x * kyz.x - my.y * kyz.y) + (mz.x * kzz.x - mz.y * kzz.y);
+      T hzi = (mx.x * kxz.y + mx.y * kxz.x) + (my.x * kyz.y + my.y * kyz.x) + (mz.x * kzz.y + mz.y * kzz.x);
+      *px = cmk<V>(hxr * inv_n, hxi * inv_n);
+      *py = cmk<V>(hyr * inv_n, hyi * inv_n);
+      *pz = cmk<V>(hzr * inv_n, hzi * inv_n);
+    }
+    __syncthreads();
+  }
+  if (flags & PASS_INV) {
+    V* r = fft_lines<T, true>(cur, oth, nlines, stride, p, tw);
+    if (r != cur) {
+      oth = cur;
+      cur = r;
+    }
+  }
+  for (int idx = threadIdx.x; idx < ncomp * store_lim * ntx; idx += blockDim.x) {
+    const int t = idx % ntx;
+    const int rest = idx / ntx;
+    const int pos = rest % store_lim, c = rest / store_lim;
+    S[c * nspec + pbase + pos * pos_stride + t] = cur[(long long)(c * ntx + t) * stride + pos];
+  }
+}
+
+// =========================================================== lattice helpers
+// Neighbour index along an axis, or -1 when the bond does not exist (open
+// edge, or a periodic axis of length 1 where the neighbour is the cell itself).
+__device__ __forceinline__ long long nbr_idx(const Geom& g, int x, int y, int z, int axis, int dir) {
+  int c[3] = {x, y, z};
+  const int n[3] = {g.nx, g.ny, g.nz};
+  int v = c[axis] + dir;
+  if (v < 0 || v >= n[axis]) {
+    if (!g.per[axis]) return -1;
+    v = v < 0 ? v + n[axis] : v - n[axis];
+  }
+  if (v == c[axis]) return -1;
+  c[axis] = v;
+  return c[0] + (long long)g.nx * (c[1] + (long long)g.ny * c[2]);
+}
+
+__device__ __forceinline__ int axis_color(int v, int n, int per) {
+  if (per && (n & 1) && n > 1 && v == n - 1) return 2;
+  return v & 1;
+}
+
+__device__ __forceinline__ int cell_color(const Geom& g, int x, int y, int z) {
+  int s = axis_color(x, g.nx, g.per[0]) + axis_color(y, g.ny, g.per[1]) + axis_color(z, g.nz, g.per[2]);
+  return g.ncolors == 2 ? (s & 1) : (s % 3);
+}
+
+// =========================================================== Metropolis sweep
+//
+// One sublattice colour of one sweep.  This replaces mcKernel2
+// (src/mc_sampling.h:27-41, launched src/main.cu:1101-1120), whose body is not
+// published.  Cells of one colour share no exchange or DMI bond, so they are
+// updated in place concurrently.  For cell i:
+//   F   = sum_a wex_a sum_(+-) m_nbr + DMI(nbr) + cz + cd (h_i - K0 m_i)
+//   dE  = -(m' - m).F - can[(m'.u)^2 - (m.u)^2] - cd/2 [m'K0m' - mK0m]   (units of kT)
+//   accept when dE <= 0 or u < exp(-dE)
+// with (u0, u1, u) = Philox4x32-10(key = seed; counter = (i, sweep, stage, 0)),
+// m' = (sqrt(1-z^2) cos 2 pi u1, sqrt(1-z^2) sin 2 pi u1, z = 2 u0 - 1).
+template <typename T>
+struct Prop;
+
+template <>
+struct Prop<double> {
+  __device__ static void draw(mmcm::u32x4 r, double& px, double& py, double& pz, double& ua) {
+    pz = 2.0 * mmcm::u01_f64(r.x) - 1.0;
+    double t = 1.0 - pz * pz;
+    if (t < 0) t = 0;
+    double s = mmcm::dsqrt(t), sn, cs;
+    mmcm::sincospi(2.0 * mmcm::u01_f64(r.y), &sn, &cs);
+    px = s * cs;
+    py = s * sn;
+    ua = mmcm::u01_f64(r.z);
+  }
+  __device__ static bool accept(double dE, double ua) { return dE <= 0.0 || ua < mmcm::exp(-dE); }
+};
+
+template <>
+struct Prop<float> {
+  __device__ static void draw(mmcm::u32x4 r, float& px, float& py, float& pz, float& ua) {
+    pz = 2.0f * mmcm::u01_f32(r.x) - 1.0f;
+    float s = sqrtf(fmaxf(0.0f, 1.0f - pz * pz)), sn, cs;
+    sincospif(2.0f * mmcm::u01_f32(r.y), &sn, &cs);
+    px = s * cs;
+    py = s * sn;
+    ua = mmcm::u01_f32(r.z);
+  }
+  __device__ static bool accept(float dE, float ua) { return dE <= 0.0f || ua < __expf(-dE); }
+};
+
+template <typename T>
+__device__ __forceinline__ bool mc_trial(const Geom& g, const McCoef<T>& c, T* __restrict__ m,
+                                         const T* __restrict__ h, uint32_t stage, uint32_t sweep, int x, int y,
+                                         int z) {
+  const long long n = g.n;
+  T* mx = m;
+  T* my = m + n;
+  T* mz = m + 2 * n;
+  const long long i = x + (long long)g.nx * (y + (long long)g.ny * z);
+  T Fx = 0, Fy = 0, Fz = 0;
+  long long nb[3][2];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    nb[a][0] = nbr_idx(g, x, y, z, a, -1);
+    nb[a][1] = nbr_idx(g, x, y, z, a, 1);
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const long long j = nb[a][s];
+      if (j < 0) continue;
+      Fx = Fx + c.wex[a] * mx[j];
+      Fy = Fy + c.wex[a] * my[j];
+      Fz = Fz + c.wex[a] * mz[j];
+    }
+  }
+  const long long xm = nb[0][0], xp = nb[0][1], ym = nb[1][0], yp = nb[1][1];
+  const T dxmz = (xp >= 0 ? mz[xp] : (T)0) - (xm >= 0 ? mz[xm] : (T)0);
+  const T dxmx = (xp >= 0 ? mx[xp] : (T)0) - (xm >= 0 ? mx[xm] : (T)0);
+  const T dymz = (yp >= 0 ? mz[yp] : (T)0) - (ym >= 0 ? mz[ym] : (T)0);
+  const T dymy = (yp >= 0 ? my[yp] : (T)0) - (ym >= 0 ? my[ym] : (T)0);
+  Fx = Fx + c.wdm[0] * dxmz;
+  Fy = Fy + c.wdm[1] * dymz;
+  Fz = Fz - (c.wdm[0] * dxmx + c.wdm[1] * dymy);
+  Fx = Fx + c.cz[0];
+  Fy = Fy + c.cz[1];
+  Fz = Fz + c.cz[2];
+  const T ox = mx[i], oy = my[i], oz = mz[i];
+  if (c.cd != (T)0) {
+    const T sx = c.k0[0] * ox + c.k0[1] * oy + c.k0[2] * oz;
+    const T sy = c.k0[1] * ox + c.k0[3] * oy + c.k0[4] * oz;
+    const T sz = c.k0[2] * ox + c.k0[4] * oy + c.k0[5] * oz;
+    Fx = Fx + c.cd * (h[i] - sx);
+    Fy = Fy + c.cd * (h[n + i] - sy);
+    Fz = Fz + c.cd * (h[2 * n + i] - sz);
+  }
+  mmcm::u32x4 ctr = {(uint32_t)i, sweep, stage, mmcm::STREAM_SWEEP};
+  mmcm::u32x4 r = mmcm::philox4x32_10(ctr, c.key0, c.key1);
+  T px, py, pz, ua;
+  Prop<T>::draw(r, px, py, pz, ua);
+  const T ddx = px - ox, ddy = py - oy, ddz = pz - oz;
+  T dE = -(ddx * Fx + ddy * Fy + ddz * Fz);
+  const T pun = px * c.u[0] + py * c.u[1] + pz * c.u[2];
+  const T puo = ox * c.u[0] + oy * c.u[1] + oz * c.u[2];
+  dE = dE - c.can * (pun * pun - puo * puo);
+  if (c.cd != (T)0) {
+    const T qn = px * (c.k0[0] * px + c.k0[1] * py + c.k0[2] * pz) + py * (c.k0[1] * px + c.k0[3] * py + c.k0[4] * pz) +
+                 pz * (c.k0[2] * px + c.k0[4] * py + c.k0[5] * pz);
+    const T qo = ox * (c.k0[0] * ox + c.k0[1] * oy + c.k0[2] * oz) + oy * (c.k0[1] * ox + c.k0[3] * oy + c.k0[4] * oz) +
+                 oz * (c.k0[2] * ox + c.k0[4] * oy + c.k0[5] * oz);
+    dE = dE - (T)0.5 * c.cd * (qn - qo);
+  }
+  if (Prop<T>::accept(dE, ua)) {
+    mx[i] = px;
+    my[i] = py;
+    mz[i] = pz;
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void count_accepts(bool acc, unsigned long long* counter) {
+  const unsigned mask = __ballot_sync(0xffffffffu, acc);
+  if ((threadIdx.x & 31) == 0 && mask) atomicAdd(counter, (unsigned long long)__popc(mask));
+}
+
+// Two-colour checkerboard: thread t -> row t / hxc, x = 2 (t mod hxc) + parity.
+template <typename T>
+__global__ void k_mc_checker(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
+                             const SweepCounters* __restrict__ ctr, int color, unsigned long long* acc) {
+  const McCoef<T> c = *cp;
+  const int hxc = (g.nx + 1) >> 1;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long nrows = (long long)g.ny * g.nz;
+  bool accepted = false;
+  if (t < nrows * hxc) {
+    const int row = (int)(t / hxc);
+    const int j = (int)(t - (long long)row * hxc);
+    const int y = row % g.ny, z = row / g.ny;
+    const int x = 2 * j + ((color + y + z) & 1);
+    if (x < g.nx) accepted = mc_trial<T>(g, c, m, h, ctr->stage, ctr->sweep, x, y, z);
+  }
+  count_accepts(accepted, acc);
+}
+
+// General colouring (odd periodic axes): every thread tests its cell's colour.
+template <typename T>
+__global__ void k_mc_general(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
+                             const SweepCounters* __restrict__ ctr, int color, unsigned long long* acc) {
+  const McCoef<T> c = *cp;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool accepted = false;
+  if (i < g.n) {
+    const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
+    if (cell_color(g, x, y, z) == color) accepted = mc_trial<T>(g, c, m, h, ctr->stage, ctr->sweep, x, y, z);
+  }
+  count_accepts(accepted, acc);
+}
+
+// =========================================================== energy
+// Per-cell energies in FP64 whatever T is (calEnergyKernel,
+// src/effective_H.h:35-43, + thrust::reduce, src/main.cu:945-948), reduced
+// per block in a fixed order; a second single-block kernel sums the blocks.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_energy(Geom g, EnCoef e, const T* __restrict__ m, const T* __restrict__ h,
+                                                double* __restrict__ partials) {
+  __shared__ double red[NQ][8];
+  const long long n = g.n;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double q[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) q[k] = 0;
+  if (i < n) {
+    const T* mx = m;
+    const T* my = m + n;
+    const T* mz = m + 2 * n;
+    const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
+    const double ax = mx[i], ay = my[i], az = mz[i];
+    for (int a = 0; a < 3; ++a) {
+      const long long j = nbr_idx(g, x, y, z, a, 1);
+      if (j < 0) continue;
+      const double ddx = (double)mx[j] - ax, ddy = (double)my[j] - ay, ddz = (double)mz[j] - az;
+      q[0] += e.aexV_d2[a] * (ddx * ddx + ddy * ddy + ddz * ddz);
+    }
+    const long long xp = nbr_idx(g, x, y, z, 0, 1), xm = nbr_idx(g, x, y, z, 0, -1);
+    const long long yp = nbr_idx(g, x, y, z, 1, 1), ym = nbr_idx(g, x, y, z, 1, -1);
+    const double dxmz = (xp >= 0 ? (double)mz[xp] : 0.0) - (xm >= 0 ? (double)mz[xm] : 0.0);
+    const double dxmx = (xp >= 0 ? (double)mx[xp] : 0.0) - (xm >= 0 ? (double)mx[xm] : 0.0);
+    const double dymz = (yp >= 0 ? (double)mz[yp] : 0.0) - (ym >= 0 ? (double)mz[ym] : 0.0);
+    const double dymy = (yp >= 0 ? (double)my[yp] : 0.0) - (ym >= 0 ? (double)my[ym] : 0.0);
+    q[1] = -(ax * e.dV_2d[0] * dxmz + ay * e.dV_2d[1] * dymz - az * (e.dV_2d[0] * dxmx + e.dV_2d[1] * dymy));
+    const double mu = ax * e.u[0] + ay * e.u[1] + az * e.u[2];
+    q[2] = -e.kuV * mu * mu;
+    q[3] = -(ax * e.msVB[0] + ay * e.msVB[1] + az * e.msVB[2]);
+    if (e.demag != 0.0 && h)
+      q[4] = -e.demag * (ax * (double)h[i] + ay * (double)h[n + i] + az * (double)h[2 * n + i]);
+    q[5] = ax;
+    q[6] = ay;
+    q[7] = az;
+    const long long i2 = nbr_idx(g, x, y, z, 0, 1);
+    const long long i4 = nbr_idx(g, x, y, z, 1, 1);
+    if (i2 >= 0 && i4 >= 0) {
+      const int x2 = (int)(i2 % g.nx);
+      const long long i3 = nbr_idx(g, x2, y, z, 1, 1);
+      const long long tri[2][3] = {{i, i2, i3}, {i, i3, i4}};
+      for (int t = 0; t < 2; ++t) {
+        const long long a = tri[t][0], b = tri[t][1], cc = tri[t][2];
+        const double pax = mx[a], pay = my[a], paz = mz[a];
+        const double pbx = mx[b], pby = my[b], pbz = mz[b];
+        const double pcx = mx[cc], pcy = my[cc], pcz = mz[cc];
+        const double trip =
+            pax * (pby * pcz - pbz * pcy) + pay * (pbz * pcx - pbx * pcz) + paz * (pbx * pcy - pby * pcx);
+        const double den = 1.0 + (pax * pbx + pay * pby + paz * pbz) + (pbx * pcx + pby * pcy + pbz * pcz) +
+                           (pcx * pax + pcy * pay + pcz * paz);
+        q[8] += 2.0 * atan2(trip, den);
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) {
+    const double v = warp_sum(q[k]);
+    if (lane == 0) red[k][warp] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    double s = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+    partials[(long long)blockIdx.x * NQ + threadIdx.x] = s;
+  }
+}
+
+static __global__ void __launch_bounds__(256) k_reduce_partials(const double* __restrict__ partials, int nblocks,
+                                                         double* __restrict__ out) {
+  __shared__ double red[NQ][8];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = 0; k < NQ; ++k) {
+    double s = 0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partials[(long long)b * NQ + k];
+    s = warp_sum(s);
+    if (lane == 0) red[k][warp] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < NQ) {
+    double s = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
+    out[threadIdx.x] = s;
+  }
+}
+
+// =========================================================== effective field
+// Per-term H in A/m (the DEBUG_H_FIELD dumps of src/main.cu:965-1086).
+template <typename T>
+__global__ void k_field(Geom g, HCoef c, int term, const T* __restrict__ m, const T* __restrict__ h,
+                        double* __restrict__ out) {
+  const long long n = g.n;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const T* mx = m;
+  const T* my = m + n;
+  const T* mz = m + 2 * n;
+  const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
+  const double ax = mx[i], ay = my[i], az = mz[i];
+  double f0 = 0, f1 = 0, f2 = 0;
+  const bool all = term == 5;
+  if (term == 0 || all) {
+    for (int a = 0; a < 3; ++a)
+      for (int dir = -1; dir <= 1; dir += 2) {
+        const long long j = nbr_idx(g, x, y, z, a, dir);
+        if (j < 0) continue;
+        f0 += c.ex_d2[a] * ((double)mx[j] - ax);
+        f1 += c.ex_d2[a] * ((double)my[j] - ay);
+        f2 += c.ex_d2[a] * ((double)mz[j] - az);
+      }
+  }
+  if (term == 1 || all) {
+    const long long xp = nbr_idx(g, x, y, z, 0, 1), xm = nbr_idx(g, x, y, z, 0, -1);
+    const long long yp = nbr_idx(g, x, y, z, 1, 1), ym = nbr_idx(g, x, y, z, 1, -1);
+    const double dxmz = (xp >= 0 ? (double)mz[xp] : 0.0) - (xm >= 0 ? (double)mz[xm] : 0.0);
+    const double dxmx = (xp >= 0 ? (double)mx[xp] : 0.0) - (xm >= 0 ? (double)mx[xm] : 0.0);
+    const double dymz = (yp >= 0 ? (double)mz[yp] : 0.0) - (ym >= 0 ? (double)mz[ym] : 0.0);
+    const double dymy = (yp >= 0 ? (double)my[yp] : 0.0) - (ym >= 0 ? (double)my[ym] : 0.0);
+    f0 += c.dm_2d[0] * dxmz;
+    f1 += c.dm_2d[1] * dymz;
+    f2 += -(c.dm_2d[0] * dxmx + c.dm_2d[1] * dymy);
+  }
+  if (term == 2 || all) {
+    const double mu = ax * c.u[0] + ay * c.u[1] + az * c.u[2];
+    f0 += c.an * mu * c.u[0];
+    f1 += c.an * mu * c.u[1];
+    f2 += c.an * mu * c.u[2];
+  }
+  if (term == 3 || all) {
+    f0 += c.b[0];
+    f1 += c.b[1];
+    f2 += c.b[2];
+  }
+  if ((term == 4 || all) && c.ms != 0.0 && h) {
+    f0 += c.ms * (double)h[i];
+    f1 += c.ms * (double)h[n + i];
+    f2 += c.ms * (double)h[2 * n + i];
+  }
+  out[i] = f0;
+  out[n + i] = f1;
+  out[2 * n + i] = f2;
+}
+
+// =========================================================== init / utility
+// Uniform directions from Philox(key = seed; counter = (i, 0, 0, STREAM_INIT)),
+// computed in FP64 and rounded to T (replaces randInitMx, src/mx_init.h:21-97).
+template <typename T>
+__global__ void k_init(long long n, uint32_t k0, uint32_t k1, T* __restrict__ m) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  mmcm::u32x4 ctr = {(uint32_t)i, 0u, 0u, mmcm::STREAM_INIT};
+  mmcm::u32x4 r = mmcm::philox4x32_10(ctr, k0, k1);
+  double z = 2.0 * mmcm::u01_f64(r.x) - 1.0;
+  double t = 1.0 - z * z;
+  if (t < 0) t = 0;
+  double s = mmcm::dsqrt(t), sn, cs;
+  mmcm::sincospi(2.0 * mmcm::u01_f64(r.y), &sn, &cs);
+  m[i] = (T)(s * cs);
+  m[n + i] = (T)(s * sn);
+  m[2 * n + i] = (T)z;
+}
+
+template <typename T>
+__global__ void k_from_f64(long long n, const double* __restrict__ src, T* __restrict__ dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (T)src[i];
+}
+template <typename T>
+__global__ void k_to_f64(long long n, const T* __restrict__ src, double* __restrict__ dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = (double)src[i];
+}
+template <typename T>
+__global__ void k_khat_store(long long count, const double2* __restrict__ src, C<T>* __restrict__ dst) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dst[i] = cmk<C<T>>((T)src[i].x, (T)src[i].y);
+}
+
+// =========================================================== host launchers
+#define MMC_TRY_ATTR(x)                  \
+  do {                                   \
+    cudaError_t e_ = (x);                \
+    if (e_ != cudaSuccess) return e_;    \
+  } while (0)
+inline size_t x_pass_smem(const FftPlan& p, int lines_per_row, int rows, size_t csize) {
+  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)rows * lines_per_row * p.n) * csize;
+}
+inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize) {
+  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)ncomp * tx * (p.n + 1)) * csize;
+}
+
+// Raises the dynamic shared-memory limit of the FFT pass kernels to the
+// device's opt-in maximum.  Called once per device at handle creation, never
+// inside a stream capture.
+template <typename T>
+cudaError_t prepare_impl(int max_dyn_smem) {
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_x_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    max_dyn_smem));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_x_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    max_dyn_smem));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_col_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    max_dyn_smem));
+  return cudaSuccess;
+}
+
+template <typename T>
+cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int nrows, const T* in,
+                          long long in_cstride, C<T>* S, long long nspec, int nyp, int hx, int rpc, int threads,
+                          cudaStream_t st) {
+  const int lines = (ncomp + 1) / 2;
+  size_t sm = x_pass_smem(p, lines, rpc, sizeof(C<T>));
+  dim3 grid((nrows + rpc - 1) / rpc);
+  k_x_forward<T><<<grid, threads, sm, st>>>(p, ncomp, xdata, ydata, nrows, in, in_cstride, S, nspec, nyp, hx, rpc);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, const C<T>* khat, int hx,
+                         int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
+                         int flags, T inv_n, int tx, int threads, cudaStream_t st) {
+  size_t sm = col_pass_smem(p, ncomp, tx, sizeof(C<T>));
+  dim3 grid((hx + tx - 1) / tx, planes);
+  k_col_pass<T><<<grid, threads, sm, st>>>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
+                                           store_lim, flags, inv_n, tx);
+  return cudaGetLastError();
+}
+
+#define MMC_TRY(x)                       \
+  do {                                   \
+    cudaError_t e_ = (x);                \
+    if (e_ != cudaSuccess) return e_;    \
+  } while (0)
+
+template <typename T>
+cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
+                       const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st) {
+  C<T>* S = reinterpret_cast<C<T>*>(spec);
+  const C<T>* K = reinterpret_cast<const C<T>*>(khat);
+  const long long ns = g.nspec;
+  const T inv_n = (T)(1.0 / (double)g.np);
+  const int rows = g.ny * g.nz;
+  MMC_TRY(run_x_forward<T>(px, 3, g.nx, g.ny, rows, m, g.n, S, ns, g.nyp, g.hx, tun.x_rows_per_cta, tun.x_threads,
+                           st));
+  const long long ystride = g.hx, yplane = (long long)g.nyp * g.hx;
+  if (g.nzp == 1) {
+    MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV,
+                            inv_n, tun.col_tx, tun.col_threads, st));
+  } else {
+    MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.ny, g.nyp, PASS_FWD, inv_n, tun.col_tx,
+                            tun.col_threads, st));
+    MMC_TRY(run_col_pass<T>(pz, 3, S, ns, K, g.hx, g.nyp, ystride, yplane, g.nz, g.nz,
+                            PASS_FWD | PASS_MUL | PASS_INV, inv_n, tun.col_tx_z, tun.col_threads, st));
+    MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.nyp, g.ny, PASS_INV, inv_n, tun.col_tx,
+                            tun.col_threads, st));
+  }
+  const int rpc = tun.x_rows_per_cta;
+  size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
+  k_x_inverse<T><<<(rows + rpc - 1) / rpc, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.nx, g.ny, rows, h, g.n,
+                                                                    rpc);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
+                    unsigned long long* acc, cudaStream_t st) {
+  const int threads = 256;
+  if (g.ncolors == 2) {
+    const long long total = (long long)g.ny * g.nz * ((g.nx + 1) / 2);
+    k_mc_checker<T><<<(unsigned)((total + threads - 1) / threads), threads, 0, st>>>(g, c, m, h, ctr, color, acc);
+  } else {
+    k_mc_general<T><<<(unsigned)((g.n + threads - 1) / threads), threads, 0, st>>>(g, c, m, h, ctr, color, acc);
+  }
+  return cudaGetLastError();
+}
+
+inline int energy_blocks(const Geom& g) { return (int)((g.n + 255) / 256); }
+
+template <typename T>
+cudaError_t energy_impl(const Geom& g, const EnCoef& e, const T* m, const T* h, double* partials, int npartials,
+                        double* out, cudaStream_t st) {
+  const int nb = energy_blocks(g);
+  if (nb > npartials) return cudaErrorInvalidValue;
+  k_energy<T><<<nb, 256, 0, st>>>(g, e, m, h, partials);
+  MMC_TRY(cudaGetLastError());
+  k_reduce_partials<<<1, 256, 0, st>>>(partials, nb, out);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t field_impl(const Geom& g, const HCoef& c, int term, const T* m, const T* h, double* out,
+                       cudaStream_t st) {
+  k_field<T><<<(unsigned)((g.n + 255) / 256), 256, 0, st>>>(g, c, term, m, h, out);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t init_impl(const Geom& g, uint64_t seed, T* m, cudaStream_t st) {
+  k_init<T><<<(unsigned)((g.n + 255) / 256), 256, 0, st>>>(g.n, (uint32_t)(seed & 0xffffffffu),
+                                                          (uint32_t)(seed >> 32), m);
+  return cudaGetLastError();
+}
+
+// ----------------------------------------------------------- launcher bodies
+// Explicitly instantiated for float in kernels_f32.cu and for double in kernels_f64.cu.
+template <typename T>
+cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
+                         const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat,
+                         cudaStream_t st) {
+  return demag_impl<T>(g, px, py, pz, tun, m, h, spec, khat, st);
+}
+template <typename T>
+cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
+                      unsigned long long* acc, cudaStream_t st) {
+  return mc_impl<T>(g, c, m, h, ctr, color, acc, st);
+}
+template <typename T>
+cudaError_t launch_energy(const Geom& g, const EnCoef& e, const T* m, const T* h, double* partials, int npartials,
+                          double* out, cudaStream_t st) {
+  return energy_impl<T>(g, e, m, h, partials, npartials, out, st);
+}
+template <typename T>
+cudaError_t launch_field(const Geom& g, const HCoef& c, int term, const T* m, const T* h, double* out,
+                         cudaStream_t st) {
+  return field_impl<T>(g, c, term, m, h, out, st);
+}
+template <typename T>
+cudaError_t launch_init(const Geom& g, uint64_t seed, T* m, cudaStream_t st) {
+  return init_impl<T>(g, seed, m, st);
+}
+template <typename T>
+cudaError_t launch_prepare(int max_dyn_smem) {
+  return prepare_impl<T>(max_dyn_smem);
+}
+template <typename T>
+cudaError_t launch_from_f64(long long count, const double* src, T* dst, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  k_from_f64<T><<<(unsigned)((count + 255) / 256), 256, 0, st>>>(count, src, dst);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_to_f64(long long count, const T* src, double* dst, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  k_to_f64<T><<<(unsigned)((count + 255) / 256), 256, 0, st>>>(count, src, dst);
+  return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat, cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  k_khat_store<T><<<(unsigned)((count + 255) / 256), 256, 0, st>>>(count, spec64, reinterpret_cast<C<T>*>(khat));
+  return cudaGetLastError();
+}
+
+#define MMC_INSTANTIATE_LAUNCHERS(T)                                                                          \
+  template cudaError_t launch_demag<T>(const Geom&, const FftPlan&, const FftPlan&, const FftPlan&,           \
+                                       const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t);   \
+  template cudaError_t launch_mc<T>(const Geom&, const McCoef<T>*, T*, const T*, const SweepCounters*, int,   \
+                                    unsigned long long*, cudaStream_t);                                       \
+  template cudaError_t launch_energy<T>(const Geom&, const EnCoef&, const T*, const T*, double*, int, double*, \
+                                        cudaStream_t);                                                         \
+  template cudaError_t launch_field<T>(const Geom&, const HCoef&, int, const T*, const T*, double*,            \
+                                       cudaStream_t);                                                          \
+  template cudaError_t launch_init<T>(const Geom&, uint64_t, T*, cudaStream_t);                               \
+  template cudaError_t launch_prepare<T>(int);                                                                \
+  template cudaError_t launch_from_f64<T>(long long, const double*, T*, cudaStream_t);                        \
+  template cudaError_t launch_to_f64<T>(long long, const T*, double*, cudaStream_t);                          \
+  template cudaError_t launch_khat_store<T>(long long, const double2*, void*, cudaStream_t);
+
+}  // namespace mmc

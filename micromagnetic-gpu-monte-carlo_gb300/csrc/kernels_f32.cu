@@ -1,0 +1,7 @@
+// kernels_f32.cu -- FP32 instantiation of the hot-path kernels (multiply-add
+// contraction enabled).
+#include "kernels.cuh"
+
+namespace mmc {
+MMC_INSTANTIATE_LAUNCHERS(float)
+}  // namespace mmc

@@ -1,0 +1,131 @@
+// mmc_internal.h -- structures shared by the host runtime and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mmc {
+
+constexpr int FFT_MAX_STAGES = 24;
+constexpr int FFT_MAX_RADIX = 31;  // largest prime factor an FFT length may have
+
+// Mixed-radix Stockham plan for one transform length.  Stage s has radix
+// radix[s] and ns[s] = product of the earlier radices.  Twiddles of stage s
+// live at tw_off[s]: entry (t-1)*ns + k = exp(-2 pi i t k / (ns*radix)) for
+// t in [1, radix), k in [0, ns); the radix-th roots of unity exp(-2 pi i m /
+// radix) live at root_off[s].
+struct FftPlan {
+  int n;
+  int nstages;
+  int radix[FFT_MAX_STAGES];
+  int ns[FFT_MAX_STAGES];
+  int tw_off[FFT_MAX_STAGES];
+  int root_off[FFT_MAX_STAGES];
+  int tw_total;
+  const double2* tw64;
+  const float2* tw32;
+};
+
+// Lattice geometry.  Cell i = x + nx*(y + ny*z).  The padded grid (nxp, nyp,
+// nzp) follows src/main.cu:254-263 of the reference.  The spectrum keeps the
+// kx half-axis: hx = nxp/2 + 1, layout [comp][kz][ky][kx], nspec = hx*nyp*nzp.
+struct Geom {
+  int nx, ny, nz;
+  int nxp, nyp, nzp;
+  int hx;
+  int per[3];      // periodic neighbours on this axis (pbc != 0)
+  int ncolors;     // 2, or 3 when a periodic axis has odd length
+  long long n;     // nx*ny*nz
+  long long np;    // nxp*nyp*nzp
+  long long nspec; // hx*nyp*nzp
+};
+
+// Metropolis coefficients, all in units of kT (see the sweep kernel).
+template <typename T>
+struct McCoef {
+  T wex[3];   // 2 Aex V / (d_a^2 kT)
+  T wdm[2];   // Dind V / (d_a kT), a = x, y
+  T can;      // Ku1 V / kT
+  T u[3];     // anisotropy axis (unit)
+  T cz[3];    // Ms V B / kT
+  T cd;       // mu0 Ms^2 V / kT, 0 when demag is off
+  T k0[6];    // self tensor xx, xy, xz, yy, yz, zz
+  uint32_t key0, key1;  // Philox key = seed
+};
+
+// Energy prefactors (SI, J).
+struct EnCoef {
+  double aexV_d2[3];  // Aex V / d_a^2
+  double dV_2d[2];    // Dind V / (2 d_a)
+  double kuV;         // Ku1 V
+  double u[3];
+  double msVB[3];     // Ms V B
+  double demag;       // mu0 Ms^2 V / 2, 0 when demag is off
+};
+
+// Effective-field prefactors (A/m).
+struct HCoef {
+  double ex_d2[3];  // 2 Aex / (mu0 Ms d_a^2)
+  double dm_2d[2];  // 2 Dind / (mu0 Ms) / (2 d_a)
+  double an;        // 2 Ku1 / (mu0 Ms)
+  double u[3];
+  double b[3];      // B / mu0
+  double ms;        // Ms, 0 when demag is off
+};
+
+// Number of reduced quantities produced by the energy kernel:
+// E_ex, E_dmi, E_an, E_zeeman, E_demag, sum mx, sum my, sum mz, sum solid angle.
+constexpr int NQ = 9;
+
+// Launch shapes chosen by the host (autotuned).
+struct DemagTuning {
+  int x_rows_per_cta;
+  int x_threads;
+  int col_tx;      // kx columns per tile in the y pass
+  int col_tx_z;    // kx columns per tile in the z pass
+  int col_threads;
+};
+
+// Device counters read by the sweep kernels: [stage, sweep].
+struct SweepCounters {
+  uint32_t stage;
+  uint32_t sweep;
+};
+
+// ------------------------------------------------------------- launchers
+// Implemented in kernels_f32.cu / kernels_f64.cu (T = float / double) and newell.cu.
+template <typename T>
+cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
+                         const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat,
+                         cudaStream_t st);
+template <typename T>
+cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr,
+                      int color, unsigned long long* acc, cudaStream_t st);
+template <typename T>
+cudaError_t launch_energy(const Geom& g, const EnCoef& e, const T* m, const T* h, double* partials,
+                          int npartials, double* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_field(const Geom& g, const HCoef& c, int term, const T* m, const T* h, double* out,
+                         cudaStream_t st);
+template <typename T>
+cudaError_t launch_init(const Geom& g, uint64_t seed, T* m, cudaStream_t st);
+template <typename T>
+cudaError_t launch_prepare(int max_dyn_smem);
+template <typename T>
+cudaError_t launch_from_f64(long long count, const double* src, T* dst, cudaStream_t st);
+template <typename T>
+cudaError_t launch_to_f64(long long count, const T* src, double* dst, cudaStream_t st);
+template <typename T>
+cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat, cudaStream_t st);
+
+// FP64 setup: the Newell tensor (newell.cu) and its forward transform.
+cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz,
+                          double pi, double* k6, int px0, int px1, int finalize, cudaStream_t st);
+cudaError_t launch_tensor_fft(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
+                              const DemagTuning& tun, const double* k6, double2* spec64, cudaStream_t st);
+cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st);
+cudaError_t launch_philox_selftest(long long n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out,
+                                   uint32_t* out_curand, cudaStream_t st);
+
+int energy_partials_count(const Geom& g);
+
+}  // namespace mmc

@@ -1,0 +1,129 @@
+// newell.cu -- FP64 Newell demag tensor with periodic images.
+//
+// The reference declares ktensorKernel2_step1 / _step2_div_const
+// (src/demag_cu.h:20-28) without publishing their bodies; its complete CPU
+// version is ktensorcpu::ktensorCPU (src/demag_cu.cu:119-248), which this
+// kernel follows term for term: for each padded grid point the wrapped signed
+// offset (:149-151), the image loops over [-max(pbc,0), max(pbc,0)] per axis
+// (as the GPU orchestration src/main.cu:475-491 does), the 64 parity-signed
+// evaluations of the f / g potentials of src/demag_cu.h:43-71 with the
+// component argument permutations (:190-210), and the division by
+// -4 pi dx dy dz (:221-228).  One thread owns one grid point and accumulates
+// in the reference's order.  Elementary functions come from mmc_math.h and
+// this file is compiled with -fmad=false, so the result is bit-identical to
+// the CPU oracle's.
+#include <cuda_runtime.h>
+
+#include "mmc_internal.h"
+#include "mmc_math.h"
+
+namespace mmc {
+
+namespace {
+
+__device__ __forceinline__ double absv(double x) { return x > 0 ? x : -x; }
+
+__device__ __forceinline__ double newell_f(double x, double y, double z) {
+  const double EPS = 1e-200;
+  x = absv(x);
+  y = absv(y);
+  z = absv(z);
+  const double R = mmcm::dsqrt(x * x + y * y + z * z);
+  const double t1 = y / 2.0 * (z * z - x * x) * mmcm::asinh(y / (mmcm::dsqrt(x * x + z * z) + EPS));
+  const double t2 = z / 2.0 * (y * y - x * x) * mmcm::asinh(z / (mmcm::dsqrt(x * x + y * y) + EPS));
+  const double t3 = x * y * z * mmcm::atan(y * z / (x * R + EPS));
+  const double t4 = 1.0 / 6.0 * (2 * x * x - y * y - z * z) * R;
+  return t1 + t2 - t3 + t4;
+}
+
+__device__ __forceinline__ double newell_g(double x, double y, double z) {
+  const double EPS = 1e-200;
+  z = absv(z);
+  const double R = mmcm::dsqrt(x * x + y * y + z * z);
+  const double t1 = x * y * z * mmcm::asinh(z / (mmcm::dsqrt(x * x + y * y) + EPS));
+  const double t2 = y / 6.0 * (3.0 * z * z - y * y) * mmcm::asinh(x / (mmcm::dsqrt(y * y + z * z) + EPS));
+  const double t3 = x / 6.0 * (3.0 * z * z - x * x) * mmcm::asinh(y / (mmcm::dsqrt(x * x + z * z) + EPS));
+  const double t4 = z * z * z / 6.0 * mmcm::atan(x * y / (z * R + EPS));
+  const double t5 = z * y * y / 2.0 * mmcm::atan(x * z / (y * R + EPS));
+  const double t6 = z * x * x / 2.0 * mmcm::atan(y * z / (x * R + EPS));
+  const double t7 = x * y * R / 3.0;
+  return t1 + t2 + t3 - t4 - t5 - t6 - t7;
+}
+
+__device__ __forceinline__ int wrap_offset(int x, int n) { return (x + (n + 1) / 2 - 1) % n - (n + 1) / 2 + 1; }
+
+// Adds images px in [px0, px1] (all py, pz) to the running sums of every
+// point.  The sums live in k6 between launches, so splitting the image range
+// over several launches keeps the reference's summation order exactly; the
+// launch with `finalize` divides by -4 pi dx dy dz.
+__global__ void __launch_bounds__(128) k_newell(int nxp, int nyp, int nzp, double dx, double dy, double dz, int Px,
+                                                int Py, int Pz, int px0, int px1, int finalize, double pi,
+                                                double* __restrict__ k6, long long np) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const int x = (int)(i % nxp), y = (int)((i / nxp) % nyp), z = (int)(i / ((long long)nxp * nyp));
+  const int idx_x = wrap_offset(x, nxp), idx_y = wrap_offset(y, nyp), idx_z = wrap_offset(z, nzp);
+  double kxx = 0, kxy = 0, kxz = 0, kyy = 0, kyz = 0, kzz = 0;
+  if (px0 > -Px) {
+    kxx = k6[i];
+    kxy = k6[np + i];
+    kxz = k6[2 * np + i];
+    kyy = k6[3 * np + i];
+    kyz = k6[4 * np + i];
+    kzz = k6[5 * np + i];
+  }
+  for (int px = px0; px <= px1; px++)
+    for (int py = -Py; py <= Py; py++)
+      for (int pz = -Pz; pz <= Pz; pz++) {
+        const int ix = idx_x + px * nxp, iy = idx_y + py * nyp, iz = idx_z + pz * nzp;
+#pragma unroll 1
+        for (int bits = 0; bits < 64; ++bits) {
+          // bit order matches the nested FOR01 loops ikx, iky, ikz, ilx, ily, ilz
+          const int ikx = (bits >> 5) & 1, iky = (bits >> 4) & 1, ikz = (bits >> 3) & 1;
+          const int ilx = (bits >> 2) & 1, ily = (bits >> 1) & 1, ilz = bits & 1;
+          const int iix = ix + ikx - ilx, iiy = iy + iky - ily, iiz = iz + ikz - ilz;
+          const bool sign = ((ikx + iky + ikz + ilx + ily + ilz) % 2 == 0);
+          const double X = iix * dx, Y = iiy * dy, Z = iiz * dz;
+          double v;
+          v = newell_f(X, Y, Z);
+          kxx += sign ? v : -v;
+          v = newell_g(X, Y, Z);
+          kxy += sign ? v : -v;
+          v = newell_g(X, Z, Y);
+          kxz += sign ? v : -v;
+          v = newell_f(Y, Z, X);
+          kyy += sign ? v : -v;
+          v = newell_g(Y, Z, X);
+          kyz += sign ? v : -v;
+          v = newell_f(Z, X, Y);
+          kzz += sign ? v : -v;
+        }
+      }
+  if (finalize) {
+    const double d = -pi * 4.0 * dx * dy * dz;
+    kxx = kxx / d;
+    kxy = kxy / d;
+    kxz = kxz / d;
+    kyy = kyy / d;
+    kyz = kyz / d;
+    kzz = kzz / d;
+  }
+  k6[i] = kxx;
+  k6[np + i] = kxy;
+  k6[2 * np + i] = kxz;
+  k6[3 * np + i] = kyy;
+  k6[4 * np + i] = kyz;
+  k6[5 * np + i] = kzz;
+}
+
+}  // namespace
+
+cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz, double pi,
+                          double* k6, int px0, int px1, int finalize, cudaStream_t st) {
+  const int threads = 128;
+  k_newell<<<(unsigned)((g.np + threads - 1) / threads), threads, 0, st>>>(g.nxp, g.nyp, g.nzp, dx, dy, dz, Px, Py,
+                                                                          Pz, px0, px1, finalize, pi, k6, g.np);
+  return cudaGetLastError();
+}
+
+}  // namespace mmc

@@ -1,0 +1,1039 @@
+// runtime.cpp -- the C ABI of include/mmc.h: device state of one lattice,
+// demag tensor build and cache, sweeps (captured in CUDA graphs) and the
+// temperature-stage loop of the reference's main() (src/main.cu:801-1139).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <string>
+#include <sys/stat.h>
+#include <dirent.h>
+#include <vector>
+
+#include "host_common.h"
+#include "mmc_internal.h"
+
+namespace mmc {
+const char* last_error_cstr();
+}
+
+using namespace mmc;
+
+namespace {
+
+const double kB = 1.3806488e-23;  // src/constant.h:22
+
+double pi_of(const mmc_config* c) { return c->use_reference_pi ? 3.14159265358 : 3.14159265358979323846; }
+
+#define CU(x)                                                                               \
+  do {                                                                                      \
+    cudaError_t e_ = (x);                                                                   \
+    if (e_ != cudaSuccess)                                                                  \
+      return fail(e_ == cudaErrorMemoryAllocation ? MMC_ERR_OOM : MMC_ERR_CUDA,             \
+                  std::string(#x) + ": " + cudaGetErrorString(e_));                         \
+  } while (0)
+
+#define TRY(x)                    \
+  do {                            \
+    int s_ = (x);                 \
+    if (s_ != MMC_OK) return s_;  \
+  } while (0)
+
+// ------------------------------------------------------------------ FFT plans
+struct PlanHost {
+  FftPlan p{};
+  double2* d64 = nullptr;
+  float2* d32 = nullptr;
+};
+
+void unit_root(long long j, long long N, double* c, double* s) {
+  // exp(-2 pi i j / N) from long double trigonometry on the reduced angle
+  j %= N;
+  if (j < 0) j += N;
+  const long double pi = 3.141592653589793238462643383279502884L;
+  long double a = 2.0L * pi * (long double)j / (long double)N;
+  *c = (double)cosl(a);
+  *s = (double)-sinl(a);
+}
+
+int make_plan(int n, PlanHost* ph) {
+  FftPlan& p = ph->p;
+  std::memset(&p, 0, sizeof p);
+  p.n = n;
+  std::vector<int> rad;
+  int m = n;
+  while (m % 4 == 0) rad.push_back(4), m /= 4;
+  while (m % 2 == 0) rad.push_back(2), m /= 2;
+  for (int f = 3; m > 1 && f <= FFT_MAX_RADIX; f += 2)
+    while (m % f == 0) rad.push_back(f), m /= f;
+  if (m > 1)
+    return fail(MMC_ERR_UNSUPPORTED, "FFT length " + std::to_string(n) + " has a prime factor above " +
+                                         std::to_string(FFT_MAX_RADIX));
+  if ((int)rad.size() > FFT_MAX_STAGES) return fail(MMC_ERR_UNSUPPORTED, "FFT length has too many factors");
+  std::vector<double> tw;
+  int ns = 1;
+  for (size_t s = 0; s < rad.size(); ++s) {
+    int R = rad[s];
+    p.radix[s] = R;
+    p.ns[s] = ns;
+    p.tw_off[s] = (int)(tw.size() / 2);
+    for (int t = 1; t < R; ++t)
+      for (int k = 0; k < ns; ++k) {
+        double c, sn;
+        unit_root((long long)t * k, (long long)ns * R, &c, &sn);
+        tw.push_back(c);
+        tw.push_back(sn);
+      }
+    p.root_off[s] = (int)(tw.size() / 2);
+    if (R != 2 && R != 3 && R != 4)
+      for (int q = 0; q < R; ++q) {
+        double c, sn;
+        unit_root(q, R, &c, &sn);
+        tw.push_back(c);
+        tw.push_back(sn);
+      }
+    ns *= R;
+  }
+  p.nstages = (int)rad.size();
+  p.tw_total = (int)(tw.size() / 2);
+  size_t cnt = tw.size() / 2;
+  if (cnt == 0) cnt = 1, tw.push_back(1.0), tw.push_back(0.0);
+  std::vector<float> tw32(tw.size());
+  for (size_t i = 0; i < tw.size(); ++i) tw32[i] = (float)tw[i];
+  CU(cudaMalloc(&ph->d64, cnt * sizeof(double2)));
+  CU(cudaMalloc(&ph->d32, cnt * sizeof(float2)));
+  CU(cudaMemcpy(ph->d64, tw.data(), cnt * sizeof(double2), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(ph->d32, tw32.data(), cnt * sizeof(float2), cudaMemcpyHostToDevice));
+  p.tw64 = ph->d64;
+  p.tw32 = ph->d32;
+  return MMC_OK;
+}
+
+void free_plan(PlanHost* ph) {
+  if (ph->d64) cudaFree(ph->d64);
+  if (ph->d32) cudaFree(ph->d32);
+  ph->d64 = nullptr;
+  ph->d32 = nullptr;
+}
+
+size_t smem_limit() { return 200 * 1024; }
+
+// Launch shapes: enough CTAs to cover 2x the SM count where the shape allows,
+// within the shared-memory budget.
+DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz, size_t csize,
+                          int nsm) {
+  DemagTuning t;
+  const int rows = g.ny * g.nz;
+  auto xsm = [&](int r) {
+    return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize;
+  };
+  int r = 1;
+  while (r < 8 && (rows + 2 * r - 1) / (2 * r) >= 2 * nsm && xsm(2 * r) <= 96 * 1024) r *= 2;
+  t.x_rows_per_cta = r;
+  t.x_threads = px.n >= 512 ? 256 : 128;
+  auto csm = [&](const FftPlan& p, int tx) {
+    return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * (p.n + 1)) * csize;
+  };
+  auto pick = [&](const FftPlan& p, int planes) {
+    int tx = 16;
+    while (tx > 1 && (((long long)(g.hx + tx - 1) / tx) * planes < 2 * nsm || csm(p, tx) > 96 * 1024)) tx /= 2;
+    while (tx > 1 && csm(p, tx) > smem_limit()) tx /= 2;
+    return tx;
+  };
+  t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz);
+  t.col_tx_z = pick(pz, g.nyp);
+  t.col_threads = 256;
+  return t;
+}
+
+}  // namespace
+
+// =================================================================== handle
+struct mmc_handle {
+  mmc_config cfg;
+  int device = 0;
+  int prec = 32;
+  size_t tsize = 4;
+  Geom g{};
+  cudaStream_t st = nullptr;
+  PlanHost px, py, pz;
+  DemagTuning tun{};
+  void* m = nullptr;     // 3n T
+  void* h = nullptr;     // 3n T, dimensionless demag field K*m
+  void* spec = nullptr;  // 3*nspec complex T
+  void* khat = nullptr;  // 6*nspec complex T
+  void* coef = nullptr;  // McCoef<T> in device memory
+  double* partials = nullptr;
+  int npartials = 0;
+  double* red = nullptr;     // NQ doubles, device
+  double* red_host = nullptr;  // NQ doubles, pinned
+  unsigned long long* acc = nullptr;
+  SweepCounters* ctr = nullptr;
+  double* stage64 = nullptr;  // 3n doubles, device (host <-> device staging)
+  double* field64 = nullptr;  // 3n doubles, device
+  bool demag_built = false;
+  double k0[6] = {0, 0, 0, 0, 0, 0};
+  std::vector<double> tensor;  // 6*np, x fastest
+  std::atomic<int> stop{0};
+  unsigned long long proposed = 0;
+  unsigned long long acc_base = 0;
+  // graph of `graph_sweeps` sweeps
+  cudaGraphExec_t gexec = nullptr;
+  int graph_sweeps = 0;
+  long long seed = 0;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  double last_run_ms = 0;
+};
+
+namespace {
+
+int sync_check(mmc_handle* h) {
+  CU(cudaStreamSynchronize(h->st));
+  return MMC_OK;
+}
+
+int set_dev(mmc_handle* h) {
+  CU(cudaSetDevice(h->device));
+  return MMC_OK;
+}
+
+template <typename T>
+McCoef<T> make_mc_coef(const mmc_handle* h, double T_K) {
+  const mmc_config& c = h->cfg;
+  McCoef<T> k;
+  const double kT = kB * T_K;
+  const double V = c.dx * c.dy * c.dz;
+  const double d[3] = {c.dx, c.dy, c.dz};
+  for (int a = 0; a < 3; ++a) k.wex[a] = (T)(2.0 * c.Aex * V / (d[a] * d[a] * kT));
+  k.wdm[0] = (T)(c.Dind * V / (d[0] * kT));
+  k.wdm[1] = (T)(c.Dind * V / (d[1] * kT));
+  k.can = (T)(c.Ku1 * V / kT);
+  double un = std::sqrt(c.anisUx * c.anisUx + c.anisUy * c.anisUy + c.anisUz * c.anisUz);
+  k.u[0] = (T)(un > 0 ? c.anisUx / un : 0);
+  k.u[1] = (T)(un > 0 ? c.anisUy / un : 0);
+  k.u[2] = (T)(un > 0 ? c.anisUz / un : 0);
+  k.cz[0] = (T)(c.ms * V * c.Bextx / kT);
+  k.cz[1] = (T)(c.ms * V * c.Bexty / kT);
+  k.cz[2] = (T)(c.ms * V * c.Bextz / kT);
+  const double mu0 = 4e-7 * pi_of(&c);
+  k.cd = (T)(c.cal_demag_flag ? mu0 * c.ms * c.ms * V / kT : 0.0);
+  for (int q = 0; q < 6; ++q) k.k0[q] = (T)(c.cal_demag_flag ? h->k0[q] : 0.0);
+  k.key0 = (uint32_t)((uint64_t)h->seed & 0xffffffffu);
+  k.key1 = (uint32_t)((uint64_t)h->seed >> 32);
+  return k;
+}
+
+int upload_coef(mmc_handle* h, double T_K) {
+  if (h->prec == 32) {
+    McCoef<float> k = make_mc_coef<float>(h, T_K);
+    CU(cudaMemcpyAsync(h->coef, &k, sizeof k, cudaMemcpyHostToDevice, h->st));
+  } else {
+    McCoef<double> k = make_mc_coef<double>(h, T_K);
+    CU(cudaMemcpyAsync(h->coef, &k, sizeof k, cudaMemcpyHostToDevice, h->st));
+  }
+  // the source is a stack object: wait for the copy before it goes out of scope
+  CU(cudaStreamSynchronize(h->st));
+  return MMC_OK;
+}
+
+EnCoef make_en_coef(const mmc_handle* h) {
+  const mmc_config& c = h->cfg;
+  EnCoef e;
+  const double V = c.dx * c.dy * c.dz;
+  const double d[3] = {c.dx, c.dy, c.dz};
+  for (int a = 0; a < 3; ++a) e.aexV_d2[a] = c.Aex * V / (d[a] * d[a]);
+  e.dV_2d[0] = c.Dind * V / (2.0 * d[0]);
+  e.dV_2d[1] = c.Dind * V / (2.0 * d[1]);
+  e.kuV = c.Ku1 * V;
+  double un = std::sqrt(c.anisUx * c.anisUx + c.anisUy * c.anisUy + c.anisUz * c.anisUz);
+  e.u[0] = un > 0 ? c.anisUx / un : 0;
+  e.u[1] = un > 0 ? c.anisUy / un : 0;
+  e.u[2] = un > 0 ? c.anisUz / un : 0;
+  e.msVB[0] = c.ms * V * c.Bextx;
+  e.msVB[1] = c.ms * V * c.Bexty;
+  e.msVB[2] = c.ms * V * c.Bextz;
+  const double mu0 = 4e-7 * pi_of(&c);
+  e.demag = c.cal_demag_flag ? 0.5 * mu0 * c.ms * c.ms * V : 0.0;
+  return e;
+}
+
+HCoef make_h_coef(const mmc_handle* h) {
+  const mmc_config& c = h->cfg;
+  HCoef k;
+  const double mu0 = 4e-7 * pi_of(&c);
+  const double d[3] = {c.dx, c.dy, c.dz};
+  for (int a = 0; a < 3; ++a) k.ex_d2[a] = 2.0 * c.Aex / (mu0 * c.ms) / (d[a] * d[a]);
+  k.dm_2d[0] = 2.0 * c.Dind / (mu0 * c.ms) / (2.0 * d[0]);
+  k.dm_2d[1] = 2.0 * c.Dind / (mu0 * c.ms) / (2.0 * d[1]);
+  k.an = 2.0 * c.Ku1 / (mu0 * c.ms);
+  double un = std::sqrt(c.anisUx * c.anisUx + c.anisUy * c.anisUy + c.anisUz * c.anisUz);
+  k.u[0] = un > 0 ? c.anisUx / un : 0;
+  k.u[1] = un > 0 ? c.anisUy / un : 0;
+  k.u[2] = un > 0 ? c.anisUz / un : 0;
+  k.b[0] = c.Bextx / mu0;
+  k.b[1] = c.Bexty / mu0;
+  k.b[2] = c.Bextz / mu0;
+  k.ms = c.cal_demag_flag ? c.ms : 0.0;
+  return k;
+}
+
+cudaError_t demag(mmc_handle* h) {
+  if (h->prec == 32)
+    return launch_demag<float>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const float*)h->m, (float*)h->h, h->spec,
+                               h->khat, h->st);
+  return launch_demag<double>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const double*)h->m, (double*)h->h, h->spec,
+                              h->khat, h->st);
+}
+
+cudaError_t mc_color(mmc_handle* h, int color) {
+  if (h->prec == 32)
+    return launch_mc<float>(h->g, (const McCoef<float>*)h->coef, (float*)h->m, (const float*)h->h, h->ctr, color,
+                            h->acc, h->st);
+  return launch_mc<double>(h->g, (const McCoef<double>*)h->coef, (double*)h->m, (const double*)h->h, h->ctr, color,
+                           h->acc, h->st);
+}
+
+// Enqueues one full sweep: demag refresh, every colour, counter advance.
+cudaError_t enqueue_sweep(mmc_handle* h) {
+  cudaError_t e;
+  if (h->cfg.cal_demag_flag) {
+    e = demag(h);
+    if (e != cudaSuccess) return e;
+  }
+  for (int c = 0; c < h->g.ncolors; ++c) {
+    e = mc_color(h, c);
+    if (e != cudaSuccess) return e;
+  }
+  return launch_advance(h->ctr, 1, h->st);
+}
+
+int ensure_graph(mmc_handle* h, int nsw) {
+  if (h->gexec && h->graph_sweeps == nsw) return MMC_OK;
+  if (h->gexec) {
+    cudaGraphExecDestroy(h->gexec);
+    h->gexec = nullptr;
+  }
+  cudaGraph_t graph;
+  CU(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < nsw && e == cudaSuccess; ++s) e = enqueue_sweep(h);
+  cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
+  if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("sweep capture: ") + cudaGetErrorString(e));
+  if (e2 != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("sweep capture end: ") + cudaGetErrorString(e2));
+  e = cudaGraphInstantiate(&h->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  h->graph_sweeps = nsw;
+  return MMC_OK;
+}
+
+int build_demag_impl(mmc_handle* h, const char* cache_dir);
+
+int ensure_demag(mmc_handle* h) {
+  if (!h->cfg.cal_demag_flag || h->demag_built) return MMC_OK;
+  return build_demag_impl(h, h->cfg.tensor_cache);
+}
+
+// Runs `nsweeps` sweeps with counters (stage, sweep0); graph replays for the bulk.
+int run_sweeps_impl(mmc_handle* h, double T_K, long long stage, long long sweep0, long long nsweeps) {
+  if (nsweeps <= 0) return MMC_OK;
+  TRY(ensure_demag(h));
+  TRY(upload_coef(h, T_K));
+  SweepCounters c0{(uint32_t)stage, (uint32_t)sweep0};
+  CU(cudaMemcpyAsync(h->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  const int G = 64;
+  long long done = 0;
+  CU(cudaEventRecord(h->ev[0], h->st));
+  if (nsweeps >= G) {
+    TRY(ensure_graph(h, G));
+    while (nsweeps - done >= G) {
+      if (h->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
+      CU(cudaGraphLaunch(h->gexec, h->st));
+      done += G;
+      // bound the amount of queued work so a stop request takes effect quickly
+      if ((done / G) % 16 == 0) CU(cudaStreamSynchronize(h->st));
+    }
+  }
+  for (; done < nsweeps; ++done) CU(enqueue_sweep(h));
+  CU(cudaEventRecord(h->ev[1], h->st));
+  CU(cudaStreamSynchronize(h->st));
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+  h->last_run_ms = ms;
+  h->proposed += (unsigned long long)nsweeps * (unsigned long long)h->g.n;
+  return MMC_OK;
+}
+
+int profile_sweeps_impl(mmc_handle* h, double T_K, long long stage, long long sweep0, long long nsweeps,
+                        double out[3]) {
+  TRY(ensure_demag(h));
+  TRY(upload_coef(h, T_K));
+  SweepCounters c0{(uint32_t)stage, (uint32_t)sweep0};
+  CU(cudaMemcpyAsync(h->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  double tdem = 0, tmc = 0;
+  cudaEvent_t a = h->ev[0], b = h->ev[1], c = h->ev[2], t0 = h->ev[3];
+  CU(cudaEventRecord(t0, h->st));
+  for (long long s = 0; s < nsweeps; ++s) {
+    CU(cudaEventRecord(a, h->st));
+    if (h->cfg.cal_demag_flag) CU(demag(h));
+    CU(cudaEventRecord(b, h->st));
+    for (int col = 0; col < h->g.ncolors; ++col) CU(mc_color(h, col));
+    CU(cudaEventRecord(c, h->st));
+    CU(launch_advance(h->ctr, 1, h->st));
+    CU(cudaEventSynchronize(c));
+    float x = 0, y = 0;
+    CU(cudaEventElapsedTime(&x, a, b));
+    CU(cudaEventElapsedTime(&y, b, c));
+    tdem += x;
+    tmc += y;
+  }
+  CU(cudaEventRecord(b, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  float tot = 0;
+  CU(cudaEventElapsedTime(&tot, t0, b));
+  out[0] = tdem;
+  out[1] = tmc;
+  out[2] = tot;
+  h->proposed += (unsigned long long)nsweeps * (unsigned long long)h->g.n;
+  return MMC_OK;
+}
+
+std::string cache_name(const mmc_handle* h) {
+  char b[256];
+  std::snprintf(b, sizeof b, "cache_%d_%d_%d-%g_%g_%g-%d_%d_%d.ovf", h->g.nxp, h->g.nyp, h->g.nzp, h->cfg.dx,
+                h->cfg.dy, h->cfg.dz, h->cfg.pbc_x, h->cfg.pbc_y, h->cfg.pbc_z);
+  return b;
+}
+
+bool dir_exists(const std::string& d) {
+  struct stat sb;
+  return !d.empty() && stat(d.c_str(), &sb) == 0 && S_ISDIR(sb.st_mode);
+}
+
+std::string join(const std::string& d, const std::string& f) {
+  if (d.empty()) return f;
+  return d.back() == '/' ? d + f : d + "/" + f;
+}
+
+// Tensor cache in the reference's raw format (src/main.cu:427-455, 548-572):
+// 6 blocks xx,xy,xz,yy,yz,zz of nxp*nyp*nzp doubles, z fastest / x slowest.
+bool cache_load(mmc_handle* h, const std::string& path) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) return false;
+  const Geom& g = h->g;
+  std::vector<double> raw(6 * (size_t)g.np);
+  in.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * sizeof(double)));
+  if (!in || in.gcount() != (std::streamsize)(raw.size() * sizeof(double))) return false;
+  h->tensor.assign(6 * (size_t)g.np, 0.0);
+  for (int c = 0; c < 6; ++c)
+    for (int x = 0; x < g.nxp; ++x)
+      for (int y = 0; y < g.nyp; ++y)
+        for (int z = 0; z < g.nzp; ++z)
+          h->tensor[c * g.np + x + (long long)g.nxp * (y + (long long)g.nyp * z)] =
+              raw[c * g.np + z + (long long)g.nzp * (y + (long long)g.nyp * x)];
+  return true;
+}
+
+bool cache_save(const mmc_handle* h, const std::string& path) {
+  const Geom& g = h->g;
+  std::vector<double> raw(6 * (size_t)g.np);
+  for (int c = 0; c < 6; ++c)
+    for (int x = 0; x < g.nxp; ++x)
+      for (int y = 0; y < g.nyp; ++y)
+        for (int z = 0; z < g.nzp; ++z)
+          raw[c * g.np + z + (long long)g.nzp * (y + (long long)g.nyp * x)] =
+              h->tensor[c * g.np + x + (long long)g.nxp * (y + (long long)g.nyp * z)];
+  std::ofstream out(path, std::ios::binary | std::ios::trunc);
+  if (!out) return false;
+  out.write(reinterpret_cast<const char*>(raw.data()), (std::streamsize)(raw.size() * sizeof(double)));
+  return (bool)out;
+}
+
+int build_demag_impl(mmc_handle* h, const char* cache_dir) {
+  TRY(set_dev(h));
+  const Geom& g = h->g;
+  const mmc_config& c = h->cfg;
+  std::string dir = cache_dir ? cache_dir : "";
+  std::string path = dir.empty() ? "" : join(dir, cache_name(h));
+  bool loaded = !path.empty() && cache_load(h, path);
+  double* k6 = nullptr;
+  double2* spec64 = nullptr;
+  CU(cudaMalloc(&k6, 6 * (size_t)g.np * sizeof(double)));
+  int status = MMC_OK;
+  do {
+    if (loaded) {
+      cudaError_t e = cudaMemcpy(k6, h->tensor.data(), 6 * (size_t)g.np * sizeof(double), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
+        break;
+      }
+    } else {
+      const int Px = std::max(c.pbc_x, 0), Py = std::max(c.pbc_y, 0), Pz = std::max(c.pbc_z, 0);
+      // Each launch adds a slab of x images to every point's running sum; about
+      // 1e9 f/g evaluations per launch keeps launches near a second.
+      const double per_px = (double)g.np * (2.0 * Py + 1) * (2.0 * Pz + 1) * 384.0;
+      const int slab = std::max(1, (int)(1e9 / per_px));
+      for (int px0 = -Px; px0 <= Px; px0 += slab) {
+        if (h->stop.load()) {
+          status = fail(MMC_ERR_INTERRUPTED, "stop requested during the tensor build");
+          break;
+        }
+        const int px1 = std::min(Px, px0 + slab - 1);
+        cudaError_t e = launch_newell(g, c.dx, c.dy, c.dz, Px, Py, Pz, pi_of(&c), k6, px0, px1, px1 == Px, h->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+        if (e != cudaSuccess) {
+          status = fail(MMC_ERR_CUDA, std::string("tensor build: ") + cudaGetErrorString(e));
+          break;
+        }
+      }
+      if (status != MMC_OK) break;
+      h->tensor.assign(6 * (size_t)g.np, 0.0);
+      cudaError_t e = cudaMemcpy(h->tensor.data(), k6, 6 * (size_t)g.np * sizeof(double), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) {
+        status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
+        break;
+      }
+      if (!path.empty() && dir_exists(dir)) cache_save(h, path);
+    }
+    for (int q = 0; q < 6; ++q) h->k0[q] = h->tensor[(size_t)q * g.np];
+    cudaError_t e = cudaMalloc(&spec64, 6 * (size_t)g.nspec * sizeof(double2));
+    if (e != cudaSuccess) {
+      status = fail(MMC_ERR_OOM, "tensor spectrum allocation");
+      break;
+    }
+    DemagTuning tt = h->tun;
+    // six-component setup transform: narrower tiles keep shared memory in budget
+    while (tt.col_tx > 1 && ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx * (h->py.p.n + 1)) *
+                                    sizeof(double2) > smem_limit())
+      tt.col_tx /= 2;
+    while (tt.col_tx_z > 1 && ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx_z * (h->pz.p.n + 1)) *
+                                      sizeof(double2) > smem_limit())
+      tt.col_tx_z /= 2;
+    tt.col_tx = std::min(tt.col_tx, tt.col_tx_z);
+    tt.col_tx_z = tt.col_tx;
+    e = launch_tensor_fft(g, h->px.p, h->py.p, h->pz.p, tt, k6, spec64, h->st);
+    if (e == cudaSuccess) {
+      if (h->prec == 32) e = launch_khat_store<float>(6 * g.nspec, spec64, h->khat, h->st);
+      else e = launch_khat_store<double>(6 * g.nspec, spec64, h->khat, h->st);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) {
+      status = fail(MMC_ERR_CUDA, std::string("tensor transform: ") + cudaGetErrorString(e));
+      break;
+    }
+    h->demag_built = true;
+  } while (0);
+  if (spec64) cudaFree(spec64);
+  if (k6) cudaFree(k6);
+  return status;
+}
+
+int get_m_impl(mmc_handle* h, double* mx, double* my, double* mz) {
+  const long long n = h->g.n;
+  cudaError_t e = h->prec == 32 ? launch_to_f64<float>(3 * n, (const float*)h->m, h->stage64, h->st)
+                                : launch_to_f64<double>(3 * n, (const double*)h->m, h->stage64, h->st);
+  CU(e);
+  CU(cudaMemcpyAsync(mx, h->stage64, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(my, h->stage64 + n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(mz, h->stage64 + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  return MMC_OK;
+}
+
+int set_m_impl(mmc_handle* h, const double* mx, const double* my, const double* mz) {
+  const long long n = h->g.n;
+  CU(cudaMemcpyAsync(h->stage64, mx, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CU(cudaMemcpyAsync(h->stage64 + n, my, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  CU(cudaMemcpyAsync(h->stage64 + 2 * n, mz, n * sizeof(double), cudaMemcpyHostToDevice, h->st));
+  cudaError_t e = h->prec == 32 ? launch_from_f64<float>(3 * n, h->stage64, (float*)h->m, h->st)
+                                : launch_from_f64<double>(3 * n, h->stage64, (double*)h->m, h->st);
+  CU(e);
+  CU(cudaStreamSynchronize(h->st));
+  return MMC_OK;
+}
+
+int energy_impl(mmc_handle* h, mmc_observables* out) {
+  TRY(ensure_demag(h));
+  if (h->cfg.cal_demag_flag) CU(demag(h));
+  EnCoef e = make_en_coef(h);
+  cudaError_t err =
+      h->prec == 32
+          ? launch_energy<float>(h->g, e, (const float*)h->m, h->cfg.cal_demag_flag ? (const float*)h->h : nullptr,
+                                 h->partials, h->npartials, h->red, h->st)
+          : launch_energy<double>(h->g, e, (const double*)h->m, h->cfg.cal_demag_flag ? (const double*)h->h : nullptr,
+                                  h->partials, h->npartials, h->red, h->st);
+  CU(err);
+  CU(cudaMemcpyAsync(h->red_host, h->red, NQ * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  unsigned long long acc = 0;
+  CU(cudaMemcpyAsync(&acc, h->acc, sizeof acc, cudaMemcpyDeviceToHost, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  const double* r = h->red_host;
+  const double n = (double)h->g.n;
+  out->e_exchange = r[0];
+  out->e_dmi = r[1];
+  out->e_anisotropy = r[2];
+  out->e_zeeman = r[3];
+  out->e_demag = r[4];
+  out->e_total = r[0] + r[1] + r[2] + r[3] + r[4];
+  out->m[0] = r[5] / n;
+  out->m[1] = r[6] / n;
+  out->m[2] = r[7] / n;
+  out->q = r[8] / (4.0 * 3.14159265358979323846) / (double)h->g.nz;
+  out->accepted = acc - h->acc_base;
+  out->proposed = h->proposed;
+  h->acc_base = acc;
+  h->proposed = 0;
+  return MMC_OK;
+}
+
+void destroy_impl(mmc_handle* h) {
+  if (!h) return;
+  cudaSetDevice(h->device);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  void* bufs[] = {h->m, h->h, h->spec, h->khat, h->coef, h->partials, h->red, h->acc, h->ctr, h->stage64, h->field64};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  if (h->red_host) cudaFreeHost(h->red_host);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  free_plan(&h->px);
+  free_plan(&h->py);
+  free_plan(&h->pz);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+}
+
+int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
+  *out = nullptr;
+  TRY(config_validate(cfg));
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(MMC_ERR_NO_DEVICE, "no CUDA device");
+  if (device < 0 || device >= ndev) return fail(MMC_ERR_INVALID, "device index out of range");
+  mmc_handle* h = new mmc_handle();
+  h->cfg = *cfg;
+  h->device = device;
+  h->prec = cfg->precision;
+  h->tsize = h->prec == 32 ? 4 : 8;
+  h->seed = cfg->randomseed < 0 ? (long long)std::time(nullptr) : cfg->randomseed;
+  h->cfg.randomseed = h->seed;
+  auto bail = [&](int st) {
+    std::string msg = last_error_cstr();
+    destroy_impl(h);
+    fail(st, msg);
+    return st;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return bail(fail(MMC_ERR_CUDA, "cudaSetDevice failed"));
+  Geom& g = h->g;
+  g.nx = cfg->nx;
+  g.ny = cfg->ny;
+  g.nz = cfg->nz;
+  // src/main.cu:254-263
+  g.nxp = cfg->pbc_x == 0 ? 2 * cfg->nx - 1 : cfg->nx;
+  g.nyp = cfg->pbc_y == 0 ? 2 * cfg->ny - 1 : cfg->ny;
+  g.nzp = cfg->pbc_z == 0 ? 2 * cfg->nz - 1 : cfg->nz;
+  g.hx = g.nxp / 2 + 1;
+  g.per[0] = cfg->pbc_x != 0;
+  g.per[1] = cfg->pbc_y != 0;
+  g.per[2] = cfg->pbc_z != 0;
+  g.ncolors = 2;
+  const int dims[3] = {g.nx, g.ny, g.nz};
+  for (int a = 0; a < 3; ++a)
+    if (g.per[a] && (dims[a] & 1) && dims[a] > 1) g.ncolors = 3;
+  g.n = (long long)g.nx * g.ny * g.nz;
+  g.np = (long long)g.nxp * g.nyp * g.nzp;
+  g.nspec = (long long)g.hx * g.nyp * g.nzp;
+  int st;
+  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(MMC_ERR_CUDA, "stream creation failed"));
+  if ((st = make_plan(g.nxp, &h->px)) != MMC_OK) return bail(st);
+  if ((st = make_plan(g.nyp, &h->py)) != MMC_OK) return bail(st);
+  if ((st = make_plan(g.nzp, &h->pz)) != MMC_OK) return bail(st);
+  int nsm = 148, optin = 48 * 1024;
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+  if (launch_prepare<float>(optin) != cudaSuccess || launch_prepare<double>(optin) != cudaSuccess)
+    return bail(fail(MMC_ERR_CUDA, "kernel attribute setup failed"));
+  const size_t csize = 2 * h->tsize;
+  h->tun = choose_tuning(g, h->px.p, h->py.p, h->pz.p, csize, nsm);
+  // shared-memory feasibility of the per-sweep passes
+  if (((size_t)((h->px.p.tw_total + 1) & ~1) + 2 * 2 * (size_t)h->px.p.n) * csize > smem_limit() ||
+      ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)(h->py.p.n + 1)) * csize > smem_limit() ||
+      ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)(h->pz.p.n + 1)) * csize > smem_limit() ||
+      ((size_t)((h->px.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)h->px.p.n) * 16 > smem_limit())
+    return bail(fail(MMC_ERR_UNSUPPORTED, "padded lattice dimension too large for the shared-memory FFT"));
+  auto alloc = [&](void** p, size_t bytes) -> int {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(MMC_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return MMC_OK;
+  };
+  h->npartials = energy_partials_count(g);
+  if ((st = alloc(&h->m, 3 * g.n * h->tsize)) != MMC_OK) return bail(st);
+  if ((st = alloc(&h->h, 3 * g.n * h->tsize)) != MMC_OK) return bail(st);
+  if (cfg->cal_demag_flag) {
+    if ((st = alloc(&h->spec, 3 * g.nspec * csize)) != MMC_OK) return bail(st);
+    if ((st = alloc(&h->khat, 6 * g.nspec * csize)) != MMC_OK) return bail(st);
+  }
+  if ((st = alloc(&h->coef, sizeof(McCoef<double>))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&h->partials, (size_t)h->npartials * NQ * sizeof(double))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&h->red, NQ * sizeof(double))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&h->acc, sizeof(unsigned long long))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&h->ctr, sizeof(SweepCounters))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&h->stage64, 3 * g.n * sizeof(double))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&h->field64, 3 * g.n * sizeof(double))) != MMC_OK) return bail(st);
+  for (auto& e : h->ev)
+    if (cudaEventCreate(&e) != cudaSuccess) return bail(fail(MMC_ERR_CUDA, "event creation failed"));
+  if (cudaMallocHost(&h->red_host, NQ * sizeof(double)) != cudaSuccess)
+    return bail(fail(MMC_ERR_OOM, "pinned allocation failed"));
+  if (cudaMemset(h->acc, 0, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(h->h, 0, 3 * g.n * h->tsize) != cudaSuccess)
+    return bail(fail(MMC_ERR_CUDA, "memset failed"));
+  // initial magnetisation (src/main.cu:289-333)
+  if (cfg->use_random_init) {
+    cudaError_t e = h->prec == 32 ? launch_init<float>(g, (uint64_t)h->seed, (float*)h->m, h->st)
+                                  : launch_init<double>(g, (uint64_t)h->seed, (double*)h->m, h->st);
+    if (e != cudaSuccess || cudaStreamSynchronize(h->st) != cudaSuccess)
+      return bail(fail(MMC_ERR_CUDA, "init kernel failed"));
+  } else if (cfg->ovf_filename[0]) {
+    std::vector<double> mm(3 * g.n);
+    if ((st = ovf_read(cfg->ovf_filename, g.nx, g.ny, g.nz, cfg->dx, cfg->dy, cfg->dz, mm.data(), mm.data() + g.n,
+                       mm.data() + 2 * g.n)) != MMC_OK)
+      return bail(st);
+    if ((st = set_m_impl(h, mm.data(), mm.data() + g.n, mm.data() + 2 * g.n)) != MMC_OK) return bail(st);
+  } else {
+    std::vector<double> mm(3 * g.n, 0.0);
+    for (long long i = 0; i < g.n; ++i) mm[2 * g.n + i] = 1.0;
+    if ((st = set_m_impl(h, mm.data(), mm.data() + g.n, mm.data() + 2 * g.n)) != MMC_OK) return bail(st);
+  }
+  clear_error();
+  *out = h;
+  return MMC_OK;
+}
+
+bool has_ext(const std::string& f, const char* e) {
+  size_t n = std::strlen(e);
+  if (f.size() < n) return false;
+  std::string t = f.substr(f.size() - n);
+  for (auto& ch : t) ch = (char)std::tolower((unsigned char)ch);
+  return t == e;
+}
+
+// src/main.cu:193-231: create the output folder, or empty it of images and OVF files.
+int prepare_output_dir(const std::string& dir) {
+  if (!dir_exists(dir)) {
+    std::string acc;
+    for (size_t i = 0; i <= dir.size(); ++i) {
+      if (i == dir.size() || dir[i] == '/') {
+        acc = dir.substr(0, i);
+        if (!acc.empty() && !dir_exists(acc)) mkdir(acc.c_str(), 0755);
+      }
+    }
+    if (!dir_exists(dir)) return fail(MMC_ERR_IO, "cannot create output folder: " + dir);
+    return MMC_OK;
+  }
+  DIR* d = opendir(dir.c_str());
+  if (!d) return fail(MMC_ERR_IO, "cannot open output folder: " + dir);
+  while (struct dirent* e = readdir(d)) {
+    std::string f = e->d_name;
+    if (has_ext(f, ".ovf") || has_ext(f, ".png") || has_ext(f, ".jpg") || has_ext(f, ".jpeg"))
+      std::remove(join(dir, f).c_str());
+  }
+  closedir(d);
+  return MMC_OK;
+}
+
+int snapshot(mmc_handle* h, const std::string& dir, long long count, double T, long long sweep) {
+  const long long n = h->g.n;
+  std::vector<double> mm(3 * n);
+  TRY(get_m_impl(h, mm.data(), mm.data() + n, mm.data() + 2 * n));
+  char name[256];
+  std::snprintf(name, sizeof name, "%06lld_%.2fK_%lld.ovf", count, T, sweep);
+  return ovf_write(join(dir, name), h->g.nx, h->g.ny, h->g.nz, h->cfg.dx, h->cfg.dy, h->cfg.dz, mm.data(),
+                   mm.data() + n, mm.data() + 2 * n, h->cfg.ovf_format, "m");
+}
+
+// The temperature-stage loop (src/main.cu:801-1139).  T is stepped in the
+// working precision as the reference's FLOAT_ Temperature is.
+template <typename R>
+int anneal_loop(mmc_handle* h, const std::string& dir, int verbose) {
+  const mmc_config& c = h->cfg;
+  const std::string efile = join(dir, "energy.txt");
+  {
+    FILE* fp = std::fopen(efile.c_str(), "w");
+    if (!fp) return fail(MMC_ERR_IO, "cannot create " + efile);
+    std::fclose(fp);
+  }
+  R T = (R)c.Temperature_start;
+  const R Tend = (R)c.Temperature_end, Tstep = (R)c.Temperature_step;
+  long long out_count = 0, stage = 0;
+  auto t0 = std::chrono::steady_clock::now();
+  while (T > Tend) {
+    if (verbose) std::printf("\n\nTemperature: %.2f K\n", (double)T);
+    long long s = 0;
+    while (s < c.circle_per_stage) {
+      if (h->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
+      if (s % c.terminal_output_period == 0 && verbose) {
+        double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (s == 0) {
+          t0 = std::chrono::steady_clock::now();
+          std::printf("Stage: %lld \n", s);
+        } else {
+          std::printf("Stage: %lld, elapsed time: %f s, speed: %f stages/s\n", s, el, (double)s / el);
+        }
+      }
+      if (s % c.ms_output_period == 0) {
+        TRY(snapshot(h, dir, out_count, (double)T, s));
+        ++out_count;
+      }
+      if (s % c.energy_output_period == 0) {
+        mmc_observables o;
+        TRY(energy_impl(h, &o));
+        if (verbose) std::printf("\nEnergy:  %g\n", o.e_total);
+        FILE* fp = std::fopen(efile.c_str(), "a");
+        if (!fp) return fail(MMC_ERR_IO, "cannot append to " + efile);
+        std::fprintf(fp, "%f %lld %g\n", (double)T, s, o.e_total);
+        std::fclose(fp);
+      }
+      long long next = c.circle_per_stage;
+      const long long per[3] = {c.terminal_output_period, c.ms_output_period, c.energy_output_period};
+      for (long long p : per) next = std::min(next, (s / p + 1) * p);
+      TRY(run_sweeps_impl(h, (double)T, stage, s, next - s));
+      s = next;
+    }
+    T = c.Temperature_use_exp ? (R)(T * Tstep) : (R)(T - Tstep);
+    ++stage;
+  }
+  if (verbose) std::printf("~~~~~~~~~~~~~~END~~~~~~~~~~~~~~~~~~~~~~~~~ \n");
+  return MMC_OK;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+int mmc_abi_version(void) { return MMC_ABI_VERSION; }
+
+size_t mmc_config_size(void) { return sizeof(mmc_config); }
+
+const char* mmc_status_string(int s) {
+  switch (s) {
+    case MMC_OK: return "ok";
+    case MMC_ERR_INVALID: return "invalid argument";
+    case MMC_ERR_CONFIG: return "configuration error";
+    case MMC_ERR_IO: return "I/O error";
+    case MMC_ERR_CUDA: return "CUDA error";
+    case MMC_ERR_NO_DEVICE: return "no CUDA device";
+    case MMC_ERR_UNSUPPORTED: return "unsupported";
+    case MMC_ERR_INTERRUPTED: return "interrupted";
+    case MMC_ERR_TIMEOUT: return "device wait timed out";
+    case MMC_ERR_STATE: return "wrong call order";
+    case MMC_ERR_OOM: return "out of device memory";
+    default: return "unknown status";
+  }
+}
+
+const char* mmc_last_error(void) { return last_error_cstr(); }
+
+void mmc_config_defaults(mmc_config* cfg) {
+  if (cfg) config_defaults(cfg);
+}
+
+int mmc_config_load_ini(const char* path, mmc_config* cfg) {
+  if (!path || !cfg) return fail(MMC_ERR_INVALID, "null argument");
+  return config_load_ini(path, cfg);
+}
+
+int mmc_config_format(const mmc_config* cfg, char* buf, size_t len) {
+  if (!cfg || !buf || len == 0) return fail(MMC_ERR_INVALID, "null argument");
+  std::string s = config_format(cfg);
+  std::snprintf(buf, len, "%s", s.c_str());
+  return MMC_OK;
+}
+
+int mmc_padded_dims(const mmc_config* cfg, int out[3]) {
+  if (!cfg || !out) return fail(MMC_ERR_INVALID, "null argument");
+  out[0] = cfg->pbc_x == 0 ? 2 * cfg->nx - 1 : cfg->nx;
+  out[1] = cfg->pbc_y == 0 ? 2 * cfg->ny - 1 : cfg->ny;
+  out[2] = cfg->pbc_z == 0 ? 2 * cfg->nz - 1 : cfg->nz;
+  return MMC_OK;
+}
+
+int mmc_create(const mmc_config* cfg, int device, mmc_handle** out) {
+  if (!cfg || !out) return fail(MMC_ERR_INVALID, "null argument");
+  return create_impl(cfg, device, out);
+}
+
+void mmc_destroy(mmc_handle* h) { destroy_impl(h); }
+
+int mmc_init_random(mmc_handle* h, long long seed) {
+  if (!h) return fail(MMC_ERR_INVALID, "null handle");
+  TRY(set_dev(h));
+  cudaError_t e = h->prec == 32 ? launch_init<float>(h->g, (uint64_t)seed, (float*)h->m, h->st)
+                                : launch_init<double>(h->g, (uint64_t)seed, (double*)h->m, h->st);
+  CU(e);
+  return sync_check(h);
+}
+
+int mmc_set_m(mmc_handle* h, const double* mx, const double* my, const double* mz) {
+  if (!h || !mx || !my || !mz) return fail(MMC_ERR_INVALID, "null argument");
+  TRY(set_dev(h));
+  return set_m_impl(h, mx, my, mz);
+}
+
+int mmc_get_m(mmc_handle* h, double* mx, double* my, double* mz) {
+  if (!h || !mx || !my || !mz) return fail(MMC_ERR_INVALID, "null argument");
+  TRY(set_dev(h));
+  return get_m_impl(h, mx, my, mz);
+}
+
+int mmc_build_demag(mmc_handle* h, const char* cache_dir) {
+  if (!h) return fail(MMC_ERR_INVALID, "null handle");
+  if (!h->cfg.cal_demag_flag) return fail(MMC_ERR_STATE, "cal_demag_flag is off");
+  if (h->demag_built) return MMC_OK;
+  return build_demag_impl(h, cache_dir);
+}
+
+int mmc_get_tensor(mmc_handle* h, double* k6) {
+  if (!h || !k6) return fail(MMC_ERR_INVALID, "null argument");
+  if (!h->demag_built) return fail(MMC_ERR_STATE, "demag tensor not built");
+  std::memcpy(k6, h->tensor.data(), h->tensor.size() * sizeof(double));
+  return MMC_OK;
+}
+
+int mmc_self_tensor(mmc_handle* h, double k6[6]) {
+  if (!h || !k6) return fail(MMC_ERR_INVALID, "null argument");
+  if (!h->demag_built) return fail(MMC_ERR_STATE, "demag tensor not built");
+  for (int q = 0; q < 6; ++q) k6[q] = h->k0[q];
+  return MMC_OK;
+}
+
+int mmc_compute_demag(mmc_handle* h) {
+  if (!h) return fail(MMC_ERR_INVALID, "null handle");
+  if (!h->cfg.cal_demag_flag) return fail(MMC_ERR_STATE, "cal_demag_flag is off");
+  TRY(set_dev(h));
+  TRY(ensure_demag(h));
+  CU(demag(h));
+  return sync_check(h);
+}
+
+int mmc_demag_scratch_bytes(mmc_handle* h, size_t* bytes) {
+  if (!h || !bytes) return fail(MMC_ERR_INVALID, "null argument");
+  *bytes = 3 * (size_t)h->g.nspec * 2 * h->tsize;
+  return MMC_OK;
+}
+
+int mmc_demag_apply(mmc_handle* h, const void* mdev, void* hdev, void* scratch, size_t scratch_bytes,
+                    void* stream) {
+  if (!h || !mdev || !hdev || !scratch) return fail(MMC_ERR_INVALID, "null argument");
+  if (!h->cfg.cal_demag_flag) return fail(MMC_ERR_STATE, "cal_demag_flag is off");
+  if (scratch_bytes < 3 * (size_t)h->g.nspec * 2 * h->tsize) return fail(MMC_ERR_INVALID, "scratch too small");
+  TRY(set_dev(h));
+  TRY(ensure_demag(h));
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->st;
+  cudaError_t e = h->prec == 32 ? launch_demag<float>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const float*)mdev,
+                                                      (float*)hdev, scratch, h->khat, st)
+                                : launch_demag<double>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const double*)mdev,
+                                                       (double*)hdev, scratch, h->khat, st);
+  CU(e);
+  return MMC_OK;
+}
+
+int mmc_selftest_philox(int device, long long n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out,
+                        uint32_t* out_curand) {
+  if (n < 0 || (n > 0 && !ctr)) return fail(MMC_ERR_INVALID, "bad argument");
+  if (n == 0) return MMC_OK;
+  CU(cudaSetDevice(device));
+  uint32_t* d = nullptr;
+  CU(cudaMalloc(&d, 12 * (size_t)n * sizeof(uint32_t)));
+  cudaError_t e = cudaMemcpy(d, ctr, 4 * (size_t)n * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = launch_philox_selftest(n, d, k0, k1, d + 4 * n, d + 8 * n, nullptr);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess && out) e = cudaMemcpy(out, d + 4 * n, 4 * (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && out_curand)
+    e = cudaMemcpy(out_curand, d + 8 * n, 4 * (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  CU(e);
+  return MMC_OK;
+}
+
+int mmc_get_field(mmc_handle* h, int term, double* hx, double* hy, double* hz) {
+  if (!h || !hx || !hy || !hz) return fail(MMC_ERR_INVALID, "null argument");
+  if (term < 0 || term > 5) return fail(MMC_ERR_INVALID, "bad term");
+  TRY(set_dev(h));
+  if ((term == MMC_TERM_DEMAG || term == MMC_TERM_TOTAL) && h->cfg.cal_demag_flag && !h->demag_built)
+    return fail(MMC_ERR_STATE, "demag field not computed");
+  HCoef k = make_h_coef(h);
+  cudaError_t e = h->prec == 32 ? launch_field<float>(h->g, k, term, (const float*)h->m, (const float*)h->h,
+                                                      h->field64, h->st)
+                                : launch_field<double>(h->g, k, term, (const double*)h->m, (const double*)h->h,
+                                                       h->field64, h->st);
+  CU(e);
+  const long long n = h->g.n;
+  CU(cudaMemcpyAsync(hx, h->field64, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(hy, h->field64 + n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(hz, h->field64 + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  return sync_check(h);
+}
+
+int mmc_energy(mmc_handle* h, mmc_observables* out) {
+  if (!h || !out) return fail(MMC_ERR_INVALID, "null argument");
+  TRY(set_dev(h));
+  return energy_impl(h, out);
+}
+
+int mmc_run_sweeps(mmc_handle* h, double temperature, long long stage, long long sweep0, long long nsweeps) {
+  if (!h) return fail(MMC_ERR_INVALID, "null handle");
+  if (!(temperature > 0)) return fail(MMC_ERR_INVALID, "temperature must be > 0");
+  if (nsweeps < 0 || stage < 0 || sweep0 < 0) return fail(MMC_ERR_INVALID, "negative counter");
+  TRY(set_dev(h));
+  h->stop.store(0);
+  return run_sweeps_impl(h, temperature, stage, sweep0, nsweeps);
+}
+
+int mmc_run_anneal(mmc_handle* h, const char* output_dir, int verbose) {
+  if (!h || !output_dir) return fail(MMC_ERR_INVALID, "null argument");
+  TRY(set_dev(h));
+  h->stop.store(0);
+  TRY(prepare_output_dir(output_dir));
+  return h->prec == 32 ? anneal_loop<float>(h, output_dir, verbose) : anneal_loop<double>(h, output_dir, verbose);
+}
+
+int mmc_last_run_ms(mmc_handle* h, double* ms) {
+  if (!h || !ms) return fail(MMC_ERR_INVALID, "null argument");
+  *ms = h->last_run_ms;
+  return MMC_OK;
+}
+
+int mmc_profile_sweeps(mmc_handle* h, double temperature, long long stage, long long sweep0, long long nsweeps,
+                       double out_ms[3]) {
+  if (!h || !out_ms) return fail(MMC_ERR_INVALID, "null argument");
+  if (!(temperature > 0)) return fail(MMC_ERR_INVALID, "temperature must be > 0");
+  TRY(set_dev(h));
+  return profile_sweeps_impl(h, temperature, stage, sweep0, nsweeps, out_ms);
+}
+
+void mmc_request_stop(mmc_handle* h) {
+  if (h) h->stop.store(1);
+}
+
+int mmc_ovf_read(const char* path, int nx, int ny, int nz, double dx, double dy, double dz, double* mx, double* my,
+                 double* mz) {
+  if (!path || !mx || !my || !mz) return fail(MMC_ERR_INVALID, "null argument");
+  return ovf_read(path, nx, ny, nz, dx, dy, dz, mx, my, mz);
+}
+
+int mmc_ovf_write(const char* path, int nx, int ny, int nz, double dx, double dy, double dz, const double* mx,
+                  const double* my, const double* mz, int format, const char* title) {
+  if (!path || !mx || !my || !mz) return fail(MMC_ERR_INVALID, "null argument");
+  return ovf_write(path, nx, ny, nz, dx, dy, dz, mx, my, mz, format, title ? title : "m");
+}
+
+}  // extern "C"

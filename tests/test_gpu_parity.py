@@ -1,0 +1,298 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle and the
+committed golden fixtures.
+
+Tolerances: integer / bit work (Philox, decisions, FP64 tensor) bit-exact; FP64
+fields and energies 1e-12 relative; FP32 fields 1e-5 relative (of the field's
+largest component)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+FP64_REL = 1e-12
+FP32_REL = 1e-5
+
+
+def cfg(M, **kw):
+    base = dict(nx=16, ny=16, nz=1, dx=1e-9, dy=1e-9, dz=0.8e-9, pbc_x=2, pbc_y=2, pbc_z=0, precision=64,
+                randomseed=256, Bextx=0.02, Bexty=-0.01, Bextz=0.3, anisUx=0.1, anisUy=0.0, anisUz=1.0)
+    base.update(kw)
+    return M.Config.defaults(**base)
+
+
+GEOMS = {
+    "film16_pbc2": dict(),
+    "film12x10_open": dict(nx=12, ny=10, pbc_x=0, pbc_y=0),
+    "slab6x5x4_open": dict(nx=6, ny=5, nz=4, pbc_x=0, pbc_y=0, pbc_z=0),
+    "odd_periodic": dict(nx=15, ny=7, nz=1, pbc_x=1, pbc_y=-1),
+    "mixed_3d": dict(nx=9, ny=6, nz=3, pbc_x=1, pbc_y=0, pbc_z=1),
+    "radix_7_5": dict(nx=7, ny=10, nz=2, pbc_x=2, pbc_y=1, pbc_z=0),
+}
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def test_philox_matches_oracle_and_curand(M, O):
+    rng = np.random.default_rng(3)
+    ctr = rng.integers(0, 2 ** 32, size=(4096, 4), dtype=np.uint64).astype(np.uint32)
+    ctr[0] = 0
+    ctr[1] = 0xFFFFFFFF
+    ours, cur = M.philox_device(ctr, 0xA4093822, 0x299F31D0)
+    assert np.array_equal(ours, cur)
+    for i in range(0, 4096, 97):
+        assert np.array_equal(ours[i], O.philox(ctr[i], [0xA4093822, 0x299F31D0]))
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_init_matches_oracle(M, O, prec):
+    c = cfg(M, nx=33, ny=17, nz=3, precision=prec)
+    with M.Lattice(c) as lat:
+        m = lat.get_m()
+    want = O.init_random(c, 256)
+    if prec == 64:
+        assert np.array_equal(m, want)
+    else:
+        assert np.array_equal(m, want.astype(np.float32).astype(np.float64))
+
+
+@pytest.mark.parametrize("case", range(4))
+def test_tensor_matches_golden(M, case):
+    with open(os.path.join(GOLDEN, "newell_golden.json")) as f:
+        g = json.load(f)["tensors"][case]
+    c = cfg(M, nx=g["nx"], ny=g["ny"], nz=g["nz"], dx=g["dx"], dy=g["dy"], dz=g["dz"], pbc_x=g["pbc"][0],
+            pbc_y=g["pbc"][1], pbc_z=g["pbc"][2])
+    with M.Lattice(c) as lat:
+        lat.build_demag()
+        k = lat.tensor()
+    np.testing.assert_allclose(k, np.array(g["K"]), rtol=0, atol=5e-13)
+
+
+@pytest.mark.parametrize("geom", sorted(GEOMS))
+def test_tensor_bitwise_equals_oracle(M, O, geom):
+    c = cfg(M, **GEOMS[geom])
+    with M.Lattice(c) as lat:
+        lat.build_demag()
+        k = lat.tensor()
+        k0 = lat.self_tensor()
+    want = O.tensor(c)
+    assert np.array_equal(k, want)
+    assert np.array_equal(k0, want[:, 0])
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("geom", sorted(GEOMS))
+def test_demag_field_matches_direct_sum(M, O, geom, prec):
+    c = cfg(M, precision=prec, **GEOMS[geom])
+    with M.Lattice(c) as lat:
+        lat.build_demag()
+        m = lat.get_m()
+        lat.compute_demag()
+        H = lat.field(M.TERM_DEMAG)
+        k = lat.tensor()
+    want = c.ms * O.demag_direct(c, k, m)
+    assert rel(H, want) <= (FP64_REL if prec == 64 else FP32_REL)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("term", [0, 1, 2, 3, 5])
+@pytest.mark.parametrize("geom", ["film16_pbc2", "slab6x5x4_open", "odd_periodic"])
+def test_field_terms(M, O, geom, term, prec):
+    c = cfg(M, precision=prec, Dind=6e-3, **GEOMS[geom])
+    with M.Lattice(c) as lat:
+        lat.compute_demag()
+        m = lat.get_m()
+        H = lat.field(term)
+        k = lat.tensor()
+    hd = O.demag_direct(c, k, m)
+    want = O.field(c, term, m, hd)
+    assert rel(H, want) <= (FP64_REL if prec == 64 else FP32_REL)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+@pytest.mark.parametrize("geom", sorted(GEOMS))
+def test_energy_and_observables(M, O, geom, prec):
+    c = cfg(M, precision=prec, **GEOMS[geom])
+    with M.Lattice(c) as lat:
+        o = lat.energy()
+        m = lat.get_m()
+        k = lat.tensor()
+    want = O.energy(c, m, O.demag_direct(c, k, m))
+    got = np.array([o.e_exchange, o.e_dmi, o.e_anisotropy, o.e_zeeman, o.e_demag, *o.m, o.q])
+    tol = 1e-11 if prec == 64 else 2e-5
+    scale = np.abs(want[:5]).sum()
+    assert np.abs(got[:5] - want[:5]).max() <= tol * scale
+    assert np.abs(got[5:8] - want[5:8]).max() <= 1e-12
+    assert abs(got[8] - want[8]) <= 1e-9
+    assert abs(o.e_total - want[:5].sum()) <= tol * scale
+
+
+@pytest.mark.parametrize("demag", [0, 1])
+@pytest.mark.parametrize("geom", ["film16_pbc2", "odd_periodic", "mixed_3d"])
+def test_fp64_decisions_bitwise_100_sweeps(M, O, geom, demag):
+    """FP64 accept/reject decisions identical to the oracle's for 100 sweeps:
+    the final state (every spin is its initial vector or a Philox proposal) and
+    the accept count must match exactly."""
+    c = cfg(M, cal_demag_flag=demag, **GEOMS[geom])
+    with M.Lattice(c) as lat:
+        m0 = lat.get_m()
+        k = lat.tensor() if demag else None
+        T = 120.0
+        lat.run_sweeps(T, 4, 0, 100)
+        m_gpu = lat.get_m()
+        o = lat.energy()
+    m = m0.copy()
+    acc = O.sweeps(c, k, T, 4, 0, 100, m, demag_mode=1)
+    assert o.proposed == 100 * m.shape[1]
+    assert o.accepted == acc
+    assert np.array_equal(m_gpu, m)
+
+
+def test_trajectory_fixture(M):
+    z = np.load(os.path.join(GOLDEN, "trajectory_fp64.npz"))
+    c = M.Config.defaults(nx=8, ny=8, nz=1, pbc_x=2, pbc_y=2, pbc_z=0, precision=64, randomseed=256,
+                          cal_demag_flag=1)
+    with M.Lattice(c) as lat:
+        lat.build_demag()
+        assert np.array_equal(lat.tensor(), z["k6"])
+        assert np.array_equal(lat.get_m(), z["m0"])
+        lat.run_sweeps(float(z["T"][0]), int(z["stage"][0]), 0, 20)
+        assert np.array_equal(lat.get_m(), z["m20"])
+        o = lat.energy()
+    assert o.accepted == int(z["accepted"][0])
+    e = z["e20"]
+    assert abs(o.e_total - e[:5].sum()) <= 1e-11 * np.abs(e[:5]).sum()
+
+
+def test_fp32_tracks_fp64_for_a_few_sweeps(M):
+    """FP32 and FP64 runs share the random stream; with the same start they make
+    the same decisions until a near-tie, so early states agree closely."""
+    c64 = cfg(M, precision=64)
+    c32 = cfg(M, precision=32)
+    with M.Lattice(c64) as a, M.Lattice(c32) as b:
+        b.set_m(a.get_m())
+        a.run_sweeps(300.0, 0, 0, 3)
+        b.run_sweeps(300.0, 0, 0, 3)
+        ma, mb = a.get_m(), b.get_m()
+    same = np.all(np.abs(ma - mb) < 1e-6, axis=0).mean()
+    assert same > 0.99
+
+
+def test_chunked_runs_equal_single_run(M):
+    c = cfg(M, nx=32, ny=32, precision=32)
+    with M.Lattice(c) as a, M.Lattice(c) as b:
+        a.run_sweeps(250.0, 2, 0, 150)  # graph replays + tail
+        for s0, ns in [(0, 10), (10, 64), (74, 76)]:
+            b.run_sweeps(250.0, 2, s0, ns)
+        assert np.array_equal(a.get_m(), b.get_m())
+
+
+def test_demag_apply_on_device_pointers(M):
+    torch = pytest.importorskip("torch")
+    c = cfg(M, nx=20, ny=12, nz=2, pbc_x=1, pbc_y=0, pbc_z=0, precision=32)
+    with M.Lattice(c) as lat:
+        lat.compute_demag()
+        want = lat.field(M.TERM_DEMAG) / c.ms
+        m = lat.get_m()
+        dev = torch.device("cuda:0")
+        mt = torch.tensor(m, dtype=torch.float32, device=dev).contiguous()
+        ht = torch.zeros_like(mt)
+        nb = lat.demag_scratch_bytes()
+        scratch = torch.empty(nb, dtype=torch.uint8, device=dev)
+        torch.cuda.synchronize()
+        lat.demag_apply(mt.data_ptr(), ht.data_ptr(), scratch.data_ptr(), nb, None)
+        lat.compute_demag()  # same stream: orders after demag_apply
+        torch.cuda.synchronize()
+        got = ht.cpu().numpy().astype(np.float64)
+        with pytest.raises(M.MmcError):
+            lat.demag_apply(mt.data_ptr(), ht.data_ptr(), scratch.data_ptr(), nb - 1, None)
+    assert rel(got, want) <= 1e-6
+
+
+def test_tensor_cache_roundtrip(M, tmp_path):
+    c = cfg(M, nx=10, ny=6, nz=1, pbc_x=3, pbc_y=0)
+    with M.Lattice(c) as lat:
+        lat.build_demag(str(tmp_path))
+        k1 = lat.tensor()
+    name = "cache_10_11_1-1e-09_1e-09_8e-10-3_0_0.ovf"
+    f = tmp_path / name
+    assert f.exists() and f.stat().st_size == 6 * 10 * 11 * 1 * 8
+    raw = np.fromfile(f, dtype=np.float64).reshape(6, 10, 11, 1)  # reference layout: x slowest, z fastest
+    assert np.array_equal(raw.transpose(0, 3, 2, 1).reshape(6, -1), k1)
+    # a cached file is used as is: perturb it and read it back
+    raw2 = raw.copy()
+    raw2[5, 0, 0, 0] = 0.5
+    raw2.tofile(f)
+    with M.Lattice(c) as lat:
+        lat.build_demag(str(tmp_path))
+        k2 = lat.tensor()
+    assert k2[5, 0] == 0.5 and np.array_equal(k2[:5], k1[:5])
+
+
+def test_anneal_outputs(M, tmp_path):
+    """The stage loop writes energy.txt ("%f %ld %g") and OVF snapshots named
+    %06ld_%.2fK_%ld.ovf, clearing old images from the output folder."""
+    c = cfg(M, nx=8, ny=8, precision=32, Temperature_start=100.0, Temperature_end=70.0, Temperature_step=0.9,
+            circle_per_stage=20, energy_output_period=10, ms_output_period=15, terminal_output_period=7)
+    out = tmp_path / "run.output"
+    out.mkdir()
+    (out / "old.png").write_text("x")
+    (out / "keep.txt").write_text("x")
+    with M.Lattice(c) as lat:
+        lat.run_anneal(out)
+    assert not (out / "old.png").exists() and (out / "keep.txt").exists()
+    lines = (out / "energy.txt").read_text().splitlines()
+    # float32 temperatures 100, 90, 81, 72.9 (> 70), four stages; energy at sweeps 0 and 10
+    temps = [float(l.split()[0]) for l in lines]
+    assert [l.split()[1] for l in lines] == ["0", "10"] * 4
+    assert temps[::2] == pytest.approx([100.0, 90.0, 81.0, 72.9], rel=1e-6)
+    snaps = sorted(p.name for p in out.glob("*.ovf"))
+    assert snaps[0] == "000000_100.00K_0.ovf" and len(snaps) == 8
+    assert "000001_100.00K_15.ovf" in snaps
+    m = M.ovf_read(out / snaps[-1], 8, 8, 1, c.dx, c.dy, c.dz)
+    np.testing.assert_allclose(np.linalg.norm(m, axis=0), 1, atol=1e-6)
+
+
+def test_stop_request_interrupts(M):
+    import threading
+    import time
+    c = cfg(M, nx=64, ny=64, precision=32)
+    with M.Lattice(c) as lat:
+        lat.build_demag()
+        t = threading.Timer(0.5, lat.request_stop)
+        t.start()
+        t0 = time.time()
+        with pytest.raises(M.MmcError) as ei:
+            lat.run_sweeps(300.0, 0, 0, 10 ** 7)
+        t.cancel()
+        assert ei.value.status == M.ERR_INTERRUPTED
+        assert time.time() - t0 < 30
+        lat.run_sweeps(300.0, 0, 0, 5)  # handle stays usable
+
+
+def test_cli_end_to_end(M, tmp_path):
+    import subprocess
+    ini = tmp_path / "tiny.ini"
+    text = open(os.path.join(os.path.dirname(__file__), "test_host_io.py")).read()
+    body = text.split('README_INI = """')[1].split('"""')[0]
+    body = (body.replace("nx = 256", "nx = 16").replace("ny = 256", "ny = 16")
+            .replace("circle_per_stage  = 100000", "circle_per_stage = 50")
+            .replace("Temperature_end = 40", "Temperature_end = 1100")
+            .replace("pbc_x = 20", "pbc_x = 2").replace("pbc_y = 20", "pbc_y = 2"))
+    ini.write_text(body)
+    cli = os.path.join(M.HERE, "bin", "mmc")
+    cache = tmp_path / "cache"
+    cache.mkdir()
+    r = subprocess.run([cli, str(ini), "-gpu=0", f'-tensorcache="{cache}"'], stdout=subprocess.PIPE,
+                       stderr=subprocess.PIPE, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = tmp_path / "tiny.output"
+    lines = (out / "energy.txt").read_text().splitlines()
+    assert len(lines) == 3  # 1400, 1260, 1134 (> 1100)
+    assert len(list(cache.glob("cache_16_16_1-*.ovf"))) == 1
+    assert len(list(out.glob("*.ovf"))) == 3
