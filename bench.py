@@ -253,32 +253,53 @@ def run_ours(args):
     e2e_t = reduce_max(dist, e2e_t)
     e2e = world * args.steps * S * n / e2e_t
 
-    # per-family attribution with CUDA events on the library's stream
-    prof_sweeps = 500
-    prof = lat.profile_sweeps(stage_temperature(args.warmup), args.warmup, 0, prof_sweeps)
-    fam = {"demag_conv": prof[0] / prof_sweeps, "metropolis_sweep": prof[1] / prof_sweeps}
     s = 4
     nh = (256 // 2 + 1) * 256
-    bytes_fam = {"demag_conv": 6 * s * n + 12 * s * nh, "metropolis_sweep": 9 * s * n}
-    dom = max(fam, key=fam.get)
     peak, peak_kind = measured_peaks()
-    achieved = bytes_fam[dom] / (fam[dom] * 1e-3) / 1e9
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-                "algorithmic_bytes_per_launch": bytes_fam[dom], "avg_ms_per_launch": fam[dom],
-                "family_ms_per_sweep": fam}
+    engine, band, blocks = lat.engine()
+    if engine == M.ENGINE_FUSED:
+        # one cooperative launch per chunk of <= 1024 sweeps: per sweep it reads
+        # and writes m (the demag field stays on chip) and reads K^ once
+        launches = args.steps * ((S + 1023) // 1024)
+        per_launch_ms = 1e3 * total / world / launches
+        sweeps_per_launch = args.steps * S / launches
+        bytes_launch = sweeps_per_launch * (6 * s * n + 12 * s * nh)
+        achieved = bytes_launch / (per_launch_ms * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": "k_fused2d", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                    "algorithmic_bytes_per_launch": bytes_launch, "avg_ms_per_launch": per_launch_ms,
+                    "bytes_per_sweep": "6*4*N (m in/out) + 12*4*N_h (K^), N=65536, N_h=33024",
+                    "band": band, "ctas": blocks}
+        gpu_launches = launches
+    else:
+        prof_sweeps = 500
+        prof = lat.profile_sweeps(stage_temperature(args.warmup), args.warmup, 0, prof_sweeps)
+        fam = {"demag_conv": prof[0] / prof_sweeps, "metropolis_sweep": prof[1] / prof_sweeps}
+        bytes_fam = {"demag_conv": 6 * s * n + 12 * s * nh, "metropolis_sweep": 9 * s * n}
+        dom = max(fam, key=fam.get)
+        achieved = bytes_fam[dom] / (fam[dom] * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                    "algorithmic_bytes_per_launch": bytes_fam[dom], "avg_ms_per_launch": fam[dom],
+                    "family_ms_per_sweep": fam}
+        gpu_launches = args.steps * S * (3 + 2 + 1)
 
     # plain FP64 path on the same workload (fewer sweeps per step)
-    cfg64 = cfg.copy(precision=64)
-    lat64 = M.Lattice(cfg64, device=local)
-    lat64.build_demag(CACHE_DIR)
-    s64 = max(100, S // 10)
-    lat64.run_sweeps(stage_temperature(0), 0, 0, s64)
-    t64 = 0.0
-    for j in range(2):
-        lat64.run_sweeps(stage_temperature(1 + j), 1 + j, 0, s64)
-        t64 += lat64.last_run_ms() / 1e3
-    fp64 = 2 * s64 * n / t64
+    fp64_line = None
+    if not args.no_fp64:
+        cfg64 = cfg.copy(precision=64, sweep_engine=M.ENGINE_KERNELS)
+        lat64 = M.Lattice(cfg64, device=local)
+        lat64.build_demag(CACHE_DIR)
+        s64 = max(100, S // 10)
+        lat64.run_sweeps(stage_temperature(0), 0, 0, s64)
+        t64 = 0.0
+        for j in range(2):
+            lat64.run_sweeps(stage_temperature(1 + j), 1 + j, 0, s64)
+            t64 += lat64.last_run_ms() / 1e3
+        fp64 = 2 * s64 * n / t64
+        lat64.close()
+        fp64_line = {"value": fp64, "unit": UNIT, "sweeps_timed": 2 * s64, "engine": "kernels",
+                     "fp32_over_fp64": value / world / fp64}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -290,9 +311,9 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * n * 8, "d2h_bytes_per_step": 3 * n * 8},
         "roofline": roofline,
         "clocks": clk.summary(),
-        "gpu_launches": args.steps * S * (3 + 2 + 1),
-        "fp64_plain": {"value": fp64, "unit": UNIT, "sweeps_timed": 2 * s64,
-                       "fp32_over_fp64": value / world / fp64},
+        "gpu_launches": gpu_launches,
+        "fp64_plain": fp64_line,
+        "engine": {"name": {1: "kernels", 2: "fused"}[engine], "band": band, "ctas": blocks},
         "setup_s": setup_s,
     }
     if rank == 0 and not args.no_cpu:
@@ -304,7 +325,6 @@ def run_ours(args):
                                 "sample": f"{nsN} FP64 sweeps of the same 256x256x1 lattice (FFT demag)",
                                 "single_thread": v1}
     lat.close()
-    lat64.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -319,6 +339,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

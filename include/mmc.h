@@ -56,6 +56,14 @@ enum mmc_term {
 
 enum mmc_ovf_format { MMC_OVF_BINARY4 = 0, MMC_OVF_BINARY8 = 1, MMC_OVF_TEXT = 2 };
 
+/* How sweeps are executed.  AUTO picks FUSED for films (nz = 1, demag on, two
+ * sublattice colours) and KERNELS otherwise.  Both give bit-identical results. */
+enum mmc_engine {
+  MMC_ENGINE_AUTO = 0,
+  MMC_ENGINE_KERNELS = 1,  /* one kernel per transform pass and colour, replayed from CUDA graphs */
+  MMC_ENGINE_FUSED = 2     /* one persistent cooperative kernel per chunk of sweeps */
+};
+
 /*
  * Simulation parameters.  The first block holds exactly the 26 ini keys of the
  * reference (src/parse_input_ini.h:15-41, example README.md:44-86) with the
@@ -87,6 +95,8 @@ typedef struct mmc_config {
   int ovf_format;                          /* enum mmc_ovf_format, default MMC_OVF_BINARY4 */
   int use_reference_pi;                    /* 1: pi = 3.14159265358 as src/constant.h:21 */
   char tensor_cache[1024];                 /* directory for the demag tensor cache ("" = off) */
+  int sweep_engine;                        /* enum mmc_engine, default MMC_ENGINE_AUTO */
+  int fused_band;                          /* rows per CTA of the fused film engine, 0 = auto */
 } mmc_config;
 
 typedef struct mmc_observables {
@@ -144,7 +154,7 @@ int mmc_get_m(mmc_handle* h, double* mx, double* my, double* mz);
 int mmc_build_demag(mmc_handle* h, const char* cache_dir);
 
 /* The real-space tensor: 6 blocks (xx,xy,xz,yy,yz,zz) of nxp*nyp*nzp doubles,
- * x fastest within a block. */
+ * x fastest within a block (built first if needed). */
 int mmc_get_tensor(mmc_handle* h, double* k6);
 
 /* Replaces calDemagMirrorTensor (src/demag_mirror.h:18-24): the tensor at zero
@@ -184,6 +194,10 @@ int mmc_energy(mmc_handle* h, mmc_observables* out);
  * so splitting a stage into several calls gives the same result. */
 int mmc_run_sweeps(mmc_handle* h, double temperature, long long stage, long long sweep0,
                    long long nsweeps);
+
+/* The sweep engine chosen at creation: out[0] = enum mmc_engine (never AUTO),
+ * out[1] = rows per CTA of the fused engine, out[2] = its CTA count. */
+int mmc_engine_info(mmc_handle* h, int out[3]);
 
 /* Device time, in ms, of the last mmc_run_sweeps() call: CUDA events recorded
  * on the handle's stream around the enqueued sweeps. */

@@ -102,7 +102,7 @@ const KeyDef kKeys[] = {
     KD(energy_output_period, K_LL, true), KD(ms_output_period, K_LL, true),
     KD(rand_block_size, K_INT, true), KD(cal_demag_flag, K_BOOL, true),
     // optional keys of this library
-    KD(use_reference_pi, K_BOOL, false), KD(tensor_cache, K_STR, false),
+    KD(use_reference_pi, K_BOOL, false), KD(tensor_cache, K_STR, false), KD(fused_band, K_INT, false),
 };
 #undef KD
 
@@ -149,6 +149,8 @@ int config_validate(const mmc_config* c) {
   if (c->precision != 32 && c->precision != 64)
     return fail(MMC_ERR_CONFIG, "precision must be 32 or 64");
   if (c->ovf_format < 0 || c->ovf_format > 2) return fail(MMC_ERR_CONFIG, "bad ovf_format");
+  if (c->sweep_engine < 0 || c->sweep_engine > 2) return fail(MMC_ERR_CONFIG, "bad sweep_engine");
+  if (c->fused_band < 0 || c->fused_band > 60) return fail(MMC_ERR_CONFIG, "fused_band must be in [0, 60]");
   if (c->circle_per_stage < 0) return fail(MMC_ERR_CONFIG, "circle_per_stage must be >= 0");
   if (c->terminal_output_period < 1 || c->energy_output_period < 1 || c->ms_output_period < 1)
     return fail(MMC_ERR_CONFIG, "output periods must be >= 1");
@@ -201,6 +203,14 @@ int config_load_ini(const std::string& path, mmc_config* cfg) {
       else if (v == "binary8" || v == "binary 8") c.ovf_format = MMC_OVF_BINARY8;
       else if (v == "text") c.ovf_format = MMC_OVF_TEXT;
       else return fail(MMC_ERR_CONFIG, "ovf_format must be binary4, binary8 or text, got " + val);
+      continue;
+    }
+    if (key == "sweep_engine") {
+      std::string v = lower(val);
+      if (v == "auto") c.sweep_engine = MMC_ENGINE_AUTO;
+      else if (v == "kernels") c.sweep_engine = MMC_ENGINE_KERNELS;
+      else if (v == "fused") c.sweep_engine = MMC_ENGINE_FUSED;
+      else return fail(MMC_ERR_CONFIG, "sweep_engine must be auto, kernels or fused, got " + val);
       continue;
     }
     const KeyDef* kd = nullptr;

@@ -260,53 +260,51 @@ struct Prop<float> {
   __device__ static bool accept(float dE, float ua) { return dE <= 0.0f || ua < __expf(-dE); }
 };
 
+// Neighbour values of one trial: v[a][s] is the neighbour along axis a on side
+// s (0 = -, 1 = +); has[a][s] tells whether that bond exists.
 template <typename T>
-__device__ __forceinline__ bool mc_trial(const Geom& g, const McCoef<T>& c, T* __restrict__ m,
-                                         const T* __restrict__ h, uint32_t stage, uint32_t sweep, int x, int y,
-                                         int z) {
-  const long long n = g.n;
-  T* mx = m;
-  T* my = m + n;
-  T* mz = m + 2 * n;
-  const long long i = x + (long long)g.nx * (y + (long long)g.ny * z);
+struct Nbrs {
+  T v[3][2][3];
+  bool has[3][2];
+};
+
+// The Metropolis decision for one cell from its neighbour values, its own m,
+// its demag field h and its counter.  Shared by every sweep kernel so that
+// all paths round identically.  Returns true and the proposal on accept.
+template <typename T>
+__device__ __forceinline__ bool mc_decide(const McCoef<T>& c, const Nbrs<T>& nb, T ox, T oy, T oz, T hx, T hy, T hz,
+                                          uint32_t cell, uint32_t stage, uint32_t sweep, T& px, T& py, T& pz) {
   T Fx = 0, Fy = 0, Fz = 0;
-  long long nb[3][2];
 #pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    nb[a][0] = nbr_idx(g, x, y, z, a, -1);
-    nb[a][1] = nbr_idx(g, x, y, z, a, 1);
+  for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      const long long j = nb[a][s];
-      if (j < 0) continue;
-      Fx = Fx + c.wex[a] * mx[j];
-      Fy = Fy + c.wex[a] * my[j];
-      Fz = Fz + c.wex[a] * mz[j];
+      if (!nb.has[a][s]) continue;
+      Fx = Fx + c.wex[a] * nb.v[a][s][0];
+      Fy = Fy + c.wex[a] * nb.v[a][s][1];
+      Fz = Fz + c.wex[a] * nb.v[a][s][2];
     }
-  }
-  const long long xm = nb[0][0], xp = nb[0][1], ym = nb[1][0], yp = nb[1][1];
-  const T dxmz = (xp >= 0 ? mz[xp] : (T)0) - (xm >= 0 ? mz[xm] : (T)0);
-  const T dxmx = (xp >= 0 ? mx[xp] : (T)0) - (xm >= 0 ? mx[xm] : (T)0);
-  const T dymz = (yp >= 0 ? mz[yp] : (T)0) - (ym >= 0 ? mz[ym] : (T)0);
-  const T dymy = (yp >= 0 ? my[yp] : (T)0) - (ym >= 0 ? my[ym] : (T)0);
+  const T dxmz = (nb.has[0][1] ? nb.v[0][1][2] : (T)0) - (nb.has[0][0] ? nb.v[0][0][2] : (T)0);
+  const T dxmx = (nb.has[0][1] ? nb.v[0][1][0] : (T)0) - (nb.has[0][0] ? nb.v[0][0][0] : (T)0);
+  const T dymz = (nb.has[1][1] ? nb.v[1][1][2] : (T)0) - (nb.has[1][0] ? nb.v[1][0][2] : (T)0);
+  const T dymy = (nb.has[1][1] ? nb.v[1][1][1] : (T)0) - (nb.has[1][0] ? nb.v[1][0][1] : (T)0);
   Fx = Fx + c.wdm[0] * dxmz;
   Fy = Fy + c.wdm[1] * dymz;
   Fz = Fz - (c.wdm[0] * dxmx + c.wdm[1] * dymy);
   Fx = Fx + c.cz[0];
   Fy = Fy + c.cz[1];
   Fz = Fz + c.cz[2];
-  const T ox = mx[i], oy = my[i], oz = mz[i];
   if (c.cd != (T)0) {
     const T sx = c.k0[0] * ox + c.k0[1] * oy + c.k0[2] * oz;
     const T sy = c.k0[1] * ox + c.k0[3] * oy + c.k0[4] * oz;
     const T sz = c.k0[2] * ox + c.k0[4] * oy + c.k0[5] * oz;
-    Fx = Fx + c.cd * (h[i] - sx);
-    Fy = Fy + c.cd * (h[n + i] - sy);
-    Fz = Fz + c.cd * (h[2 * n + i] - sz);
+    Fx = Fx + c.cd * (hx - sx);
+    Fy = Fy + c.cd * (hy - sy);
+    Fz = Fz + c.cd * (hz - sz);
   }
-  mmcm::u32x4 ctr = {(uint32_t)i, sweep, stage, mmcm::STREAM_SWEEP};
+  mmcm::u32x4 ctr = {cell, sweep, stage, mmcm::STREAM_SWEEP};
   mmcm::u32x4 r = mmcm::philox4x32_10(ctr, c.key0, c.key1);
-  T px, py, pz, ua;
+  T ua;
   Prop<T>::draw(r, px, py, pz, ua);
   const T ddx = px - ox, ddy = py - oy, ddz = pz - oz;
   T dE = -(ddx * Fx + ddy * Fy + ddz * Fz);
@@ -320,7 +318,39 @@ __device__ __forceinline__ bool mc_trial(const Geom& g, const McCoef<T>& c, T* _
                  oz * (c.k0[2] * ox + c.k0[4] * oy + c.k0[5] * oz);
     dE = dE - (T)0.5 * c.cd * (qn - qo);
   }
-  if (Prop<T>::accept(dE, ua)) {
+  return Prop<T>::accept(dE, ua);
+}
+
+template <typename T>
+__device__ __forceinline__ bool mc_trial(const Geom& g, const McCoef<T>& c, T* __restrict__ m,
+                                         const T* __restrict__ h, uint32_t stage, uint32_t sweep, int x, int y,
+                                         int z) {
+  const long long n = g.n;
+  T* mx = m;
+  T* my = m + n;
+  T* mz = m + 2 * n;
+  const long long i = x + (long long)g.nx * (y + (long long)g.ny * z);
+  Nbrs<T> nb;
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const long long j = nbr_idx(g, x, y, z, a, s ? 1 : -1);
+      nb.has[a][s] = j >= 0;
+      const long long jj = j >= 0 ? j : i;
+      nb.v[a][s][0] = mx[jj];
+      nb.v[a][s][1] = my[jj];
+      nb.v[a][s][2] = mz[jj];
+    }
+  const T ox = mx[i], oy = my[i], oz = mz[i];
+  T hx = 0, hy = 0, hz = 0;
+  if (c.cd != (T)0) {
+    hx = h[i];
+    hy = h[n + i];
+    hz = h[2 * n + i];
+  }
+  T px, py, pz;
+  if (mc_decide<T>(c, nb, ox, oy, oz, hx, hy, hz, (uint32_t)i, stage, sweep, px, py, pz)) {
     mx[i] = px;
     my[i] = py;
     mz[i] = pz;

@@ -1,7 +1,9 @@
 // kernels_f32.cu -- FP32 instantiation of the hot-path kernels (multiply-add
 // contraction enabled).
+#include "fused2d.cuh"
 #include "kernels.cuh"
 
 namespace mmc {
 MMC_INSTANTIATE_LAUNCHERS(float)
+MMC_INSTANTIATE_FUSED(float)
 }  // namespace mmc

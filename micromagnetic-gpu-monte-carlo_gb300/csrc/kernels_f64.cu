@@ -4,12 +4,17 @@
 // the CPU oracle built with -ffp-contract=off.
 #include <curand_kernel.h>
 
+#include "fused2d.cuh"
 #include "kernels.cuh"
 
 namespace mmc {
 MMC_INSTANTIATE_LAUNCHERS(double)
+MMC_INSTANTIATE_FUSED(double)
 
 int energy_partials_count(const Geom& g) { return energy_blocks(g); }
+
+size_t grid_barrier_bytes() { return sizeof(GridBarrier); }
+int grid_barrier_error(const GridBarrier* b) { return b->err; }
 
 // Forward transform of the six real tensor blocks k6[c][z][y][x] (padded
 // grid) into spec64[c][kz][ky][kx] (src/main.cu:593-642 ran cuFFT D2Z here).

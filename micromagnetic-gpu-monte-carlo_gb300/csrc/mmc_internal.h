@@ -108,6 +108,7 @@ cudaError_t launch_field(const Geom& g, const HCoef& c, int term, const T* m, co
                          cudaStream_t st);
 template <typename T>
 cudaError_t launch_init(const Geom& g, uint64_t seed, T* m, cudaStream_t st);
+// Raises the dynamic shared-memory limit of every pass kernel (once per device).
 template <typename T>
 cudaError_t launch_prepare(int max_dyn_smem);
 template <typename T>
@@ -127,5 +128,30 @@ cudaError_t launch_philox_selftest(long long n, const uint32_t* ctr, uint32_t k0
                                    uint32_t* out_curand, cudaStream_t st);
 
 int energy_partials_count(const Geom& g);
+
+// Persistent film engine (fused2d.cuh).
+struct GridBarrier;
+template <typename T>
+struct FusedArgs {
+  const McCoef<T>* coef;
+  T* m;
+  T* h;
+  void* spec;
+  const void* khat;
+  unsigned long long* acc;
+  GridBarrier* bar;
+  uint32_t stage, sweep0;
+  int nsweeps;
+  int band;
+};
+template <typename T>
+size_t fused2d_smem_bytes(const Geom& g, const FftPlan& px, const FftPlan& py, int band);
+template <typename T>
+cudaError_t fused2d_blocks_per_sm(const Geom& g, const FftPlan& px, const FftPlan& py, int band, int* out);
+template <typename T>
+cudaError_t launch_fused2d(const Geom& g, const FftPlan& px, const FftPlan& py, const FusedArgs<T>& a, int nblocks,
+                           cudaStream_t st);
+size_t grid_barrier_bytes();
+int grid_barrier_error(const GridBarrier* host_copy);
 
 }  // namespace mmc

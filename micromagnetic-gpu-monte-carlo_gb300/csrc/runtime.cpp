@@ -189,6 +189,11 @@ struct mmc_handle {
   long long seed = 0;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   double last_run_ms = 0;
+  // persistent film engine
+  int engine = MMC_ENGINE_KERNELS;
+  int fused_band = 0;
+  int fused_blocks = 0;
+  GridBarrier* bar = nullptr;
 };
 
 namespace {
@@ -340,6 +345,95 @@ int ensure_demag(mmc_handle* h) {
   return build_demag_impl(h, h->cfg.tensor_cache);
 }
 
+// The persistent film engine: chunks of at most 1024 sweeps per cooperative
+// launch; a stop request is honoured between chunks, a barrier timeout inside
+// the kernel is reported as MMC_ERR_TIMEOUT.
+template <typename T>
+cudaError_t fused_chunk(mmc_handle* h, long long stage, long long sweep0, int ns) {
+  FusedArgs<T> a;
+  a.coef = (const McCoef<T>*)h->coef;
+  a.m = (T*)h->m;
+  a.h = (T*)h->h;
+  a.spec = h->spec;
+  a.khat = h->khat;
+  a.acc = h->acc;
+  a.bar = h->bar;
+  a.stage = (uint32_t)stage;
+  a.sweep0 = (uint32_t)sweep0;
+  a.nsweeps = ns;
+  a.band = h->fused_band;
+  return launch_fused2d<T>(h->g, h->px.p, h->py.p, a, h->fused_blocks, h->st);
+}
+
+int run_fused(mmc_handle* h, long long stage, long long sweep0, long long nsweeps) {
+  CU(cudaEventRecord(h->ev[0], h->st));
+  long long done = 0;
+  while (done < nsweeps) {
+    if (h->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
+    const int ns = (int)std::min<long long>(1024, nsweeps - done);
+    CU(h->prec == 32 ? fused_chunk<float>(h, stage, sweep0 + done, ns)
+                     : fused_chunk<double>(h, stage, sweep0 + done, ns));
+    done += ns;
+    if ((done / 1024) % 8 == 0 || done == nsweeps) {
+      CU(cudaStreamSynchronize(h->st));
+      std::vector<unsigned char> hb(grid_barrier_bytes());
+      CU(cudaMemcpy(hb.data(), h->bar, hb.size(), cudaMemcpyDeviceToHost));
+      if (grid_barrier_error(reinterpret_cast<const GridBarrier*>(hb.data())))
+        return fail(MMC_ERR_TIMEOUT, "grid barrier wait ran out of its budget in the film engine");
+    }
+  }
+  CU(cudaEventRecord(h->ev[1], h->st));
+  CU(cudaStreamSynchronize(h->st));
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+  h->last_run_ms = ms;
+  h->proposed += (unsigned long long)nsweeps * (unsigned long long)h->g.n;
+  return MMC_OK;
+}
+
+// Picks the film engine's band (rows per CTA) and CTA count: the smallest band
+// from the preference list whose grid is co-resident.
+int setup_engine(mmc_handle* h, int nsm) {
+  const mmc_config& c = h->cfg;
+  const Geom& g = h->g;
+  const bool eligible = c.cal_demag_flag && g.nz == 1 && g.nzp == 1 && g.ncolors == 2;
+  if (c.sweep_engine == MMC_ENGINE_KERNELS || (c.sweep_engine == MMC_ENGINE_AUTO && !eligible)) {
+    h->engine = MMC_ENGINE_KERNELS;
+    return MMC_OK;
+  }
+  if (!eligible)
+    return fail(MMC_ERR_UNSUPPORTED, "the fused engine needs a film (nz = 1), demag on and an even or open lattice");
+  int optin = 48 * 1024;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+  std::vector<int> bands;
+  if (c.fused_band > 0) bands.push_back(c.fused_band);
+  else bands = {2, 1, 3, 4, 6, 8, 12, 16, 24, 32, 48, 60};
+  for (int b : bands) {
+    const size_t smem = h->prec == 32 ? fused2d_smem_bytes<float>(g, h->px.p, h->py.p, b)
+                                      : fused2d_smem_bytes<double>(g, h->px.p, h->py.p, b);
+    if (smem > (size_t)optin) continue;
+    int per_sm = 0;
+    cudaError_t e = h->prec == 32 ? fused2d_blocks_per_sm<float>(g, h->px.p, h->py.p, b, &per_sm)
+                                  : fused2d_blocks_per_sm<double>(g, h->px.p, h->py.p, b, &per_sm);
+    if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("occupancy query: ") + cudaGetErrorString(e));
+    const int blocks = (g.ny + b - 1) / b;
+    if (per_sm > 0 && blocks <= per_sm * nsm) {
+      h->engine = MMC_ENGINE_FUSED;
+      h->fused_band = b;
+      h->fused_blocks = blocks;
+      void* p = nullptr;
+      CU(cudaMalloc(&p, grid_barrier_bytes()));
+      CU(cudaMemset(p, 0, grid_barrier_bytes()));
+      h->bar = (GridBarrier*)p;
+      return MMC_OK;
+    }
+  }
+  if (c.sweep_engine == MMC_ENGINE_FUSED)
+    return fail(MMC_ERR_UNSUPPORTED, "no film-engine band fits this lattice on this device");
+  h->engine = MMC_ENGINE_KERNELS;
+  return MMC_OK;
+}
+
 // Runs `nsweeps` sweeps with counters (stage, sweep0); graph replays for the bulk.
 int run_sweeps_impl(mmc_handle* h, double T_K, long long stage, long long sweep0, long long nsweeps) {
   if (nsweeps <= 0) return MMC_OK;
@@ -348,6 +442,7 @@ int run_sweeps_impl(mmc_handle* h, double T_K, long long stage, long long sweep0
   SweepCounters c0{(uint32_t)stage, (uint32_t)sweep0};
   CU(cudaMemcpyAsync(h->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st));
   CU(cudaStreamSynchronize(h->st));
+  if (h->engine == MMC_ENGINE_FUSED) return run_fused(h, stage, sweep0, nsweeps);
   const int G = 64;
   long long done = 0;
   CU(cudaEventRecord(h->ev[0], h->st));
@@ -598,7 +693,8 @@ void destroy_impl(mmc_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
-  void* bufs[] = {h->m, h->h, h->spec, h->khat, h->coef, h->partials, h->red, h->acc, h->ctr, h->stage64, h->field64};
+  void* bufs[] = {h->m,   h->h,   h->spec,    h->khat,    h->coef,   h->partials,
+                  h->red, h->acc, h->ctr,     h->stage64, h->field64, (void*)h->bar};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->red_host) cudaFreeHost(h->red_host);
@@ -695,6 +791,7 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   if (cudaMemset(h->acc, 0, sizeof(unsigned long long)) != cudaSuccess ||
       cudaMemset(h->h, 0, 3 * g.n * h->tsize) != cudaSuccess)
     return bail(fail(MMC_ERR_CUDA, "memset failed"));
+  if ((st = setup_engine(h, nsm)) != MMC_OK) return bail(st);
   // initial magnetisation (src/main.cu:289-333)
   if (cfg->use_random_init) {
     cudaError_t e = h->prec == 32 ? launch_init<float>(g, (uint64_t)h->seed, (float*)h->m, h->st)
@@ -903,14 +1000,18 @@ int mmc_build_demag(mmc_handle* h, const char* cache_dir) {
 
 int mmc_get_tensor(mmc_handle* h, double* k6) {
   if (!h || !k6) return fail(MMC_ERR_INVALID, "null argument");
-  if (!h->demag_built) return fail(MMC_ERR_STATE, "demag tensor not built");
+  TRY(set_dev(h));
+  TRY(ensure_demag(h));
+  if (!h->demag_built) return fail(MMC_ERR_STATE, "demag tensor not built (cal_demag_flag is off)");
   std::memcpy(k6, h->tensor.data(), h->tensor.size() * sizeof(double));
   return MMC_OK;
 }
 
 int mmc_self_tensor(mmc_handle* h, double k6[6]) {
   if (!h || !k6) return fail(MMC_ERR_INVALID, "null argument");
-  if (!h->demag_built) return fail(MMC_ERR_STATE, "demag tensor not built");
+  TRY(set_dev(h));
+  TRY(ensure_demag(h));
+  if (!h->demag_built) return fail(MMC_ERR_STATE, "demag tensor not built (cal_demag_flag is off)");
   for (int q = 0; q < 6; ++q) k6[q] = h->k0[q];
   return MMC_OK;
 }
@@ -1004,6 +1105,14 @@ int mmc_run_anneal(mmc_handle* h, const char* output_dir, int verbose) {
   h->stop.store(0);
   TRY(prepare_output_dir(output_dir));
   return h->prec == 32 ? anneal_loop<float>(h, output_dir, verbose) : anneal_loop<double>(h, output_dir, verbose);
+}
+
+int mmc_engine_info(mmc_handle* h, int out[3]) {
+  if (!h || !out) return fail(MMC_ERR_INVALID, "null argument");
+  out[0] = h->engine;
+  out[1] = h->fused_band;
+  out[2] = h->fused_blocks;
+  return MMC_OK;
 }
 
 int mmc_last_run_ms(mmc_handle* h, double* ms) {

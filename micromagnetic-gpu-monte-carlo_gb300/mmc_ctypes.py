@@ -23,6 +23,7 @@ ERR_INVALID, ERR_CONFIG, ERR_IO, ERR_CUDA, ERR_NO_DEVICE = 1, 2, 3, 4, 5
 ERR_UNSUPPORTED, ERR_INTERRUPTED, ERR_TIMEOUT, ERR_STATE, ERR_OOM = 6, 7, 8, 9, 10
 TERM_EXCHANGE, TERM_DMI, TERM_ANISOTROPY, TERM_ZEEMAN, TERM_DEMAG, TERM_TOTAL = range(6)
 OVF_BINARY4, OVF_BINARY8, OVF_TEXT = 0, 1, 2
+ENGINE_AUTO, ENGINE_KERNELS, ENGINE_FUSED = 0, 1, 2
 
 
 class Config(ctypes.Structure):
@@ -50,6 +51,8 @@ class Config(ctypes.Structure):
         ("ovf_format", ctypes.c_int),
         ("use_reference_pi", ctypes.c_int),
         ("tensor_cache", ctypes.c_char * 1024),
+        ("sweep_engine", ctypes.c_int),
+        ("fused_band", ctypes.c_int),
     ]
 
     @classmethod
@@ -141,6 +144,7 @@ def lib(path=None):
         "mmc_run_anneal": (ctypes.c_int, [H, ctypes.c_char_p, ctypes.c_int]),
         "mmc_request_stop": (None, [H]),
         "mmc_last_run_ms": (ctypes.c_int, [H, _dp]),
+        "mmc_engine_info": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int)]),
         "mmc_profile_sweeps": (ctypes.c_int, [H, ctypes.c_double, ctypes.c_longlong, ctypes.c_longlong,
                                               ctypes.c_longlong, _dp]),
         "mmc_ovf_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -284,6 +288,12 @@ class Lattice:
 
     def run_anneal(self, outdir, verbose=False):
         check(lib().mmc_run_anneal(self.h, str(outdir).encode(), 1 if verbose else 0))
+
+    def engine(self):
+        """(engine, band, blocks) actually used for sweeps."""
+        out = (ctypes.c_int * 3)()
+        check(lib().mmc_engine_info(self.h, out))
+        return tuple(out)
 
     def last_run_ms(self):
         v = ctypes.c_double()

@@ -296,3 +296,76 @@ def test_cli_end_to_end(M, tmp_path):
     assert len(lines) == 3  # 1400, 1260, 1134 (> 1100)
     assert len(list(cache.glob("cache_16_16_1-*.ovf"))) == 1
     assert len(list(out.glob("*.ovf"))) == 3
+
+
+FILMS = {
+    "periodic32": dict(nx=32, ny=32, pbc_x=2, pbc_y=2),
+    "open20x12": dict(nx=20, ny=12, pbc_x=0, pbc_y=0),
+    "mixed24x10": dict(nx=24, ny=10, pbc_x=1, pbc_y=0),
+    "ny2_periodic": dict(nx=16, ny=2, pbc_x=1, pbc_y=1),
+    "ny3_open": dict(nx=18, ny=3, pbc_x=1, pbc_y=0),
+    "ny1": dict(nx=12, ny=1, pbc_x=1, pbc_y=0),
+    "rect_x96": dict(nx=96, ny=6, pbc_x=1, pbc_y=-1),
+}
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("film", sorted(FILMS))
+def test_fused_engine_bitwise_equals_kernels(M, film, prec):
+    c = cfg(M, precision=prec, **FILMS[film])
+    ck = c.copy(sweep_engine=M.ENGINE_KERNELS)
+    cf = c.copy(sweep_engine=M.ENGINE_FUSED)
+    with M.Lattice(ck) as a, M.Lattice(cf) as b:
+        assert a.engine()[0] == M.ENGINE_KERNELS and b.engine()[0] == M.ENGINE_FUSED
+        a.run_sweeps(180.0, 5, 0, 37)
+        b.run_sweeps(180.0, 5, 0, 37)
+        oa, ob = a.energy(), b.energy()
+        assert np.array_equal(a.get_m(), b.get_m())
+        assert oa.accepted == ob.accepted and oa.proposed == ob.proposed
+        # the demag field left behind is the one of the last sweep's start in both
+        assert np.array_equal(a.field(M.TERM_DEMAG), b.field(M.TERM_DEMAG))
+
+
+@pytest.mark.parametrize("band", [1, 2, 3, 5, 16])
+def test_fused_band_sizes(M, band):
+    c = cfg(M, nx=40, ny=30, pbc_x=1, pbc_y=1, precision=32)
+    with M.Lattice(c.copy(sweep_engine=M.ENGINE_KERNELS)) as a, \
+            M.Lattice(c.copy(sweep_engine=M.ENGINE_FUSED, fused_band=band)) as b:
+        assert b.engine()[1] == band and b.engine()[2] == (30 + band - 1) // band
+        a.run_sweeps(250.0, 1, 3, 20)
+        b.run_sweeps(250.0, 1, 3, 20)
+        assert np.array_equal(a.get_m(), b.get_m())
+
+
+def test_fused_fp64_decisions_match_oracle(M, O):
+    c = cfg(M, nx=24, ny=20, pbc_x=2, pbc_y=0, precision=64, sweep_engine=M.ENGINE_FUSED)
+    with M.Lattice(c) as lat:
+        m0 = lat.get_m()
+        k = lat.tensor()
+        lat.run_sweeps(90.0, 2, 0, 100)
+        m_gpu = lat.get_m()
+        o = lat.energy()
+    m = m0.copy()
+    acc = O.sweeps(c, k, 90.0, 2, 0, 100, m, demag_mode=1)
+    assert o.accepted == acc
+    assert np.array_equal(m_gpu, m)
+
+
+def test_fused_long_run_spans_several_launches(M):
+    c = cfg(M, nx=64, ny=64, pbc_x=1, pbc_y=1, precision=32)
+    with M.Lattice(c.copy(sweep_engine=M.ENGINE_KERNELS)) as a, M.Lattice(c.copy(sweep_engine=M.ENGINE_FUSED)) as b:
+        a.run_sweeps(400.0, 0, 0, 2500)
+        b.run_sweeps(400.0, 0, 0, 2500)
+        assert np.array_equal(a.get_m(), b.get_m())
+
+
+def test_engine_auto_selection(M):
+    with M.Lattice(cfg(M, nx=16, ny=16)) as lat:
+        assert lat.engine()[0] == M.ENGINE_FUSED
+    with M.Lattice(cfg(M, nx=6, ny=5, nz=4, pbc_x=0, pbc_y=0, pbc_z=0)) as lat:
+        assert lat.engine()[0] == M.ENGINE_KERNELS
+    with M.Lattice(cfg(M, nx=15, ny=8, pbc_x=1)) as lat:  # odd periodic: three colours
+        assert lat.engine()[0] == M.ENGINE_KERNELS
+    with pytest.raises(M.MmcError) as ei:
+        M.Lattice(cfg(M, nx=15, ny=8, pbc_x=1, sweep_engine=M.ENGINE_FUSED))
+    assert ei.value.status == M.ERR_UNSUPPORTED
