@@ -210,6 +210,15 @@ int mmc_last_run_ms(mmc_handle* h, double* ms);
 int mmc_profile_sweeps(mmc_handle* h, double temperature, long long stage, long long sweep0, long long nsweeps,
                        double out_ms[3]);
 
+/* Profiling hook of the fused film engine: runs nsweeps (<= 1024) sweeps in
+ * one launch and returns device timestamps (ns) of the phase boundaries of the
+ * first 16 sweeps for the first and the last CTA: stamps[(s*9 + p)*2 + c],
+ * points p = 0 row phase start, 1 copies landed, 2 demag field ready,
+ * 3 Metropolis done, 4 spectrum rows stored, 5 after barrier, 6 column copies
+ * landed, 7 column phase done, 8 after barrier.  stamps holds 288 words. */
+int mmc_profile_fused(mmc_handle* h, double temperature, long long stage, long long sweep0, long long nsweeps,
+                      unsigned long long* stamps);
+
 /* The whole temperature-stage loop of src/main.cu:801-1139 with its outputs
  * (energy.txt, %06ld_%.2fK_%ld.ovf snapshots) written into output_dir.
  * verbose != 0 prints progress lines to stdout. */
@@ -218,6 +227,39 @@ int mmc_run_anneal(mmc_handle* h, const char* output_dir, int verbose);
 /* Asks a running call on another thread (or a signal handler) to stop at the
  * next sweep boundary; that call returns MMC_ERR_INTERRUPTED. */
 void mmc_request_stop(mmc_handle* h);
+
+/* ---------------------------------------------------------------- batches
+ * No counterpart in the reference, which runs one lattice per process.  A
+ * batch advances nrep replicas of one geometry together (every kernel launch
+ * covers all replicas), for seed ensembles and parallel tempering.  Replicas
+ * share nx, ny, nz, cell size, pbc, precision and the demag flag; material,
+ * field, seed and temperature are per replica.  Each replica's trajectory is
+ * the one a single handle with the same config produces (same Philox streams,
+ * same arithmetic). */
+typedef struct mmc_batch mmc_batch;
+int mmc_batch_create(const mmc_config* cfgs, int nrep, int device, mmc_batch** out);
+void mmc_batch_destroy(mmc_batch* b);
+int mmc_batch_size(mmc_batch* b);
+int mmc_batch_build_demag(mmc_batch* b, const char* cache_dir);
+/* Per-replica temperatures (K); default Temperature_start of each config. */
+int mmc_batch_set_temperatures(mmc_batch* b, const double* T);
+int mmc_batch_get_temperatures(mmc_batch* b, double* T);
+/* Parallel tempering: nladders ladders of per_ladder replicas; ladder l's
+ * replicas[l*per_ladder + k] starts at temps[l*per_ladder + k] (ascending).
+ * After every swap_interval sweeps (counted by the global sweep index) the
+ * device evaluates all energies and attempts swaps of neighbouring
+ * temperatures, alternating even and odd pairs, keyed by `seed`. */
+int mmc_batch_set_ladders(mmc_batch* b, int nladders, int per_ladder, const int* replicas, const double* temps,
+                          int swap_interval, long long seed);
+/* Current replica at each ladder slot and the swap counts {attempted, accepted}. */
+int mmc_batch_ladder_state(mmc_batch* b, int* replicas, unsigned long long counts[2]);
+int mmc_batch_run_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps);
+int mmc_batch_last_run_ms(mmc_batch* b, double* ms);
+void mmc_batch_request_stop(mmc_batch* b);
+/* Observables of every replica (out holds nrep entries). */
+int mmc_batch_energy(mmc_batch* b, mmc_observables* out);
+int mmc_batch_set_m(mmc_batch* b, int replica, const double* mx, const double* my, const double* mz);
+int mmc_batch_get_m(mmc_batch* b, int replica, double* mx, double* my, double* mz);
 
 /* OVF 1.0/2.0 reader (parseOvfFile, src/ovf_io.h:88-91): text, binary 4 and
  * binary 8 data; dimensions must match and step sizes agree within 1e-5

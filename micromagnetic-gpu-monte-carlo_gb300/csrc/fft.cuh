@@ -73,7 +73,8 @@ __device__ __forceinline__ void load_twiddles(const FftPlan& p, C<T>* dst) {
 // `a` holds the input, `b` is scratch of the same shape.  Returns the buffer
 // holding the result (a or b).  All threads of the block must call it.
 template <typename T, bool INV>
-__device__ C<T>* fft_lines(C<T>* a, C<T>* b, int nlines, int stride, const FftPlan& p, const C<T>* tw) {
+__device__ __noinline__ C<T>* fft_lines(C<T>* a, C<T>* b, int nlines, int stride, const FftPlan& p,
+                                        const C<T>* tw) {
   using V = C<T>;
   V* src = a;
   V* dst = b;
@@ -160,6 +161,133 @@ __device__ C<T>* fft_lines(C<T>* a, C<T>* b, int nlines, int stride, const FftPl
     dst = t;
   }
   return src;
+}
+
+// ------------------------------------------------------------ warp-level FFT
+// 16th roots of unity exp(-2 pi i k / 16), k = 0..7 (cos, -sin).
+__device__ __forceinline__ double w16_re(int k) {
+  const double c[8] = {1.0, 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173,
+                       0.0, -0.38268343236508977173, -0.70710678118654752440, -0.92387953251128675613};
+  return c[k];
+}
+__device__ __forceinline__ double w16_im(int k) {
+  const double s[8] = {0.0, -0.38268343236508977173, -0.70710678118654752440, -0.92387953251128675613,
+                       -1.0, -0.92387953251128675613, -0.70710678118654752440, -0.38268343236508977173};
+  return s[k];
+}
+
+// In-register DFT of N in {1, 2, 4, 8, 16} values, natural order in and out,
+// by radix-2 decimation in time.  INV uses the conjugate roots.
+template <typename T, bool INV, int N>
+struct RegDft {
+  __device__ __forceinline__ static void run(C<T>* v) {
+    using V = C<T>;
+    V e[N / 2], o[N / 2];
+#pragma unroll
+    for (int i = 0; i < N / 2; ++i) {
+      e[i] = v[2 * i];
+      o[i] = v[2 * i + 1];
+    }
+    RegDft<T, INV, N / 2>::run(e);
+    RegDft<T, INV, N / 2>::run(o);
+#pragma unroll
+    for (int k = 0; k < N / 2; ++k) {
+      V t;
+      if (k == 0) {
+        t = o[k];
+      } else if (4 * k == N) {  // multiply by -i (forward) or +i (inverse)
+        t = INV ? cmk<V>(-o[k].y, o[k].x) : cmk<V>(o[k].y, -o[k].x);
+      } else {
+        const T wr = (T)w16_re(k * (16 / N));
+        const T wi = INV ? (T)-w16_im(k * (16 / N)) : (T)w16_im(k * (16 / N));
+        t = cmk<V>(o[k].x * wr - o[k].y * wi, o[k].x * wi + o[k].y * wr);
+      }
+      v[k] = cadd(e[k], t);
+      v[k + N / 2] = csub(e[k], t);
+    }
+  }
+};
+template <typename T, bool INV>
+struct RegDft<T, INV, 1> {
+  __device__ __forceinline__ static void run(C<T>*) {}
+};
+
+// Transforms `nlines` lines of length N = A * B in place; each line is owned by
+// a group of B lanes of one warp, so only __syncwarp is needed inside.
+//   x[b + B a] --(A-point DFT over a)--> Y[b][ka] --(* W_N^(b ka))-->
+//   transpose in the line (swizzled) --(B-point DFT over b)--> X[ka + A kb].
+// `roots` holds exp(-2 pi i j / N), j < N.
+template <typename T, bool INV, int A, int B>
+__device__ __noinline__ void fft_lines_warp(C<T>* buf, int nlines, int stride, const C<T>* roots) {
+  using V = C<T>;
+  constexpr int Q = A / B;
+  constexpr int GPW = 32 / B;  // lines per warp
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int grp = lane / B, b = lane - grp * B;
+  for (int line0 = warp * GPW; line0 < nlines; line0 += nwarps * GPW) {
+    const int line = line0 + grp;
+    const bool active = line < nlines;
+    V* Lp = buf + (long long)(active ? line : 0) * stride;
+    V v[A];
+    if (active) {
+#pragma unroll
+      for (int a = 0; a < A; ++a) v[a] = Lp[b + B * a];
+    }
+    RegDft<T, INV, A>::run(v);
+#pragma unroll
+    for (int ka = 1; ka < A; ++ka) {
+      const V w = roots[b * ka];
+      v[ka] = INV ? cmulc(v[ka], w) : cmul(v[ka], w);
+    }
+    __syncwarp();
+    if (active) {
+#pragma unroll
+      for (int ka = 0; ka < A; ++ka) Lp[ka * B + ((b + ka) & (B - 1))] = v[ka];
+    }
+    __syncwarp();
+    // v is dead after the transpose: reuse it for the columns
+    if (active) {
+#pragma unroll
+      for (int t = 0; t < Q; ++t) {
+        const int ka = b * Q + t;
+#pragma unroll
+        for (int bb = 0; bb < B; ++bb) v[t * B + bb] = Lp[ka * B + ((bb + ka) & (B - 1))];
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < Q; ++t) RegDft<T, INV, B>::run(v + t * B);
+    __syncwarp();
+    if (active) {
+#pragma unroll
+      for (int t = 0; t < Q; ++t)
+#pragma unroll
+        for (int kb = 0; kb < B; ++kb) Lp[(b * Q + t) + A * kb] = v[t * B + kb];
+    }
+    __syncwarp();
+  }
+}
+
+// Transform dispatcher: the warp-level path for the lengths the plan marks,
+// the Stockham stages otherwise.  Returns the buffer holding the result; all
+// threads of the block must call it after the input is complete
+// (__syncthreads()), and the result is complete for all threads on return.
+template <typename T, bool INV>
+__device__ C<T>* fft_run(C<T>* a, C<T>* b, int nlines, int stride, const FftPlan& p, const C<T>* tw) {
+  if (p.warp_a == 16 && p.warp_b == 16) {
+    fft_lines_warp<T, INV, 16, 16>(a, nlines, stride, tw + p.full_off);
+  } else if (p.warp_a == 16 && p.warp_b == 8) {
+    fft_lines_warp<T, INV, 16, 8>(a, nlines, stride, tw + p.full_off);
+  } else if (p.warp_a == 8 && p.warp_b == 8) {
+    fft_lines_warp<T, INV, 8, 8>(a, nlines, stride, tw + p.full_off);
+  } else if (p.warp_a == 16 && p.warp_b == 2) {
+    fft_lines_warp<T, INV, 16, 2>(a, nlines, stride, tw + p.full_off);
+  } else if (p.warp_a == 8 && p.warp_b == 4) {
+    fft_lines_warp<T, INV, 8, 4>(a, nlines, stride, tw + p.full_off);
+  } else {
+    return fft_lines<T, INV>(a, b, nlines, stride, p, tw);
+  }
+  __syncthreads();
+  return a;
 }
 
 }  // namespace mmc

@@ -27,9 +27,11 @@ namespace mmc {
 // Real rows in[c][row][x] (x < xdata, zero up to p.n) -> S[c][z][y][kx], kx < hx.
 template <typename T>
 __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrows, const T* __restrict__ in,
-                            long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, int hx,
-                            int rows_per_cta) {
+                            long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
+                            int rows_per_cta, long long in_rstride, long long s_rstride) {
   using V = C<T>;
+  in += blockIdx.z * in_rstride;  // replica of a batch
+  S += blockIdx.z * s_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw = reinterpret_cast<V*>(smem_raw);
   const int L = p.n;
@@ -53,7 +55,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrow
     }
   }
   __syncthreads();
-  V* res = fft_lines<T, false>(bufA, bufB, nr * npairs, L, p, tw);
+  V* res = fft_run<T, false>(bufA, bufB, nr * npairs, L, p, tw);
   for (int idx = threadIdx.x; idx < nr * npairs * hx; idx += blockDim.x) {
     const int k = idx % hx;
     const int rest = idx / hx;
@@ -63,7 +65,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrow
     const V B = line[k == 0 ? 0 : L - k];
     const int row = row0 + rr;
     const int y = row % ydata, z = row / ydata;
-    const long long off = ((long long)z * nyp + y) * hx + k;
+    const long long off = ((long long)z * nyp + y) * pitch + k;
     const int ca = 2 * pr, cb = 2 * pr + 1;
     S[ca * nspec + off] = cmk<V>((T)0.5 * (A.x + B.x), (T)0.5 * (A.y - B.y));
     if (cb < ncomp) S[cb * nspec + off] = cmk<V>((T)0.5 * (A.y + B.y), (T)-0.5 * (A.x - B.x));
@@ -72,9 +74,12 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrow
 
 // Half spectra S[0..2][z][y][kx] -> real rows out[c][row][x], x < xout.
 template <typename T>
-__global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int xout,
-                            int yout, int nrows, T* __restrict__ out, long long out_cstride, int rows_per_cta) {
+__global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
+                            int xout, int yout, int nrows, T* __restrict__ out, long long out_cstride,
+                            int rows_per_cta, long long s_rstride, long long out_rstride) {
   using V = C<T>;
+  S += blockIdx.z * s_rstride;
+  out += blockIdx.z * out_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw = reinterpret_cast<V*>(smem_raw);
   const int L = p.n;
@@ -87,7 +92,7 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
     const int rr = idx / L, k = idx - rr * L;
     const int row = row0 + rr;
     const int y = row % yout, z = row / yout;
-    const long long base = ((long long)z * nyp + y) * hx;
+    const long long base = ((long long)z * nyp + y) * pitch;
     V v[3];
     const bool lo = k < hx;
     const long long kk = lo ? k : L - k;
@@ -101,7 +106,7 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
     bufA[(long long)(rr * 2 + 1) * L + k] = v[2];
   }
   __syncthreads();
-  V* res = fft_lines<T, true>(bufA, bufB, nr * 2, L, p, tw);
+  V* res = fft_run<T, true>(bufA, bufB, nr * 2, L, p, tw);
   for (int idx = threadIdx.x; idx < nr * xout; idx += blockDim.x) {
     const int rr = idx / xout, x = idx - rr * xout;
     const long long o = (long long)(row0 + rr) * xout + x;
@@ -123,8 +128,9 @@ enum : int { PASS_FWD = 1, PASS_MUL = 2, PASS_INV = 4 };
 template <typename T>
 __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long nspec, const C<T>* __restrict__ khat,
                            int hx, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
-                           int flags, T inv_n, int tx) {
+                           int flags, T inv_n, int tx, long long s_rstride) {
   using V = C<T>;
+  S += blockIdx.z * s_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw = reinterpret_cast<V*>(smem_raw);
   const int L = p.n;
@@ -148,7 +154,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
   V* cur = bufA;
   V* oth = bufB;
   if (flags & PASS_FWD) {
-    V* r = fft_lines<T, false>(cur, oth, nlines, stride, p, tw);
+    V* r = fft_run<T, false>(cur, oth, nlines, stride, p, tw);
     if (r != cur) {
       oth = cur;
       cur = r;
@@ -178,7 +184,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
     __syncthreads();
   }
   if (flags & PASS_INV) {
-    V* r = fft_lines<T, true>(cur, oth, nlines, stride, p, tw);
+    V* r = fft_run<T, true>(cur, oth, nlines, stride, p, tw);
     if (r != cur) {
       oth = cur;
       cur = r;
@@ -268,12 +274,28 @@ struct Nbrs {
   bool has[3][2];
 };
 
-// The Metropolis decision for one cell from its neighbour values, its own m,
-// its demag field h and its counter.  Shared by every sweep kernel so that
-// all paths round identically.  Returns true and the proposal on accept.
+// Proposal of one trial: Philox4x32-10(key = seed; counter = (cell, sweep,
+// stage, 0)) -> direction m' and acceptance uniform ua.
 template <typename T>
-__device__ __forceinline__ bool mc_decide(const McCoef<T>& c, const Nbrs<T>& nb, T ox, T oy, T oz, T hx, T hy, T hz,
-                                          uint32_t cell, uint32_t stage, uint32_t sweep, T& px, T& py, T& pz) {
+struct Proposal {
+  T x, y, z, ua;
+};
+
+template <typename T>
+__device__ __forceinline__ Proposal<T> mc_propose(const McCoef<T>& c, uint32_t cell, uint32_t stage, uint32_t sweep) {
+  mmcm::u32x4 ctr = {cell, sweep, stage, mmcm::STREAM_SWEEP};
+  mmcm::u32x4 r = mmcm::philox4x32_10(ctr, c.key0, c.key1);
+  Proposal<T> p;
+  Prop<T>::draw(r, p.x, p.y, p.z, p.ua);
+  return p;
+}
+
+// The Metropolis decision for one cell from its neighbour values, its own m,
+// its demag field h and its proposal.  Shared by every sweep kernel so that
+// all paths round identically.
+template <typename T>
+__device__ __forceinline__ bool mc_accept(const McCoef<T>& c, const Nbrs<T>& nb, T ox, T oy, T oz, T hx, T hy, T hz,
+                                          const Proposal<T>& p) {
   T Fx = 0, Fy = 0, Fz = 0;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
@@ -302,10 +324,7 @@ __device__ __forceinline__ bool mc_decide(const McCoef<T>& c, const Nbrs<T>& nb,
     Fy = Fy + c.cd * (hy - sy);
     Fz = Fz + c.cd * (hz - sz);
   }
-  mmcm::u32x4 ctr = {cell, sweep, stage, mmcm::STREAM_SWEEP};
-  mmcm::u32x4 r = mmcm::philox4x32_10(ctr, c.key0, c.key1);
-  T ua;
-  Prop<T>::draw(r, px, py, pz, ua);
+  const T px = p.x, py = p.y, pz = p.z;
   const T ddx = px - ox, ddy = py - oy, ddz = pz - oz;
   T dE = -(ddx * Fx + ddy * Fy + ddz * Fz);
   const T pun = px * c.u[0] + py * c.u[1] + pz * c.u[2];
@@ -318,7 +337,17 @@ __device__ __forceinline__ bool mc_decide(const McCoef<T>& c, const Nbrs<T>& nb,
                  oz * (c.k0[2] * ox + c.k0[4] * oy + c.k0[5] * oz);
     dE = dE - (T)0.5 * c.cd * (qn - qo);
   }
-  return Prop<T>::accept(dE, ua);
+  return Prop<T>::accept(dE, p.ua);
+}
+
+template <typename T>
+__device__ __forceinline__ bool mc_decide(const McCoef<T>& c, const Nbrs<T>& nb, T ox, T oy, T oz, T hx, T hy, T hz,
+                                          uint32_t cell, uint32_t stage, uint32_t sweep, T& px, T& py, T& pz) {
+  const Proposal<T> p = mc_propose<T>(c, cell, stage, sweep);
+  px = p.x;
+  py = p.y;
+  pz = p.z;
+  return mc_accept<T>(c, nb, ox, oy, oz, hx, hy, hz, p);
 }
 
 template <typename T>
@@ -368,7 +397,11 @@ __device__ __forceinline__ void count_accepts(bool acc, unsigned long long* coun
 template <typename T>
 __global__ void k_mc_checker(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
                              const SweepCounters* __restrict__ ctr, int color, unsigned long long* acc) {
-  const McCoef<T> c = *cp;
+  // replica blockIdx.z of a batch: its own coefficients, state and counter
+  const McCoef<T> c = cp[blockIdx.z];
+  m += blockIdx.z * 3 * g.n;
+  h += blockIdx.z * 3 * g.n;
+  acc += blockIdx.z;
   const int hxc = (g.nx + 1) >> 1;
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nrows = (long long)g.ny * g.nz;
@@ -387,7 +420,10 @@ __global__ void k_mc_checker(Geom g, const McCoef<T>* __restrict__ cp, T* __rest
 template <typename T>
 __global__ void k_mc_general(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
                              const SweepCounters* __restrict__ ctr, int color, unsigned long long* acc) {
-  const McCoef<T> c = *cp;
+  const McCoef<T> c = cp[blockIdx.z];
+  m += blockIdx.z * 3 * g.n;
+  h += blockIdx.z * 3 * g.n;
+  acc += blockIdx.z;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   bool accepted = false;
   if (i < g.n) {
@@ -408,8 +444,12 @@ __device__ __forceinline__ double warp_sum(double v) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_energy(Geom g, EnCoef e, const T* __restrict__ m, const T* __restrict__ h,
-                                                double* __restrict__ partials) {
+__global__ void __launch_bounds__(256) k_energy(Geom g, const EnCoef* __restrict__ ep, const T* __restrict__ m,
+                                                const T* __restrict__ h, double* __restrict__ partials) {
+  const EnCoef e = ep[blockIdx.z];
+  m += blockIdx.z * 3 * g.n;
+  if (h) h += blockIdx.z * 3 * g.n;
+  partials += (long long)blockIdx.z * gridDim.x * NQ;
   __shared__ double red[NQ][8];
   const long long n = g.n;
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -477,7 +517,9 @@ __global__ void __launch_bounds__(256) k_energy(Geom g, EnCoef e, const T* __res
 }
 
 static __global__ void __launch_bounds__(256) k_reduce_partials(const double* __restrict__ partials, int nblocks,
-                                                         double* __restrict__ out) {
+                                                                double* __restrict__ out) {
+  partials += (long long)blockIdx.x * nblocks * NQ;  // one block per replica
+  out += blockIdx.x * NQ;
   __shared__ double red[NQ][8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int k = 0; k < NQ; ++k) {
@@ -615,23 +657,26 @@ cudaError_t prepare_impl(int max_dyn_smem) {
 
 template <typename T>
 cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int nrows, const T* in,
-                          long long in_cstride, C<T>* S, long long nspec, int nyp, int hx, int rpc, int threads,
-                          cudaStream_t st) {
+                          long long in_cstride, C<T>* S, long long nspec, int nyp, int hx, int pitch, int rpc,
+                          int threads, cudaStream_t st, int nrep = 1, long long in_rstride = 0,
+                          long long s_rstride = 0) {
   const int lines = (ncomp + 1) / 2;
   size_t sm = x_pass_smem(p, lines, rpc, sizeof(C<T>));
-  dim3 grid((nrows + rpc - 1) / rpc);
-  k_x_forward<T><<<grid, threads, sm, st>>>(p, ncomp, xdata, ydata, nrows, in, in_cstride, S, nspec, nyp, hx, rpc);
+  dim3 grid((nrows + rpc - 1) / rpc, 1, nrep);
+  k_x_forward<T><<<grid, threads, sm, st>>>(p, ncomp, xdata, ydata, nrows, in, in_cstride, S, nspec, nyp, hx, pitch,
+                                            rpc, in_rstride, s_rstride);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, const C<T>* khat, int hx,
                          int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
-                         int flags, T inv_n, int tx, int threads, cudaStream_t st) {
+                         int flags, T inv_n, int tx, int threads, cudaStream_t st, int nrep = 1,
+                         long long s_rstride = 0) {
   size_t sm = col_pass_smem(p, ncomp, tx, sizeof(C<T>));
-  dim3 grid((hx + tx - 1) / tx, planes);
+  dim3 grid((hx + tx - 1) / tx, planes, nrep);
   k_col_pass<T><<<grid, threads, sm, st>>>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
-                                           store_lim, flags, inv_n, tx);
+                                           store_lim, flags, inv_n, tx, s_rstride);
   return cudaGetLastError();
 }
 
@@ -643,42 +688,47 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
 
 template <typename T>
 cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
-                       const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st) {
+                       const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st,
+                       int nrep) {
   C<T>* S = reinterpret_cast<C<T>*>(spec);
   const C<T>* K = reinterpret_cast<const C<T>*>(khat);
   const long long ns = g.nspec;
+  const long long mr = 3 * g.n, sr = 3 * ns;  // replica strides
   const T inv_n = (T)(1.0 / (double)g.np);
   const int rows = g.ny * g.nz;
-  MMC_TRY(run_x_forward<T>(px, 3, g.nx, g.ny, rows, m, g.n, S, ns, g.nyp, g.hx, tun.x_rows_per_cta, tun.x_threads,
-                           st));
-  const long long ystride = g.hx, yplane = (long long)g.nyp * g.hx;
+  MMC_TRY(run_x_forward<T>(px, 3, g.nx, g.ny, rows, m, g.n, S, ns, g.nyp, g.hx, g.hxp, tun.x_rows_per_cta,
+                           tun.x_threads, st, nrep, mr, sr));
+  const long long ystride = g.hxp, yplane = (long long)g.nyp * g.hxp;
   if (g.nzp == 1) {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV,
-                            inv_n, tun.col_tx, tun.col_threads, st));
+                            inv_n, tun.col_tx, tun.col_threads, st, nrep, sr));
   } else {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.ny, g.nyp, PASS_FWD, inv_n, tun.col_tx,
-                            tun.col_threads, st));
+                            tun.col_threads, st, nrep, sr));
     MMC_TRY(run_col_pass<T>(pz, 3, S, ns, K, g.hx, g.nyp, ystride, yplane, g.nz, g.nz,
-                            PASS_FWD | PASS_MUL | PASS_INV, inv_n, tun.col_tx_z, tun.col_threads, st));
+                            PASS_FWD | PASS_MUL | PASS_INV, inv_n, tun.col_tx_z, tun.col_threads, st, nrep, sr));
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.nyp, g.ny, PASS_INV, inv_n, tun.col_tx,
-                            tun.col_threads, st));
+                            tun.col_threads, st, nrep, sr));
   }
   const int rpc = tun.x_rows_per_cta;
   size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
-  k_x_inverse<T><<<(rows + rpc - 1) / rpc, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.nx, g.ny, rows, h, g.n,
-                                                                    rpc);
+  dim3 grid((rows + rpc - 1) / rpc, 1, nrep);
+  k_x_inverse<T><<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.nx, g.ny, rows, h, g.n, rpc, sr,
+                                                  mr);
   return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
-                    unsigned long long* acc, cudaStream_t st) {
+                    unsigned long long* acc, cudaStream_t st, int nrep) {
   const int threads = 256;
   if (g.ncolors == 2) {
     const long long total = (long long)g.ny * g.nz * ((g.nx + 1) / 2);
-    k_mc_checker<T><<<(unsigned)((total + threads - 1) / threads), threads, 0, st>>>(g, c, m, h, ctr, color, acc);
+    dim3 grid((unsigned)((total + threads - 1) / threads), 1, nrep);
+    k_mc_checker<T><<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);
   } else {
-    k_mc_general<T><<<(unsigned)((g.n + threads - 1) / threads), threads, 0, st>>>(g, c, m, h, ctr, color, acc);
+    dim3 grid((unsigned)((g.n + threads - 1) / threads), 1, nrep);
+    k_mc_general<T><<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);
   }
   return cudaGetLastError();
 }
@@ -686,13 +736,13 @@ cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const S
 inline int energy_blocks(const Geom& g) { return (int)((g.n + 255) / 256); }
 
 template <typename T>
-cudaError_t energy_impl(const Geom& g, const EnCoef& e, const T* m, const T* h, double* partials, int npartials,
-                        double* out, cudaStream_t st) {
+cudaError_t energy_impl(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials, int npartials,
+                        double* out, cudaStream_t st, int nrep) {
   const int nb = energy_blocks(g);
   if (nb > npartials) return cudaErrorInvalidValue;
-  k_energy<T><<<nb, 256, 0, st>>>(g, e, m, h, partials);
+  k_energy<T><<<dim3(nb, 1, nrep), 256, 0, st>>>(g, e, m, h, partials);
   MMC_TRY(cudaGetLastError());
-  k_reduce_partials<<<1, 256, 0, st>>>(partials, nb, out);
+  k_reduce_partials<<<nrep, 256, 0, st>>>(partials, nb, out);
   return cudaGetLastError();
 }
 
@@ -714,19 +764,19 @@ cudaError_t init_impl(const Geom& g, uint64_t seed, T* m, cudaStream_t st) {
 // Explicitly instantiated for float in kernels_f32.cu and for double in kernels_f64.cu.
 template <typename T>
 cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
-                         const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat,
-                         cudaStream_t st) {
-  return demag_impl<T>(g, px, py, pz, tun, m, h, spec, khat, st);
+                         const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st,
+                         int nrep) {
+  return demag_impl<T>(g, px, py, pz, tun, m, h, spec, khat, st, nrep);
 }
 template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
-                      unsigned long long* acc, cudaStream_t st) {
-  return mc_impl<T>(g, c, m, h, ctr, color, acc, st);
+                      unsigned long long* acc, cudaStream_t st, int nrep) {
+  return mc_impl<T>(g, c, m, h, ctr, color, acc, st, nrep);
 }
 template <typename T>
-cudaError_t launch_energy(const Geom& g, const EnCoef& e, const T* m, const T* h, double* partials, int npartials,
-                          double* out, cudaStream_t st) {
-  return energy_impl<T>(g, e, m, h, partials, npartials, out, st);
+cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials, int npartials,
+                          double* out, cudaStream_t st, int nrep) {
+  return energy_impl<T>(g, e, m, h, partials, npartials, out, st, nrep);
 }
 template <typename T>
 cudaError_t launch_field(const Geom& g, const HCoef& c, int term, const T* m, const T* h, double* out,
@@ -762,11 +812,11 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
 
 #define MMC_INSTANTIATE_LAUNCHERS(T)                                                                          \
   template cudaError_t launch_demag<T>(const Geom&, const FftPlan&, const FftPlan&, const FftPlan&,           \
-                                       const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t);   \
+                                       const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t, int); \
   template cudaError_t launch_mc<T>(const Geom&, const McCoef<T>*, T*, const T*, const SweepCounters*, int,   \
-                                    unsigned long long*, cudaStream_t);                                       \
-  template cudaError_t launch_energy<T>(const Geom&, const EnCoef&, const T*, const T*, double*, int, double*, \
-                                        cudaStream_t);                                                         \
+                                    unsigned long long*, cudaStream_t, int);                                  \
+  template cudaError_t launch_energy<T>(const Geom&, const EnCoef*, const T*, const T*, double*, int, double*, \
+                                        cudaStream_t, int);                                                    \
   template cudaError_t launch_field<T>(const Geom&, const HCoef&, int, const T*, const T*, double*,            \
                                        cudaStream_t);                                                          \
   template cudaError_t launch_init<T>(const Geom&, uint64_t, T*, cudaStream_t);                               \

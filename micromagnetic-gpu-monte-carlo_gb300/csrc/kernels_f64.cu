@@ -4,6 +4,7 @@
 // the CPU oracle built with -ffp-contract=off.
 #include <curand_kernel.h>
 
+#include "coef.h"
 #include "fused2d.cuh"
 #include "kernels.cuh"
 
@@ -21,9 +22,10 @@ int grid_barrier_error(const GridBarrier* b) { return b->err; }
 cudaError_t launch_tensor_fft(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                               const DemagTuning& tun, const double* k6, double2* spec64, cudaStream_t st) {
   const long long ns = g.nspec;
-  MMC_TRY(run_x_forward<double>(px, 6, g.nxp, g.nyp, g.nyp * g.nzp, k6, g.np, spec64, ns, g.nyp, g.hx, 1,
-                                tun.x_threads, st));
-  const long long ystride = g.hx, yplane = (long long)g.nyp * g.hx;
+  MMC_TRY(cudaMemsetAsync(spec64, 0, 6 * (size_t)ns * sizeof(double2), st));
+  MMC_TRY(run_x_forward<double>(px, 6, g.nxp, g.nyp, g.nyp * g.nzp, k6, g.np, spec64, ns, g.nyp, g.hx, g.hxp, 1,
+                                tun.x_threads, st, 1, 0, 0));
+  const long long ystride = g.hxp, yplane = (long long)g.nyp * g.hxp;
   for (int half = 0; half < 2; ++half) {
     double2* S = spec64 + 3 * half * ns;
     if (g.nyp > 1)
@@ -42,6 +44,59 @@ cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st) 
   k_advance<<<1, 1, 0, st>>>(ctr, delta);
   return cudaGetLastError();
 }
+
+// One parallel-tempering pass: in each ladder, the temperature pairs (k, k+1)
+// with k = round mod 2, 2 + round mod 2, ... attempt a swap with probability
+// min(1, exp((1/kT_k - 1/kT_k+1)(E_k - E_k+1))), E from the energy kernel's
+// per-replica sums; u = Philox(key; ladder, round, k, STREAM_SWAP).  A swap
+// exchanges the two replicas' temperatures and recomputes their coefficients.
+template <typename T>
+__global__ void k_pt_swap(PtDevice pt, const McParams* __restrict__ params, McCoef<T>* __restrict__ coef,
+                          const double* __restrict__ red) {
+  const int l = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned int round = *pt.round;
+  if (l < pt.nladders) {
+    const double kB = 1.3806488e-23;
+    unsigned long long att = 0, acc = 0;
+    for (int k = (int)(round & 1u); k + 1 < pt.K; k += 2) {
+      const int ra = pt.replica_at[l * pt.K + k], rb = pt.replica_at[l * pt.K + k + 1];
+      const double* qa = red + (size_t)ra * NQ;
+      const double* qb = red + (size_t)rb * NQ;
+      const double Ea = qa[0] + qa[1] + qa[2] + qa[3] + qa[4];
+      const double Eb = qb[0] + qb[1] + qb[2] + qb[3] + qb[4];
+      const double Ta = pt.temps[l * pt.K + k], Tb = pt.temps[l * pt.K + k + 1];
+      const double delta = (1.0 / (kB * Ta) - 1.0 / (kB * Tb)) * (Ea - Eb);
+      mmcm::u32x4 ctr = {(uint32_t)l, round, (uint32_t)k, mmcm::STREAM_SWAP};
+      const double u = mmcm::u01_f64(mmcm::philox4x32_10(ctr, pt.key0, pt.key1).x);
+      ++att;
+      if (delta >= 0.0 || u < mmcm::exp(delta)) {
+        ++acc;
+        pt.replica_at[l * pt.K + k] = rb;
+        pt.replica_at[l * pt.K + k + 1] = ra;
+        pt.replica_T[ra] = Tb;
+        pt.replica_T[rb] = Ta;
+        coef[ra] = mc_coef_from<T>(params[ra], Tb);
+        coef[rb] = mc_coef_from<T>(params[rb], Ta);
+      }
+    }
+    atomicAdd(&pt.counts[0], att);
+    atomicAdd(&pt.counts[1], acc);
+  }
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x == 0) *pt.round = round + 1u;
+}
+
+template <typename T>
+cudaError_t launch_pt_swap(const PtDevice& pt, const McParams* params, McCoef<T>* coef, const double* red,
+                           cudaStream_t st) {
+  if (pt.nladders > 1024) return cudaErrorInvalidValue;
+  k_pt_swap<T><<<1, 1024, 0, st>>>(pt, params, coef, red);
+  return cudaGetLastError();
+}
+template cudaError_t launch_pt_swap<float>(const PtDevice&, const McParams*, McCoef<float>*, const double*,
+                                           cudaStream_t);
+template cudaError_t launch_pt_swap<double>(const PtDevice&, const McParams*, McCoef<double>*, const double*,
+                                            cudaStream_t);
 
 // Philox cross-check against cuRAND's device implementation (test hook).
 __global__ void k_philox_selftest(long long n, const uint32_t* __restrict__ ctr, uint32_t k0, uint32_t k1,

@@ -21,22 +21,30 @@ struct FftPlan {
   int tw_off[FFT_MAX_STAGES];
   int root_off[FFT_MAX_STAGES];
   int tw_total;
+  // Warp-level transform for power-of-two lengths n = A * B (A values per lane,
+  // B lanes per line): warp_a = A (0 = use the Stockham stages), and the n
+  // roots exp(-2 pi i j / n) at full_off.
+  int warp_a, warp_b;
+  int full_off;
   const double2* tw64;
   const float2* tw32;
 };
 
 // Lattice geometry.  Cell i = x + nx*(y + ny*z).  The padded grid (nxp, nyp,
 // nzp) follows src/main.cu:254-263 of the reference.  The spectrum keeps the
-// kx half-axis: hx = nxp/2 + 1, layout [comp][kz][ky][kx], nspec = hx*nyp*nzp.
+// kx half-axis: hx = nxp/2 + 1 columns stored with an even row pitch hxp (so
+// that pairs of FP32 columns are 16-byte aligned), layout [comp][kz][ky][kx],
+// nspec = hxp*nyp*nzp.  Pad columns hold zeros.
 struct Geom {
   int nx, ny, nz;
   int nxp, nyp, nzp;
   int hx;
+  int hxp;
   int per[3];      // periodic neighbours on this axis (pbc != 0)
   int ncolors;     // 2, or 3 when a periodic axis has odd length
   long long n;     // nx*ny*nz
   long long np;    // nxp*nyp*nzp
-  long long nspec; // hx*nyp*nzp
+  long long nspec; // hxp*nyp*nzp
 };
 
 // Metropolis coefficients, all in units of kT (see the sweep kernel).
@@ -93,16 +101,19 @@ struct SweepCounters {
 
 // ------------------------------------------------------------- launchers
 // Implemented in kernels_f32.cu / kernels_f64.cu (T = float / double) and newell.cu.
+// Batched forms: nrep replicas of one geometry stored back to back (m and h
+// with stride 3n, the spectrum with stride 3 nspec, one McCoef / EnCoef and
+// one accept counter per replica); the tensor spectrum is shared.
 template <typename T>
 cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                          const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat,
-                         cudaStream_t st);
+                         cudaStream_t st, int nrep = 1);
 template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr,
-                      int color, unsigned long long* acc, cudaStream_t st);
+                      int color, unsigned long long* acc, cudaStream_t st, int nrep = 1);
 template <typename T>
-cudaError_t launch_energy(const Geom& g, const EnCoef& e, const T* m, const T* h, double* partials,
-                          int npartials, double* out, cudaStream_t st);
+cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials,
+                          int npartials, double* out, cudaStream_t st, int nrep = 1);
 template <typename T>
 cudaError_t launch_field(const Geom& g, const HCoef& c, int term, const T* m, const T* h, double* out,
                          cudaStream_t st);
@@ -140,10 +151,12 @@ struct FusedArgs {
   const void* khat;
   unsigned long long* acc;
   GridBarrier* bar;
+  unsigned long long* tbuf;  // optional phase timestamps, see fused2d.cuh
   uint32_t stage, sweep0;
   int nsweeps;
   int band;
 };
+constexpr int FUSED_STAMP_WORDS = 16 * 9 * 2;  // sweeps x points x (first CTA, last CTA)
 template <typename T>
 size_t fused2d_smem_bytes(const Geom& g, const FftPlan& px, const FftPlan& py, int band);
 template <typename T>
@@ -152,6 +165,23 @@ template <typename T>
 cudaError_t launch_fused2d(const Geom& g, const FftPlan& px, const FftPlan& py, const FusedArgs<T>& a, int nblocks,
                            cudaStream_t st);
 size_t grid_barrier_bytes();
+
+// Parallel tempering across the replicas of a batch (kernels_f64.cu).
+// replica_at[l * K + k] is the replica holding temperature temps[l * K + k] of
+// ladder l; round advances once per swap pass.
+struct PtDevice {
+  int nladders, K;
+  int* replica_at;
+  const double* temps;
+  double* replica_T;
+  unsigned int* round;
+  unsigned long long* counts;  // [0] attempted, [1] accepted
+  uint32_t key0, key1;
+};
+struct McParams;
+template <typename T>
+cudaError_t launch_pt_swap(const PtDevice& pt, const McParams* params, McCoef<T>* coef, const double* red,
+                           cudaStream_t st);
 int grid_barrier_error(const GridBarrier* host_copy);
 
 }  // namespace mmc

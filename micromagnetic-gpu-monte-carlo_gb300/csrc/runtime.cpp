@@ -16,6 +16,7 @@
 #include <dirent.h>
 #include <vector>
 
+#include "coef.h"
 #include "host_common.h"
 #include "mmc_internal.h"
 
@@ -101,6 +102,22 @@ int make_plan(int n, PlanHost* ph) {
     ns *= R;
   }
   p.nstages = (int)rad.size();
+  // warp-level transform for power-of-two lengths up to 256: n = A * B
+  p.warp_a = p.warp_b = 0;
+  p.full_off = 0;
+  const int wa[4][3] = {{256, 16, 16}, {128, 16, 8}, {64, 8, 8}, {32, 8, 4}};
+  for (const auto& w : wa)
+    if (n == w[0]) {
+      p.warp_a = w[1];
+      p.warp_b = w[2];
+      p.full_off = (int)(tw.size() / 2);
+      for (int j = 0; j < n; ++j) {
+        double c, sn;
+        unit_root(j, n, &c, &sn);
+        tw.push_back(c);
+        tw.push_back(sn);
+      }
+    }
   p.tw_total = (int)(tw.size() / 2);
   size_t cnt = tw.size() / 2;
   if (cnt == 0) cnt = 1, tw.push_back(1.0), tw.push_back(0.0);
@@ -169,6 +186,7 @@ struct mmc_handle {
   void* spec = nullptr;  // 3*nspec complex T
   void* khat = nullptr;  // 6*nspec complex T
   void* coef = nullptr;  // McCoef<T> in device memory
+  EnCoef* ecoef = nullptr;
   double* partials = nullptr;
   int npartials = 0;
   double* red = nullptr;     // NQ doubles, device
@@ -208,30 +226,34 @@ int set_dev(mmc_handle* h) {
   return MMC_OK;
 }
 
+McParams make_mc_params(const mmc_config& c, const double k0[6], long long seed) {
+  McParams p;
+  p.aex = c.Aex;
+  p.dind = c.Dind;
+  p.ku1 = c.Ku1;
+  p.ms = c.ms;
+  p.b[0] = c.Bextx;
+  p.b[1] = c.Bexty;
+  p.b[2] = c.Bextz;
+  double un = std::sqrt(c.anisUx * c.anisUx + c.anisUy * c.anisUy + c.anisUz * c.anisUz);
+  p.u[0] = un > 0 ? c.anisUx / un : 0;
+  p.u[1] = un > 0 ? c.anisUy / un : 0;
+  p.u[2] = un > 0 ? c.anisUz / un : 0;
+  p.d[0] = c.dx;
+  p.d[1] = c.dy;
+  p.d[2] = c.dz;
+  p.v = c.dx * c.dy * c.dz;
+  p.mu0 = 4e-7 * pi_of(&c);
+  for (int q = 0; q < 6; ++q) p.k0[q] = c.cal_demag_flag ? k0[q] : 0.0;
+  p.demag = c.cal_demag_flag != 0;
+  p.key0 = (uint32_t)((uint64_t)seed & 0xffffffffu);
+  p.key1 = (uint32_t)((uint64_t)seed >> 32);
+  return p;
+}
+
 template <typename T>
 McCoef<T> make_mc_coef(const mmc_handle* h, double T_K) {
-  const mmc_config& c = h->cfg;
-  McCoef<T> k;
-  const double kT = kB * T_K;
-  const double V = c.dx * c.dy * c.dz;
-  const double d[3] = {c.dx, c.dy, c.dz};
-  for (int a = 0; a < 3; ++a) k.wex[a] = (T)(2.0 * c.Aex * V / (d[a] * d[a] * kT));
-  k.wdm[0] = (T)(c.Dind * V / (d[0] * kT));
-  k.wdm[1] = (T)(c.Dind * V / (d[1] * kT));
-  k.can = (T)(c.Ku1 * V / kT);
-  double un = std::sqrt(c.anisUx * c.anisUx + c.anisUy * c.anisUy + c.anisUz * c.anisUz);
-  k.u[0] = (T)(un > 0 ? c.anisUx / un : 0);
-  k.u[1] = (T)(un > 0 ? c.anisUy / un : 0);
-  k.u[2] = (T)(un > 0 ? c.anisUz / un : 0);
-  k.cz[0] = (T)(c.ms * V * c.Bextx / kT);
-  k.cz[1] = (T)(c.ms * V * c.Bexty / kT);
-  k.cz[2] = (T)(c.ms * V * c.Bextz / kT);
-  const double mu0 = 4e-7 * pi_of(&c);
-  k.cd = (T)(c.cal_demag_flag ? mu0 * c.ms * c.ms * V / kT : 0.0);
-  for (int q = 0; q < 6; ++q) k.k0[q] = (T)(c.cal_demag_flag ? h->k0[q] : 0.0);
-  k.key0 = (uint32_t)((uint64_t)h->seed & 0xffffffffu);
-  k.key1 = (uint32_t)((uint64_t)h->seed >> 32);
-  return k;
+  return mc_coef_from<T>(make_mc_params(h->cfg, h->k0, h->seed), T_K);
 }
 
 int upload_coef(mmc_handle* h, double T_K) {
@@ -349,7 +371,8 @@ int ensure_demag(mmc_handle* h) {
 // launch; a stop request is honoured between chunks, a barrier timeout inside
 // the kernel is reported as MMC_ERR_TIMEOUT.
 template <typename T>
-cudaError_t fused_chunk(mmc_handle* h, long long stage, long long sweep0, int ns) {
+cudaError_t fused_chunk(mmc_handle* h, long long stage, long long sweep0, int ns,
+                        unsigned long long* tbuf = nullptr) {
   FusedArgs<T> a;
   a.coef = (const McCoef<T>*)h->coef;
   a.m = (T*)h->m;
@@ -358,6 +381,7 @@ cudaError_t fused_chunk(mmc_handle* h, long long stage, long long sweep0, int ns
   a.khat = h->khat;
   a.acc = h->acc;
   a.bar = h->bar;
+  a.tbuf = tbuf;
   a.stage = (uint32_t)stage;
   a.sweep0 = (uint32_t)sweep0;
   a.nsweeps = ns;
@@ -396,13 +420,17 @@ int run_fused(mmc_handle* h, long long stage, long long sweep0, long long nsweep
 int setup_engine(mmc_handle* h, int nsm) {
   const mmc_config& c = h->cfg;
   const Geom& g = h->g;
-  const bool eligible = c.cal_demag_flag && g.nz == 1 && g.nzp == 1 && g.ncolors == 2;
+  // films with demag and two colours whose m rows are whole 16-byte chunks
+  const bool eligible = c.cal_demag_flag && g.nz == 1 && g.nzp == 1 && g.ncolors == 2 &&
+                        ((size_t)g.nx * h->tsize) % 16 == 0 && g.ny >= 1;
   if (c.sweep_engine == MMC_ENGINE_KERNELS || (c.sweep_engine == MMC_ENGINE_AUTO && !eligible)) {
     h->engine = MMC_ENGINE_KERNELS;
     return MMC_OK;
   }
   if (!eligible)
-    return fail(MMC_ERR_UNSUPPORTED, "the fused engine needs a film (nz = 1), demag on and an even or open lattice");
+    return fail(MMC_ERR_UNSUPPORTED,
+                "the fused engine needs a film (nz = 1), demag on, an even or open lattice and nx * sizeof(real) "
+                "a multiple of 16 bytes");
   int optin = 48 * 1024;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
   std::vector<int> bands;
@@ -659,11 +687,12 @@ int energy_impl(mmc_handle* h, mmc_observables* out) {
   TRY(ensure_demag(h));
   if (h->cfg.cal_demag_flag) CU(demag(h));
   EnCoef e = make_en_coef(h);
+  CU(cudaMemcpyAsync(h->ecoef, &e, sizeof e, cudaMemcpyHostToDevice, h->st));
   cudaError_t err =
       h->prec == 32
-          ? launch_energy<float>(h->g, e, (const float*)h->m, h->cfg.cal_demag_flag ? (const float*)h->h : nullptr,
+          ? launch_energy<float>(h->g, h->ecoef, (const float*)h->m, h->cfg.cal_demag_flag ? (const float*)h->h : nullptr,
                                  h->partials, h->npartials, h->red, h->st)
-          : launch_energy<double>(h->g, e, (const double*)h->m, h->cfg.cal_demag_flag ? (const double*)h->h : nullptr,
+          : launch_energy<double>(h->g, h->ecoef, (const double*)h->m, h->cfg.cal_demag_flag ? (const double*)h->h : nullptr,
                                   h->partials, h->npartials, h->red, h->st);
   CU(err);
   CU(cudaMemcpyAsync(h->red_host, h->red, NQ * sizeof(double), cudaMemcpyDeviceToHost, h->st));
@@ -693,8 +722,8 @@ void destroy_impl(mmc_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
-  void* bufs[] = {h->m,   h->h,   h->spec,    h->khat,    h->coef,   h->partials,
-                  h->red, h->acc, h->ctr,     h->stage64, h->field64, (void*)h->bar};
+  void* bufs[] = {h->m,   h->h,   h->spec,    h->khat,    h->coef,    h->partials,   h->red,
+                  h->acc, h->ctr, h->stage64, h->field64, (void*)h->bar, (void*)h->ecoef};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->red_host) cudaFreeHost(h->red_host);
@@ -736,6 +765,7 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   g.nyp = cfg->pbc_y == 0 ? 2 * cfg->ny - 1 : cfg->ny;
   g.nzp = cfg->pbc_z == 0 ? 2 * cfg->nz - 1 : cfg->nz;
   g.hx = g.nxp / 2 + 1;
+  g.hxp = g.hx + (g.hx & 1);
   g.per[0] = cfg->pbc_x != 0;
   g.per[1] = cfg->pbc_y != 0;
   g.per[2] = cfg->pbc_z != 0;
@@ -745,7 +775,7 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
     if (g.per[a] && (dims[a] & 1) && dims[a] > 1) g.ncolors = 3;
   g.n = (long long)g.nx * g.ny * g.nz;
   g.np = (long long)g.nxp * g.nyp * g.nzp;
-  g.nspec = (long long)g.hx * g.nyp * g.nzp;
+  g.nspec = (long long)g.hxp * g.nyp * g.nzp;
   int st;
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(MMC_ERR_CUDA, "stream creation failed"));
@@ -778,6 +808,7 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
     if ((st = alloc(&h->khat, 6 * g.nspec * csize)) != MMC_OK) return bail(st);
   }
   if ((st = alloc(&h->coef, sizeof(McCoef<double>))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&h->ecoef, sizeof(EnCoef))) != MMC_OK) return bail(st);
   if ((st = alloc((void**)&h->partials, (size_t)h->npartials * NQ * sizeof(double))) != MMC_OK) return bail(st);
   if ((st = alloc((void**)&h->red, NQ * sizeof(double))) != MMC_OK) return bail(st);
   if ((st = alloc((void**)&h->acc, sizeof(unsigned long long))) != MMC_OK) return bail(st);
@@ -789,7 +820,9 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   if (cudaMallocHost(&h->red_host, NQ * sizeof(double)) != cudaSuccess)
     return bail(fail(MMC_ERR_OOM, "pinned allocation failed"));
   if (cudaMemset(h->acc, 0, sizeof(unsigned long long)) != cudaSuccess ||
-      cudaMemset(h->h, 0, 3 * g.n * h->tsize) != cudaSuccess)
+      cudaMemset(h->h, 0, 3 * g.n * h->tsize) != cudaSuccess ||
+      (h->spec && cudaMemset(h->spec, 0, 3 * g.nspec * csize) != cudaSuccess) ||
+      (h->khat && cudaMemset(h->khat, 0, 6 * g.nspec * csize) != cudaSuccess))
     return bail(fail(MMC_ERR_CUDA, "memset failed"));
   if ((st = setup_engine(h, nsm)) != MMC_OK) return bail(st);
   // initial magnetisation (src/main.cu:289-333)
@@ -908,6 +941,301 @@ int anneal_loop(mmc_handle* h, const std::string& dir, int verbose) {
     ++stage;
   }
   if (verbose) std::printf("~~~~~~~~~~~~~~END~~~~~~~~~~~~~~~~~~~~~~~~~ \n");
+  return MMC_OK;
+}
+
+}  // namespace
+
+
+// =================================================================== batches
+// nrep replicas of one geometry advanced together: every pass kernel runs over
+// all replicas (grid.z = replica), which fills the GPU where one lattice only
+// fills a corner of it.  Replicas may differ in material, field, seed and
+// temperature; the tensor spectrum is shared.  Optional parallel-tempering
+// ladders swap temperatures on the device every `swap_interval` sweeps.
+struct mmc_batch {
+  mmc_handle* base = nullptr;  // geometry, plans, tensor (replica 0's config)
+  int R = 0;
+  std::vector<mmc_config> cfgs;
+  std::vector<long long> seeds;
+  std::vector<double> T;
+  McParams* params = nullptr;  // device, R
+  void* m = nullptr;
+  void* h = nullptr;
+  void* spec = nullptr;
+  void* coef = nullptr;
+  EnCoef* ecoef = nullptr;
+  double* partials = nullptr;
+  double* red = nullptr;
+  double* red_host = nullptr;
+  unsigned long long* acc = nullptr;
+  SweepCounters* ctr = nullptr;
+  // parallel tempering
+  int interval = 0;
+  PtDevice pt{};
+  int* d_replica_at = nullptr;
+  double* d_temps = nullptr;
+  double* d_replica_T = nullptr;
+  unsigned int* d_round = nullptr;
+  unsigned long long* d_counts = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int graph_len = 0;
+  bool graph_pt = false;
+  std::vector<unsigned long long> acc_base;
+  unsigned long long proposed = 0;
+  double last_ms = 0;
+  std::atomic<int> stop{0};
+};
+
+namespace {
+
+bool same_geometry(const mmc_config& a, const mmc_config& b) {
+  return a.nx == b.nx && a.ny == b.ny && a.nz == b.nz && a.dx == b.dx && a.dy == b.dy && a.dz == b.dz &&
+         a.pbc_x == b.pbc_x && a.pbc_y == b.pbc_y && a.pbc_z == b.pbc_z && a.precision == b.precision &&
+         a.cal_demag_flag == b.cal_demag_flag && a.use_reference_pi == b.use_reference_pi;
+}
+
+void batch_free(mmc_batch* b) {
+  if (!b) return;
+  if (b->base) cudaSetDevice(b->base->device);
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  void* bufs[] = {b->params,   b->m,           b->h,          b->spec,        b->coef,   b->ecoef,
+                  b->partials, b->red,         b->acc,        b->ctr,         b->d_replica_at,
+                  b->d_temps,  b->d_replica_T, b->d_round,    b->d_counts};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (b->red_host) cudaFreeHost(b->red_host);
+  if (b->base) destroy_impl(b->base);
+  delete b;
+}
+
+template <typename T>
+int batch_upload_coefs(mmc_batch* b) {
+  std::vector<McCoef<T>> c(b->R);
+  std::vector<McParams> p(b->R);
+  for (int r = 0; r < b->R; ++r) {
+    p[r] = make_mc_params(b->cfgs[r], b->base->k0, b->seeds[r]);
+    c[r] = mc_coef_from<T>(p[r], b->T[r]);
+  }
+  CU(cudaMemcpy(b->params, p.data(), b->R * sizeof(McParams), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->coef, c.data(), b->R * sizeof(McCoef<T>), cudaMemcpyHostToDevice));
+  return MMC_OK;
+}
+
+cudaError_t batch_demag(mmc_batch* b) {
+  mmc_handle* h = b->base;
+  if (h->prec == 32)
+    return launch_demag<float>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const float*)b->m, (float*)b->h, b->spec,
+                               h->khat, h->st, b->R);
+  return launch_demag<double>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const double*)b->m, (double*)b->h, b->spec,
+                              h->khat, h->st, b->R);
+}
+
+cudaError_t batch_sweep(mmc_batch* b) {
+  mmc_handle* h = b->base;
+  cudaError_t e;
+  if (h->cfg.cal_demag_flag && (e = batch_demag(b)) != cudaSuccess) return e;
+  for (int col = 0; col < h->g.ncolors; ++col) {
+    e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h,
+                                         b->ctr, col, b->acc, h->st, b->R)
+                      : launch_mc<double>(h->g, (const McCoef<double>*)b->coef, (double*)b->m,
+                                          (const double*)b->h, b->ctr, col, b->acc, h->st, b->R);
+    if (e != cudaSuccess) return e;
+  }
+  return launch_advance(b->ctr, 1, h->st);
+}
+
+cudaError_t batch_energy_kernels(mmc_batch* b) {
+  mmc_handle* h = b->base;
+  cudaError_t e;
+  if (h->cfg.cal_demag_flag && (e = batch_demag(b)) != cudaSuccess) return e;
+  const bool dm = h->cfg.cal_demag_flag != 0;
+  return h->prec == 32 ? launch_energy<float>(h->g, b->ecoef, (const float*)b->m, dm ? (const float*)b->h : nullptr,
+                                              b->partials, h->npartials, b->red, h->st, b->R)
+                       : launch_energy<double>(h->g, b->ecoef, (const double*)b->m,
+                                               dm ? (const double*)b->h : nullptr, b->partials, h->npartials,
+                                               b->red, h->st, b->R);
+}
+
+cudaError_t batch_swap(mmc_batch* b) {
+  mmc_handle* h = b->base;
+  return h->prec == 32 ? launch_pt_swap<float>(b->pt, b->params, (McCoef<float>*)b->coef, b->red, h->st)
+                       : launch_pt_swap<double>(b->pt, b->params, (McCoef<double>*)b->coef, b->red, h->st);
+}
+
+// A graph of `len` sweeps, followed (pt) by an energy evaluation and a swap pass.
+int batch_graph(mmc_batch* b, int len, bool pt) {
+  if (b->gexec && b->graph_len == len && b->graph_pt == pt) return MMC_OK;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  mmc_handle* h = b->base;
+  cudaGraph_t graph;
+  CU(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaSuccess;
+  for (int s = 0; s < len && e == cudaSuccess; ++s) e = batch_sweep(b);
+  if (pt && e == cudaSuccess) e = batch_energy_kernels(b);
+  if (pt && e == cudaSuccess) e = batch_swap(b);
+  cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
+  if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+  if (e2 != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("batch capture end: ") + cudaGetErrorString(e2));
+  e = cudaGraphInstantiate(&b->gexec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+  b->graph_len = len;
+  b->graph_pt = pt;
+  return MMC_OK;
+}
+
+int batch_sync_temperatures(mmc_batch* b) {
+  if (b->interval > 0) CU(cudaMemcpy(b->T.data(), b->d_replica_T, b->R * sizeof(double), cudaMemcpyDeviceToHost));
+  return MMC_OK;
+}
+
+int batch_run(mmc_batch* b, long long stage, long long sweep0, long long nsweeps) {
+  mmc_handle* h = b->base;
+  TRY(ensure_demag(h));
+  TRY(batch_sync_temperatures(b));
+  TRY(h->prec == 32 ? batch_upload_coefs<float>(b) : batch_upload_coefs<double>(b));
+  SweepCounters c0{(uint32_t)stage, (uint32_t)sweep0};
+  CU(cudaMemcpy(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice));
+  CU(cudaEventRecord(h->ev[0], h->st));
+  long long done = 0;
+  const int I = b->interval;
+  int launches = 0;
+  auto check_stop = [&]() -> int {
+    if (b->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
+    if (++launches % 64 == 0) CU(cudaStreamSynchronize(h->st));
+    return MMC_OK;
+  };
+  if (I > 0) {
+    // sweeps up to the next multiple of the swap interval, then a swap pass
+    while (done < nsweeps) {
+      const long long s = sweep0 + done;
+      const long long to_boundary = I - (s % I);
+      if (to_boundary <= nsweeps - done && to_boundary == I) {
+        TRY(batch_graph(b, I, true));
+        CU(cudaGraphLaunch(b->gexec, h->st));
+        done += I;
+      } else {
+        const long long k = std::min(to_boundary, nsweeps - done);
+        for (long long q = 0; q < k; ++q) CU(batch_sweep(b));
+        done += k;
+        if (k == to_boundary) {
+          CU(batch_energy_kernels(b));
+          CU(batch_swap(b));
+        }
+      }
+      TRY(check_stop());
+    }
+  } else {
+    const int G = 32;
+    if (nsweeps >= G) TRY(batch_graph(b, G, false));
+    while (nsweeps - done >= G) {
+      CU(cudaGraphLaunch(b->gexec, h->st));
+      done += G;
+      TRY(check_stop());
+    }
+    for (; done < nsweeps; ++done) CU(batch_sweep(b));
+  }
+  CU(cudaEventRecord(h->ev[1], h->st));
+  CU(cudaStreamSynchronize(h->st));
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
+  b->last_ms = ms;
+  b->proposed += (unsigned long long)nsweeps * (unsigned long long)h->g.n;
+  return batch_sync_temperatures(b);
+}
+
+int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out) {
+  *out = nullptr;
+  if (R < 1 || R > 65535) return fail(MMC_ERR_INVALID, "replica count must be in [1, 65535]");
+  for (int r = 0; r < R; ++r) {
+    TRY(config_validate(&cfgs[r]));
+    if (!same_geometry(cfgs[0], cfgs[r]))
+      return fail(MMC_ERR_INVALID, "batch replicas must share lattice, cell size, pbc, precision and demag flag");
+  }
+  mmc_batch* b = new mmc_batch();
+  mmc_config c0 = cfgs[0];
+  c0.sweep_engine = MMC_ENGINE_KERNELS;
+  c0.use_random_init = 1;  // the base lattice's own m is unused
+  int st = create_impl(&c0, device, &b->base);
+  if (st != MMC_OK) {
+    delete b;
+    return st;
+  }
+  mmc_handle* h = b->base;
+  b->R = R;
+  b->cfgs.assign(cfgs, cfgs + R);
+  for (int r = 0; r < R; ++r) {
+    b->seeds.push_back(cfgs[r].randomseed < 0 ? (long long)std::time(nullptr) + r : cfgs[r].randomseed);
+    b->T.push_back(cfgs[r].Temperature_start);
+  }
+  b->acc_base.assign(R, 0);
+  const Geom& g = h->g;
+  const size_t ts = h->tsize, cs = 2 * ts;
+  auto bail = [&](int s) {
+    std::string msg = last_error_cstr();
+    batch_free(b);
+    fail(s, msg);
+    return s;
+  };
+  auto alloc = [&](void** p, size_t bytes) -> int {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) return fail(MMC_ERR_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    return MMC_OK;
+  };
+  if ((st = alloc((void**)&b->params, R * sizeof(McParams))) != MMC_OK) return bail(st);
+  if ((st = alloc(&b->m, (size_t)R * 3 * g.n * ts)) != MMC_OK) return bail(st);
+  if ((st = alloc(&b->h, (size_t)R * 3 * g.n * ts)) != MMC_OK) return bail(st);
+  if (h->cfg.cal_demag_flag && (st = alloc(&b->spec, (size_t)R * 3 * g.nspec * cs)) != MMC_OK) return bail(st);
+  if ((st = alloc(&b->coef, R * sizeof(McCoef<double>))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&b->ecoef, R * sizeof(EnCoef))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&b->partials, (size_t)R * h->npartials * NQ * sizeof(double))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&b->red, (size_t)R * NQ * sizeof(double))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&b->acc, R * sizeof(unsigned long long))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&b->ctr, sizeof(SweepCounters))) != MMC_OK) return bail(st);
+  if (cudaMallocHost(&b->red_host, (size_t)R * NQ * sizeof(double)) != cudaSuccess)
+    return bail(fail(MMC_ERR_OOM, "pinned allocation failed"));
+  if (cudaMemset(b->acc, 0, R * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMemset(b->h, 0, (size_t)R * 3 * g.n * ts) != cudaSuccess ||
+      (b->spec && cudaMemset(b->spec, 0, (size_t)R * 3 * g.nspec * cs) != cudaSuccess))
+    return bail(fail(MMC_ERR_CUDA, "memset failed"));
+  std::vector<EnCoef> ec(R);
+  for (int r = 0; r < R; ++r) {
+    mmc_handle tmp;  // only cfg is read by make_en_coef
+    tmp.cfg = cfgs[r];
+    ec[r] = make_en_coef(&tmp);
+  }
+  if (cudaMemcpy(b->ecoef, ec.data(), R * sizeof(EnCoef), cudaMemcpyHostToDevice) != cudaSuccess)
+    return bail(fail(MMC_ERR_CUDA, "coefficient upload failed"));
+  // initial states: random from each replica's seed, or its OVF file
+  for (int r = 0; r < R; ++r) {
+    const size_t off = (size_t)r * 3 * g.n;
+    if (cfgs[r].use_random_init || !cfgs[r].ovf_filename[0]) {
+      cudaError_t e = h->prec == 32 ? launch_init<float>(g, (uint64_t)b->seeds[r], (float*)b->m + off, h->st)
+                                    : launch_init<double>(g, (uint64_t)b->seeds[r], (double*)b->m + off, h->st);
+      if (e != cudaSuccess) return bail(fail(MMC_ERR_CUDA, "init kernel failed"));
+    } else {
+      std::vector<double> mm(3 * g.n);
+      if ((st = ovf_read(cfgs[r].ovf_filename, g.nx, g.ny, g.nz, cfgs[r].dx, cfgs[r].dy, cfgs[r].dz, mm.data(),
+                         mm.data() + g.n, mm.data() + 2 * g.n)) != MMC_OK)
+        return bail(st);
+      if (cudaMemcpy(h->stage64, mm.data(), 3 * g.n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(fail(MMC_ERR_CUDA, "upload failed"));
+      cudaError_t e = h->prec == 32 ? launch_from_f64<float>(3 * g.n, h->stage64, (float*)b->m + off, h->st)
+                                    : launch_from_f64<double>(3 * g.n, h->stage64, (double*)b->m + off, h->st);
+      if (e != cudaSuccess) return bail(fail(MMC_ERR_CUDA, "conversion failed"));
+    }
+  }
+  if (cudaStreamSynchronize(h->st) != cudaSuccess) return bail(fail(MMC_ERR_CUDA, "init failed"));
+  clear_error();
+  *out = b;
+  return MMC_OK;
+}
+
+int batch_replica_ptr(mmc_batch* b, int r, size_t* off) {
+  if (r < 0 || r >= b->R) return fail(MMC_ERR_INVALID, "replica index out of range");
+  *off = (size_t)r * 3 * b->base->g.n;
   return MMC_OK;
 }
 
@@ -1115,6 +1443,29 @@ int mmc_engine_info(mmc_handle* h, int out[3]) {
   return MMC_OK;
 }
 
+int mmc_profile_fused(mmc_handle* h, double temperature, long long stage, long long sweep0, long long nsweeps,
+                      unsigned long long* stamps) {
+  if (!h || !stamps) return fail(MMC_ERR_INVALID, "null argument");
+  if (h->engine != MMC_ENGINE_FUSED) return fail(MMC_ERR_STATE, "the handle does not use the fused engine");
+  if (nsweeps < 1 || nsweeps > 1024) return fail(MMC_ERR_INVALID, "nsweeps must be in [1, 1024]");
+  TRY(set_dev(h));
+  TRY(ensure_demag(h));
+  TRY(upload_coef(h, temperature));
+  unsigned long long* d = nullptr;
+  CU(cudaMalloc(&d, FUSED_STAMP_WORDS * sizeof(unsigned long long)));
+  cudaError_t e = cudaMemset(d, 0, FUSED_STAMP_WORDS * sizeof(unsigned long long));
+  if (e == cudaSuccess)
+    e = h->prec == 32 ? fused_chunk<float>(h, stage, sweep0, (int)nsweeps, d)
+                      : fused_chunk<double>(h, stage, sweep0, (int)nsweeps, d);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(stamps, d, FUSED_STAMP_WORDS * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  CU(e);
+  h->proposed += (unsigned long long)nsweeps * (unsigned long long)h->g.n;
+  return MMC_OK;
+}
+
 int mmc_last_run_ms(mmc_handle* h, double* ms) {
   if (!h || !ms) return fail(MMC_ERR_INVALID, "null argument");
   *ms = h->last_run_ms;
@@ -1127,6 +1478,180 @@ int mmc_profile_sweeps(mmc_handle* h, double temperature, long long stage, long 
   if (!(temperature > 0)) return fail(MMC_ERR_INVALID, "temperature must be > 0");
   TRY(set_dev(h));
   return profile_sweeps_impl(h, temperature, stage, sweep0, nsweeps, out_ms);
+}
+
+
+int mmc_batch_create(const mmc_config* cfgs, int nrep, int device, mmc_batch** out) {
+  if (!cfgs || !out) return fail(MMC_ERR_INVALID, "null argument");
+  return batch_create_impl(cfgs, nrep, device, out);
+}
+
+void mmc_batch_destroy(mmc_batch* b) { batch_free(b); }
+
+int mmc_batch_size(mmc_batch* b) { return b ? b->R : 0; }
+
+int mmc_batch_set_temperatures(mmc_batch* b, const double* T) {
+  if (!b || !T) return fail(MMC_ERR_INVALID, "null argument");
+  for (int r = 0; r < b->R; ++r)
+    if (!(T[r] > 0)) return fail(MMC_ERR_INVALID, "temperatures must be > 0");
+  b->T.assign(T, T + b->R);
+  if (b->interval > 0) {
+    TRY(set_dev(b->base));
+    CU(cudaMemcpy(b->d_replica_T, b->T.data(), b->R * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  return MMC_OK;
+}
+
+int mmc_batch_get_temperatures(mmc_batch* b, double* T) {
+  if (!b || !T) return fail(MMC_ERR_INVALID, "null argument");
+  TRY(set_dev(b->base));
+  TRY(batch_sync_temperatures(b));
+  std::memcpy(T, b->T.data(), b->R * sizeof(double));
+  return MMC_OK;
+}
+
+int mmc_batch_set_ladders(mmc_batch* b, int nladders, int per_ladder, const int* replicas, const double* temps,
+                          int swap_interval, long long seed) {
+  if (!b || !replicas || !temps) return fail(MMC_ERR_INVALID, "null argument");
+  if (nladders < 1 || per_ladder < 2 || (long long)nladders * per_ladder > b->R || swap_interval < 1)
+    return fail(MMC_ERR_INVALID, "bad ladder shape");
+  std::vector<int> seen(b->R, 0);
+  for (int i = 0; i < nladders * per_ladder; ++i) {
+    if (replicas[i] < 0 || replicas[i] >= b->R || seen[replicas[i]]++)
+      return fail(MMC_ERR_INVALID, "ladder replicas must be distinct indices of the batch");
+    if (!(temps[i] > 0)) return fail(MMC_ERR_INVALID, "ladder temperatures must be > 0");
+  }
+  TRY(set_dev(b->base));
+  const size_t nk = (size_t)nladders * per_ladder;
+  auto re = [&](void** p, size_t bytes) -> int {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    CU(cudaMalloc(p, bytes));
+    return MMC_OK;
+  };
+  TRY(re((void**)&b->d_replica_at, nk * sizeof(int)));
+  TRY(re((void**)&b->d_temps, nk * sizeof(double)));
+  TRY(re((void**)&b->d_replica_T, b->R * sizeof(double)));
+  TRY(re((void**)&b->d_round, sizeof(unsigned int)));
+  TRY(re((void**)&b->d_counts, 2 * sizeof(unsigned long long)));
+  for (size_t i = 0; i < nk; ++i) b->T[replicas[i]] = temps[i];
+  CU(cudaMemcpy(b->d_replica_at, replicas, nk * sizeof(int), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_temps, temps, nk * sizeof(double), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_replica_T, b->T.data(), b->R * sizeof(double), cudaMemcpyHostToDevice));
+  CU(cudaMemset(b->d_round, 0, sizeof(unsigned int)));
+  CU(cudaMemset(b->d_counts, 0, 2 * sizeof(unsigned long long)));
+  b->pt.nladders = nladders;
+  b->pt.K = per_ladder;
+  b->pt.replica_at = b->d_replica_at;
+  b->pt.temps = b->d_temps;
+  b->pt.replica_T = b->d_replica_T;
+  b->pt.round = b->d_round;
+  b->pt.counts = b->d_counts;
+  b->pt.key0 = (uint32_t)((uint64_t)seed & 0xffffffffu);
+  b->pt.key1 = (uint32_t)((uint64_t)seed >> 32);
+  b->interval = swap_interval;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  return MMC_OK;
+}
+
+int mmc_batch_ladder_state(mmc_batch* b, int* replicas, unsigned long long counts[2]) {
+  if (!b || b->interval <= 0) return fail(MMC_ERR_STATE, "no ladders set");
+  TRY(set_dev(b->base));
+  if (replicas)
+    CU(cudaMemcpy(replicas, b->d_replica_at, (size_t)b->pt.nladders * b->pt.K * sizeof(int), cudaMemcpyDeviceToHost));
+  if (counts) CU(cudaMemcpy(counts, b->d_counts, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  return MMC_OK;
+}
+
+int mmc_batch_run_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps) {
+  if (!b) return fail(MMC_ERR_INVALID, "null batch");
+  if (nsweeps < 0 || stage < 0 || sweep0 < 0) return fail(MMC_ERR_INVALID, "negative counter");
+  TRY(set_dev(b->base));
+  b->stop.store(0);
+  if (nsweeps == 0) return MMC_OK;
+  return batch_run(b, stage, sweep0, nsweeps);
+}
+
+int mmc_batch_last_run_ms(mmc_batch* b, double* ms) {
+  if (!b || !ms) return fail(MMC_ERR_INVALID, "null argument");
+  *ms = b->last_ms;
+  return MMC_OK;
+}
+
+void mmc_batch_request_stop(mmc_batch* b) {
+  if (b) b->stop.store(1);
+}
+
+int mmc_batch_energy(mmc_batch* b, mmc_observables* out) {
+  if (!b || !out) return fail(MMC_ERR_INVALID, "null argument");
+  mmc_handle* h = b->base;
+  TRY(set_dev(h));
+  TRY(ensure_demag(h));
+  CU(batch_energy_kernels(b));
+  std::vector<unsigned long long> acc(b->R);
+  CU(cudaMemcpyAsync(b->red_host, b->red, (size_t)b->R * NQ * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaMemcpyAsync(acc.data(), b->acc, b->R * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  const double n = (double)h->g.n;
+  for (int r = 0; r < b->R; ++r) {
+    const double* q = b->red_host + (size_t)r * NQ;
+    mmc_observables& o = out[r];
+    o.e_exchange = q[0];
+    o.e_dmi = q[1];
+    o.e_anisotropy = q[2];
+    o.e_zeeman = q[3];
+    o.e_demag = q[4];
+    o.e_total = q[0] + q[1] + q[2] + q[3] + q[4];
+    o.m[0] = q[5] / n;
+    o.m[1] = q[6] / n;
+    o.m[2] = q[7] / n;
+    o.q = q[8] / (4.0 * 3.14159265358979323846) / (double)h->g.nz;
+    o.accepted = acc[r] - b->acc_base[r];
+    o.proposed = b->proposed;
+    b->acc_base[r] = acc[r];
+  }
+  b->proposed = 0;
+  return MMC_OK;
+}
+
+int mmc_batch_set_m(mmc_batch* b, int r, const double* mx, const double* my, const double* mz) {
+  if (!b || !mx || !my || !mz) return fail(MMC_ERR_INVALID, "null argument");
+  size_t off;
+  TRY(batch_replica_ptr(b, r, &off));
+  mmc_handle* h = b->base;
+  TRY(set_dev(h));
+  const long long n = h->g.n;
+  CU(cudaMemcpy(h->stage64, mx, n * sizeof(double), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(h->stage64 + n, my, n * sizeof(double), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(h->stage64 + 2 * n, mz, n * sizeof(double), cudaMemcpyHostToDevice));
+  CU(h->prec == 32 ? launch_from_f64<float>(3 * n, h->stage64, (float*)b->m + off, h->st)
+                   : launch_from_f64<double>(3 * n, h->stage64, (double*)b->m + off, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  return MMC_OK;
+}
+
+int mmc_batch_get_m(mmc_batch* b, int r, double* mx, double* my, double* mz) {
+  if (!b || !mx || !my || !mz) return fail(MMC_ERR_INVALID, "null argument");
+  size_t off;
+  TRY(batch_replica_ptr(b, r, &off));
+  mmc_handle* h = b->base;
+  TRY(set_dev(h));
+  const long long n = h->g.n;
+  CU(h->prec == 32 ? launch_to_f64<float>(3 * n, (const float*)b->m + off, h->stage64, h->st)
+                   : launch_to_f64<double>(3 * n, (const double*)b->m + off, h->stage64, h->st));
+  CU(cudaStreamSynchronize(h->st));
+  CU(cudaMemcpy(mx, h->stage64, n * sizeof(double), cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(my, h->stage64 + n, n * sizeof(double), cudaMemcpyDeviceToHost));
+  CU(cudaMemcpy(mz, h->stage64 + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return MMC_OK;
+}
+
+int mmc_batch_build_demag(mmc_batch* b, const char* cache_dir) {
+  if (!b) return fail(MMC_ERR_INVALID, "null batch");
+  if (!b->base->cfg.cal_demag_flag) return fail(MMC_ERR_STATE, "cal_demag_flag is off");
+  if (b->base->demag_built) return MMC_OK;
+  return build_demag_impl(b->base, cache_dir);
 }
 
 void mmc_request_stop(mmc_handle* h) {

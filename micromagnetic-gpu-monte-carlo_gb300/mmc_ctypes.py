@@ -145,6 +145,8 @@ def lib(path=None):
         "mmc_request_stop": (None, [H]),
         "mmc_last_run_ms": (ctypes.c_int, [H, _dp]),
         "mmc_engine_info": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int)]),
+        "mmc_profile_fused": (ctypes.c_int, [H, ctypes.c_double, ctypes.c_longlong, ctypes.c_longlong,
+                                             ctypes.c_longlong, ctypes.POINTER(ctypes.c_ulonglong)]),
         "mmc_profile_sweeps": (ctypes.c_int, [H, ctypes.c_double, ctypes.c_longlong, ctypes.c_longlong,
                                               ctypes.c_longlong, _dp]),
         "mmc_ovf_read": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -152,6 +154,22 @@ def lib(path=None):
         "mmc_ovf_write": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                          ctypes.c_double, ctypes.c_double, _dp, _dp, _dp, ctypes.c_int,
                                          ctypes.c_char_p]),
+        "mmc_batch_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_int, ctypes.c_int, ctypes.POINTER(H)]),
+        "mmc_batch_destroy": (None, [H]),
+        "mmc_batch_size": (ctypes.c_int, [H]),
+        "mmc_batch_build_demag": (ctypes.c_int, [H, ctypes.c_char_p]),
+        "mmc_batch_set_temperatures": (ctypes.c_int, [H, _dp]),
+        "mmc_batch_get_temperatures": (ctypes.c_int, [H, _dp]),
+        "mmc_batch_set_ladders": (ctypes.c_int, [H, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp,
+                                                 ctypes.c_int, ctypes.c_longlong]),
+        "mmc_batch_ladder_state": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int),
+                                                  ctypes.POINTER(ctypes.c_ulonglong)]),
+        "mmc_batch_run_sweeps": (ctypes.c_int, [H, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong]),
+        "mmc_batch_last_run_ms": (ctypes.c_int, [H, _dp]),
+        "mmc_batch_request_stop": (None, [H]),
+        "mmc_batch_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
+        "mmc_batch_set_m": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
+        "mmc_batch_get_m": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
         "mmc_selftest_philox": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong, _u32p, ctypes.c_uint32,
                                                ctypes.c_uint32, _u32p, _u32p]),
     }
@@ -305,6 +323,13 @@ class Lattice:
         check(lib().mmc_profile_sweeps(self.h, float(T), stage, sweep0, nsweeps, dptr(out)))
         return out
 
+    def profile_fused(self, T, stage, sweep0, nsweeps):
+        """Phase timestamps (ns) of the fused engine: array [16 sweeps, 9 points, 2 CTAs]."""
+        out = np.zeros(16 * 9 * 2, dtype=np.uint64)
+        check(lib().mmc_profile_fused(self.h, float(T), stage, sweep0, nsweeps,
+                                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))))
+        return out.reshape(16, 9, 2)
+
     def request_stop(self):
         lib().mmc_request_stop(self.h)
 
@@ -323,3 +348,80 @@ def header_functions(header=HEADER):
     text = open(header).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     return sorted(set(re.findall(r"\b(mmc_[a-z0-9_]+)\s*\(", text)))
+
+
+class Batch:
+    """Replicas of one geometry advanced together (an mmc_batch)."""
+
+    def __init__(self, cfgs, device=0):
+        arr = (Config * len(cfgs))(*cfgs)
+        self.h = ctypes.c_void_p()
+        check(lib().mmc_batch_create(arr, len(cfgs), device, ctypes.byref(self.h)))
+        self.R = len(cfgs)
+        self.n = cfgs[0].nx * cfgs[0].ny * cfgs[0].nz
+
+    def close(self):
+        if self.h:
+            lib().mmc_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build_demag(self, cache_dir=""):
+        check(lib().mmc_batch_build_demag(self.h, cache_dir.encode() if cache_dir else None))
+
+    def set_temperatures(self, T):
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        check(lib().mmc_batch_set_temperatures(self.h, dptr(T)))
+
+    def temperatures(self):
+        T = np.zeros(self.R)
+        check(lib().mmc_batch_get_temperatures(self.h, dptr(T)))
+        return T
+
+    def set_ladders(self, replicas, temps, swap_interval, seed):
+        rep = np.ascontiguousarray(replicas, dtype=np.int32)
+        tp = np.ascontiguousarray(temps, dtype=np.float64)
+        nl, K = rep.shape
+        check(lib().mmc_batch_set_ladders(self.h, nl, K, rep.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                          dptr(tp), swap_interval, seed))
+        self._ladder_shape = rep.shape
+
+    def ladder_state(self):
+        rep = np.zeros(self._ladder_shape, np.int32)
+        cnt = np.zeros(2, np.uint64)
+        check(lib().mmc_batch_ladder_state(self.h, rep.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                           cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_ulonglong))))
+        return rep, cnt
+
+    def run_sweeps(self, stage, sweep0, nsweeps):
+        check(lib().mmc_batch_run_sweeps(self.h, stage, sweep0, nsweeps))
+
+    def last_run_ms(self):
+        v = ctypes.c_double()
+        check(lib().mmc_batch_last_run_ms(self.h, ctypes.byref(v)))
+        return v.value
+
+    def energy(self):
+        out = (Observables * self.R)()
+        check(lib().mmc_batch_energy(self.h, out))
+        return list(out)
+
+    def set_m(self, r, m):
+        m = np.ascontiguousarray(m, dtype=np.float64).reshape(3, self.n)
+        check(lib().mmc_batch_set_m(self.h, r, dptr(m[0]), dptr(m[1]), dptr(m[2])))
+
+    def get_m(self, r):
+        m = np.zeros((3, self.n))
+        check(lib().mmc_batch_get_m(self.h, r, dptr(m[0]), dptr(m[1]), dptr(m[2])))
+        return m

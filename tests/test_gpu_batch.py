@@ -1,0 +1,108 @@
+"""Batched replicas and parallel tempering (GPU)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def cfgs_for(M, R, prec, **kw):
+    out = []
+    for r in range(R):
+        base = dict(nx=32, ny=24, nz=1, pbc_x=2, pbc_y=1, pbc_z=0, precision=prec, randomseed=100 + 7 * r,
+                    Bextz=0.1 + 0.05 * r, Dind=3e-3 + 1e-3 * r, Temperature_start=150.0 + 40 * r)
+        base.update(kw)
+        out.append(M.Config.defaults(**base))
+    return out
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("geom", [dict(), dict(nx=12, ny=10, nz=3, pbc_x=0, pbc_y=0, pbc_z=0),
+                                  dict(nx=15, ny=8, pbc_x=1, pbc_y=1)])
+def test_batch_replicas_equal_single_runs(M, prec, geom):
+    cfgs = cfgs_for(M, 3, prec, **geom)
+    with M.Batch(cfgs) as b:
+        b.run_sweeps(2, 0, 45)
+        obs = b.energy()
+        ms = [b.get_m(r) for r in range(3)]
+    for r, c in enumerate(cfgs):
+        with M.Lattice(c) as lat:
+            lat.run_sweeps(c.Temperature_start, 2, 0, 45)
+            o = lat.energy()
+            assert np.array_equal(lat.get_m(), ms[r]), r
+        assert o.accepted == obs[r].accepted
+        assert o.e_total == pytest.approx(obs[r].e_total, rel=1e-12 if prec == 64 else 1e-6)
+
+
+def test_batch_temperatures_and_chunking(M):
+    cfgs = cfgs_for(M, 4, 32)
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        T = np.array([100.0, 200.0, 300.0, 400.0])
+        a.set_temperatures(T)
+        b.set_temperatures(T)
+        a.run_sweeps(0, 0, 70)
+        b.run_sweeps(0, 0, 33)
+        b.run_sweeps(0, 33, 37)
+        for r in range(4):
+            assert np.array_equal(a.get_m(r), b.get_m(r))
+        assert np.array_equal(a.temperatures(), T)
+
+
+def test_parallel_tempering_first_round_matches_host_rule(M, O):
+    """After one swap interval, the ladder state equals the swap rule applied on
+    the host to the energies of the same states."""
+    K = 6
+    temps = 60.0 * (1.5 ** np.arange(K))
+    cfgs = [M.Config.defaults(nx=24, ny=24, nz=1, pbc_x=1, pbc_y=1, pbc_z=0, precision=64, randomseed=11 + r)
+            for r in range(K)]
+    interval = 10
+    with M.Batch(cfgs) as plain:
+        plain.set_temperatures(temps)
+        plain.run_sweeps(0, 0, interval)
+        E = np.array([o.e_total for o in plain.energy()])
+    with M.Batch(cfgs) as pt:
+        pt.set_ladders(np.arange(K)[None, :], temps[None, :], interval, seed=1234)
+        pt.run_sweeps(0, 0, interval)
+        rep, cnt = pt.ladder_state()
+        Tnow = pt.temperatures()
+    kB = 1.3806488e-23
+    at = list(range(K))
+    acc = 0
+    for k in range(0, K - 1, 2):  # round 0: even pairs
+        a, b = at[k], at[k + 1]
+        delta = (1 / (kB * temps[k]) - 1 / (kB * temps[k + 1])) * (E[a] - E[b])
+        r = O.philox([0, 0, k, 2], [1234, 0])[0]
+        u = (r + 0.5) * 2.0 ** -32
+        if delta >= 0 or u < np.exp(delta):
+            at[k], at[k + 1] = b, a
+            acc += 1
+    assert list(rep[0]) == at
+    assert int(cnt[0]) == K // 2 and int(cnt[1]) == acc
+    for k in range(K):
+        assert Tnow[at[k]] == temps[k]
+
+
+def test_parallel_tempering_invariants(M):
+    nl, K = 2, 4
+    cfgs = [M.Config.defaults(nx=16, ny=16, nz=1, pbc_x=1, pbc_y=1, pbc_z=0, precision=32, randomseed=r + 1,
+                              Bextz=0.2 if r < K else 0.4) for r in range(nl * K)]
+    temps = np.array([[50.0, 90.0, 160.0, 290.0]] * nl)
+    reps = np.arange(nl * K).reshape(nl, K)
+    with M.Batch(cfgs) as b:
+        b.set_ladders(reps, temps, 10, seed=7)
+        b.run_sweeps(0, 0, 200)
+        rep, cnt = b.ladder_state()
+        T = b.temperatures()
+    rounds = 20
+    assert int(cnt[0]) == nl * (rounds // 2 * 2 + rounds // 2 * 1)
+    assert 0 < int(cnt[1]) <= int(cnt[0])
+    for l in range(nl):
+        assert sorted(rep[l]) == sorted(reps[l])  # swaps stay inside a ladder
+        for k in range(K):
+            assert T[rep[l, k]] == temps[l, k]
+
+
+def test_batch_rejects_mixed_geometry(M):
+    a = M.Config.defaults(nx=16, ny=16)
+    b = M.Config.defaults(nx=16, ny=8)
+    with pytest.raises(M.MmcError):
+        M.Batch([a, b])

@@ -303,7 +303,7 @@ FILMS = {
     "open20x12": dict(nx=20, ny=12, pbc_x=0, pbc_y=0),
     "mixed24x10": dict(nx=24, ny=10, pbc_x=1, pbc_y=0),
     "ny2_periodic": dict(nx=16, ny=2, pbc_x=1, pbc_y=1),
-    "ny3_open": dict(nx=18, ny=3, pbc_x=1, pbc_y=0),
+    "ny3_open": dict(nx=20, ny=3, pbc_x=1, pbc_y=0),
     "ny1": dict(nx=12, ny=1, pbc_x=1, pbc_y=0),
     "rect_x96": dict(nx=96, ny=6, pbc_x=1, pbc_y=-1),
 }
