@@ -6,10 +6,12 @@ dz = 0.8 nm, Ms = 1.6e6 A/m, Aex = 16 pJ/m, Dind = 6 mJ/m^2, Ku1 = 2 MJ/m^3
 along z, Bext = 0.3 T along z, 20 periodic images in x and y, open in z, demag
 on, random unit-vector start from seed 256, anneal 1400 K -> 40 K by x0.90 per
 stage with 10000 Metropolis sweeps per stage.  One bench step is one
-temperature stage (10000 sweeps of 65536 trials), taken in anneal order.  The
-lattice state is resident in HBM between steps; an L2 flush (a 512 MB write)
-separates the timed steps.  FP32 bulk arithmetic ("f32"); the plain FP64 path
-is timed on the same workload as well.
+temperature stage (10000 sweeps) of a batch of R = 32 replicas of that film
+(seeds 256..287, the seed ensemble the statistical checks use), all replicas
+advanced by every kernel launch.  The lattice states are resident in HBM
+between steps; an L2 flush (a 512 MB write) separates the timed steps.  FP32
+bulk arithmetic ("f32").  One lattice in FP32 and the plain FP64 path are timed
+on the same film as well, and the FP64 CPU oracle on the host cores.
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--impl ours|reference]
 
@@ -210,121 +212,129 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     os.makedirs(CACHE_DIR, exist_ok=True)
-    seed = 256 + rank
-    cfg = M.Config.defaults(precision=32, **dict(WORKLOAD, randomseed=seed))
-    lat = M.Lattice(cfg, device=local)
-    t0 = time.perf_counter()
-    lat.build_demag(CACHE_DIR)
-    setup_s = time.perf_counter() - t0
-    n = lat.n
+    R = args.batch
     S = args.sweeps
+    seeds = [256 + rank * R + r for r in range(R)]
+    cfgs = [M.Config.defaults(precision=32, **dict(WORKLOAD, randomseed=sd)) for sd in seeds]
+    t0 = time.perf_counter()
+    batch = M.Batch(cfgs, device=local)
+    batch.build_demag(CACHE_DIR)
+    setup_s = time.perf_counter() - t0
+    n = 65536
 
-    # warm-up stages
+    def run_stage(k):
+        batch.set_temperatures(np.full(R, stage_temperature(k)))
+        batch.run_sweeps(k, 0, S)
+        return batch.last_run_ms() / 1e3
+
     for k in range(args.warmup):
-        lat.run_sweeps(stage_temperature(k), k, 0, S)
+        run_stage(k)
     barrier(dist)
     torch.cuda.synchronize(dev)
     times = []
     with ClockSampler(local) as clk:
         for j in range(args.steps):
-            k = args.warmup + j
             l2_flush(torch, dev)
-            lat.run_sweeps(stage_temperature(k), k, 0, S)
-            times.append(lat.last_run_ms() / 1e3)
+            times.append(run_stage(args.warmup + j))
     torch.cuda.synchronize(dev)
     barrier(dist)
     total = reduce_max(dist, sum(times))
-    value = world * args.steps * S * n / total
+    value = world * args.steps * S * R * n / total
 
-    # end to end through the public API with host buffers
-    pin_in = torch.empty((3, n), dtype=torch.float64).pin_memory()
-    pin_out = torch.empty((3, n), dtype=torch.float64).pin_memory()
-    pin_in.numpy()[:] = lat.get_m()
+    # end to end through the public API: every step uploads all replicas from
+    # pinned host memory, runs the stage and reads all replicas back
+    pin = torch.empty((R, 3, n), dtype=torch.float64).pin_memory()
+    pin_out = torch.empty((R, 3, n), dtype=torch.float64).pin_memory()
+    host = pin.numpy()
+    for r in range(R):
+        host[r] = batch.get_m(r)
+    L = M.lib()
     e2e_t = 0.0
     for j in range(args.steps):
         k = args.warmup + args.steps + j
         l2_flush(torch, dev)
         t0 = time.perf_counter()
-        lat.set_m(pin_in.numpy())
-        lat.run_sweeps(stage_temperature(k), k, 0, S)
-        mo = pin_out.numpy()
-        M.check(M.lib().mmc_get_m(lat.h, M.dptr(mo[0]), M.dptr(mo[1]), M.dptr(mo[2])))
+        for r in range(R):
+            M.check(L.mmc_batch_set_m(batch.h, r, M.dptr(host[r, 0]), M.dptr(host[r, 1]), M.dptr(host[r, 2])))
+        batch.set_temperatures(np.full(R, stage_temperature(k)))
+        batch.run_sweeps(k, 0, S)
+        out = pin_out.numpy()
+        for r in range(R):
+            M.check(L.mmc_batch_get_m(batch.h, r, M.dptr(out[r, 0]), M.dptr(out[r, 1]), M.dptr(out[r, 2])))
         e2e_t += time.perf_counter() - t0
     e2e_t = reduce_max(dist, e2e_t)
-    e2e = world * args.steps * S * n / e2e_t
+    e2e = world * args.steps * S * R * n / e2e_t
 
-    s = 4
-    nh = (256 // 2 + 1) * 256
+    # per-kernel attribution (CUDA events on the batch's stream), same workload
+    prof_sweeps = 200
+    prof = batch.profile_sweeps(args.warmup, 0, prof_sweeps) / prof_sweeps  # ms per batch sweep
+    s_ = 4
+    hxp, nh = 130, 129 * 256
+    kbytes = {
+        "k_x_forward": R * (3 * s_ * n + 3 * 2 * s_ * nh),
+        "k_col_pass": R * 2 * (3 * 2 * s_ * nh) + 6 * 2 * s_ * nh,
+        "k_x_inverse": R * (3 * 2 * s_ * nh + 3 * s_ * n),
+        "k_mc_checker": R * n * 9 * s_,  # both colours: 36 B per trial
+    }
+    fam = dict(zip(["k_x_forward", "k_col_pass", "k_x_inverse", "k_mc_checker"], prof[:4]))
+    dom = max(fam, key=fam.get)
+    launches = 2 if dom == "k_mc_checker" else 1
+    per_launch_ms = fam[dom] / launches
+    bytes_launch = kbytes[dom] / launches
     peak, peak_kind = measured_peaks()
-    engine, band, blocks = lat.engine()
-    if engine == M.ENGINE_FUSED:
-        # one cooperative launch per chunk of <= 1024 sweeps: per sweep it reads
-        # and writes m (the demag field stays on chip) and reads K^ once
-        launches = args.steps * ((S + 1023) // 1024)
-        per_launch_ms = 1e3 * total / world / launches
-        sweeps_per_launch = args.steps * S / launches
-        bytes_launch = sweeps_per_launch * (6 * s * n + 12 * s * nh)
-        achieved = bytes_launch / (per_launch_ms * 1e-3) / 1e9
-        roofline = {"bound": "hbm", "kernel": "k_fused2d", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-                    "algorithmic_bytes_per_launch": bytes_launch, "avg_ms_per_launch": per_launch_ms,
-                    "bytes_per_sweep": "6*4*N (m in/out) + 12*4*N_h (K^), N=65536, N_h=33024",
-                    "band": band, "ctas": blocks}
-        gpu_launches = launches
-    else:
-        prof_sweeps = 500
-        prof = lat.profile_sweeps(stage_temperature(args.warmup), args.warmup, 0, prof_sweeps)
-        fam = {"demag_conv": prof[0] / prof_sweeps, "metropolis_sweep": prof[1] / prof_sweeps}
-        bytes_fam = {"demag_conv": 6 * s * n + 12 * s * nh, "metropolis_sweep": 9 * s * n}
-        dom = max(fam, key=fam.get)
-        achieved = bytes_fam[dom] / (fam[dom] * 1e-3) / 1e9
-        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
-                    "algorithmic_bytes_per_launch": bytes_fam[dom], "avg_ms_per_launch": fam[dom],
-                    "family_ms_per_sweep": fam}
-        gpu_launches = args.steps * S * (3 + 2 + 1)
+    achieved = bytes_launch / (per_launch_ms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "algorithmic_bytes_per_launch": bytes_launch, "avg_ms_per_launch": per_launch_ms,
+                "kernel_ms_per_batch_sweep": fam, "launch_shape": batch.launch_shape(),
+                "bytes_model": "x passes: 3*4*N real + 3*8*N_h complex per replica; column pass: 2 x 3*8*N_h "
+                               "per replica + 6*8*N_h shared tensor; sweep: 36 B per trial; N=65536, N_h=33024"}
+    batch.close()
 
-    # plain FP64 path on the same workload (fewer sweeps per step)
+    # one lattice, FP32 (the film engine) and the plain FP64 path
+    single = M.Lattice(M.Config.defaults(precision=32, **WORKLOAD), device=local)
+    single.build_demag(CACHE_DIR)
+    single.run_sweeps(stage_temperature(0), 0, 0, 1000)
+    single.run_sweeps(stage_temperature(1), 1, 0, 4000)
+    single_v = 4000 * n / (single.last_run_ms() / 1e3)
+    single_engine = single.engine()
     fp64_line = None
     if not args.no_fp64:
-        cfg64 = cfg.copy(precision=64, sweep_engine=M.ENGINE_KERNELS)
-        lat64 = M.Lattice(cfg64, device=local)
+        lat64 = M.Lattice(M.Config.defaults(precision=64, sweep_engine=M.ENGINE_KERNELS, **WORKLOAD), device=local)
         lat64.build_demag(CACHE_DIR)
-        s64 = max(100, S // 10)
-        lat64.run_sweeps(stage_temperature(0), 0, 0, s64)
-        t64 = 0.0
-        for j in range(2):
-            lat64.run_sweeps(stage_temperature(1 + j), 1 + j, 0, s64)
-            t64 += lat64.last_run_ms() / 1e3
-        fp64 = 2 * s64 * n / t64
+        lat64.run_sweeps(stage_temperature(0), 0, 0, 200)
+        lat64.run_sweeps(stage_temperature(1), 1, 0, 1000)
+        fp64 = 1000 * n / (lat64.last_run_ms() / 1e3)
         lat64.close()
-        fp64_line = {"value": fp64, "unit": UNIT, "sweeps_timed": 2 * s64, "engine": "kernels",
-                     "fp32_over_fp64": value / world / fp64}
+        fp64_line = {"value": fp64, "unit": UNIT, "engine": "kernels", "lattices": 1,
+                     "batched_fp32_over_fp64": value / world / fp64, "single_fp32_over_fp64": single_v / fp64}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "anneal stage 256x256x1, demag, PBC 20 images (x,y), 10000 sweeps/stage",
-                   "sweeps_per_step": S, "cells": n, "precision": "fp32 bulk, fp64 tensor and energy",
-                   "l2": "512 MB flush between timed steps", "replicas": world},
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": 3 * n * 8, "d2h_bytes_per_step": 3 * n * 8},
+        "config": {"workload": f"anneal stage of {R} replicas of the 256x256x1 film, demag, PBC 20 images (x,y), "
+                               f"{S} sweeps/stage", "replicas_per_gpu": R, "seeds": f"{seeds[0]}..{seeds[-1]}",
+                   "sweeps_per_step": S, "cells_per_replica": n,
+                   "precision": "fp32 bulk, fp64 tensor and energy",
+                   "l2": "512 MB flush between timed steps"},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": R * 3 * n * 8, "d2h_bytes_per_step": R * 3 * n * 8},
         "roofline": roofline,
         "clocks": clk.summary(),
-        "gpu_launches": gpu_launches,
+        "gpu_launches": args.steps * S * 6,
+        "single_lattice_fp32": {"value": single_v, "unit": UNIT, "engine": single_engine},
         "fp64_plain": fp64_line,
-        "engine": {"name": {1: "kernels", 2: "fused"}[engine], "band": band, "ctas": blocks},
         "setup_s": setup_s,
     }
     if rank == 0 and not args.no_cpu:
-        k6 = lat.tensor()
+        k6 = single.tensor()
         v1, ns1 = cpu_sample(M, O, k6, seconds=args.cpu_seconds, threads=1)
         cores = os.cpu_count() or 1
         vN, nsN = cpu_sample(M, O, k6, seconds=args.cpu_seconds, threads=cores)
         line["cpu_baseline"] = {"value": vN, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": f"{nsN} FP64 sweeps of the same 256x256x1 lattice (FFT demag)",
+                                "sample": f"{nsN} FP64 sweeps of one 256x256x1 lattice (FFT demag), same tensor",
                                 "single_thread": v1}
-    lat.close()
+    single.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -336,6 +346,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sweeps", type=int, default=SWEEPS_PER_STAGE)
+    ap.add_argument("--batch", type=int, default=32, help="replicas of the 256x256x1 lattice per GPU")
     ap.add_argument("--cpu-seconds", type=float, default=8.0)
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")

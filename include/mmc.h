@@ -255,6 +255,14 @@ int mmc_batch_set_ladders(mmc_batch* b, int nladders, int per_ladder, const int*
 int mmc_batch_ladder_state(mmc_batch* b, int* replicas, unsigned long long counts[2]);
 int mmc_batch_run_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps);
 int mmc_batch_last_run_ms(mmc_batch* b, double* ms);
+/* Runs nsweeps sweeps without graphs and times each kernel family with CUDA
+ * events on the batch's stream (totals in ms): out_ms[0] forward x transform,
+ * [1] column passes (y/z transforms with the tensor product), [2] inverse x
+ * transform, [3] Metropolis colours, [4] sum. */
+int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps, double out_ms[5]);
+/* Launch shape of the batch's pass kernels: rows per CTA and threads of the x
+ * passes, kx columns per tile of the y and z passes, threads of the column passes. */
+int mmc_batch_launch_shape(mmc_batch* b, int out[5]);
 void mmc_batch_request_stop(mmc_batch* b);
 /* Observables of every replica (out holds nrep entries). */
 int mmc_batch_energy(mmc_batch* b, mmc_observables* out);

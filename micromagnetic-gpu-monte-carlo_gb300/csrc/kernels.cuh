@@ -395,7 +395,7 @@ __device__ __forceinline__ void count_accepts(bool acc, unsigned long long* coun
 
 // Two-colour checkerboard: thread t -> row t / hxc, x = 2 (t mod hxc) + parity.
 template <typename T>
-__global__ void k_mc_checker(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
+__global__ void __launch_bounds__(256, 4) k_mc_checker(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
                              const SweepCounters* __restrict__ ctr, int color, unsigned long long* acc) {
   // replica blockIdx.z of a batch: its own coefficients, state and counter
   const McCoef<T> c = cp[blockIdx.z];
@@ -418,7 +418,7 @@ __global__ void k_mc_checker(Geom g, const McCoef<T>* __restrict__ cp, T* __rest
 
 // General colouring (odd periodic axes): every thread tests its cell's colour.
 template <typename T>
-__global__ void k_mc_general(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
+__global__ void __launch_bounds__(256, 4) k_mc_general(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
                              const SweepCounters* __restrict__ ctr, int color, unsigned long long* acc) {
   const McCoef<T> c = cp[blockIdx.z];
   m += blockIdx.z * 3 * g.n;
@@ -689,15 +689,17 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
 template <typename T>
 cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                        const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st,
-                       int nrep) {
+                       int nrep, cudaEvent_t* ev) {
   C<T>* S = reinterpret_cast<C<T>*>(spec);
   const C<T>* K = reinterpret_cast<const C<T>*>(khat);
   const long long ns = g.nspec;
   const long long mr = 3 * g.n, sr = 3 * ns;  // replica strides
   const T inv_n = (T)(1.0 / (double)g.np);
   const int rows = g.ny * g.nz;
+  if (ev) MMC_TRY(cudaEventRecord(ev[0], st));
   MMC_TRY(run_x_forward<T>(px, 3, g.nx, g.ny, rows, m, g.n, S, ns, g.nyp, g.hx, g.hxp, tun.x_rows_per_cta,
                            tun.x_threads, st, nrep, mr, sr));
+  if (ev) MMC_TRY(cudaEventRecord(ev[1], st));
   const long long ystride = g.hxp, yplane = (long long)g.nyp * g.hxp;
   if (g.nzp == 1) {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV,
@@ -710,12 +712,15 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.nyp, g.ny, PASS_INV, inv_n, tun.col_tx,
                             tun.col_threads, st, nrep, sr));
   }
+  if (ev) MMC_TRY(cudaEventRecord(ev[2], st));
   const int rpc = tun.x_rows_per_cta;
   size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
   dim3 grid((rows + rpc - 1) / rpc, 1, nrep);
   k_x_inverse<T><<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.nx, g.ny, rows, h, g.n, rpc, sr,
                                                   mr);
-  return cudaGetLastError();
+  MMC_TRY(cudaGetLastError());
+  if (ev) MMC_TRY(cudaEventRecord(ev[3], st));
+  return cudaSuccess;
 }
 
 template <typename T>
@@ -765,8 +770,8 @@ cudaError_t init_impl(const Geom& g, uint64_t seed, T* m, cudaStream_t st) {
 template <typename T>
 cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                          const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st,
-                         int nrep) {
-  return demag_impl<T>(g, px, py, pz, tun, m, h, spec, khat, st, nrep);
+                         int nrep, cudaEvent_t* ev) {
+  return demag_impl<T>(g, px, py, pz, tun, m, h, spec, khat, st, nrep, ev);
 }
 template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
@@ -812,7 +817,8 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
 
 #define MMC_INSTANTIATE_LAUNCHERS(T)                                                                          \
   template cudaError_t launch_demag<T>(const Geom&, const FftPlan&, const FftPlan&, const FftPlan&,           \
-                                       const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t, int); \
+                                       const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t, int, \
+                                       cudaEvent_t*);                                                          \
   template cudaError_t launch_mc<T>(const Geom&, const McCoef<T>*, T*, const T*, const SweepCounters*, int,   \
                                     unsigned long long*, cudaStream_t, int);                                  \
   template cudaError_t launch_energy<T>(const Geom&, const EnCoef*, const T*, const T*, double*, int, double*, \

@@ -53,9 +53,8 @@ cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st) 
 template <typename T>
 __global__ void k_pt_swap(PtDevice pt, const McParams* __restrict__ params, McCoef<T>* __restrict__ coef,
                           const double* __restrict__ red) {
-  const int l = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned int round = *pt.round;
-  if (l < pt.nladders) {
+  for (int l = threadIdx.x; l < pt.nladders; l += blockDim.x) {
     const double kB = 1.3806488e-23;
     unsigned long long att = 0, acc = 0;
     for (int k = (int)(round & 1u); k + 1 < pt.K; k += 2) {
@@ -83,14 +82,13 @@ __global__ void k_pt_swap(PtDevice pt, const McParams* __restrict__ params, McCo
     atomicAdd(&pt.counts[1], acc);
   }
   __syncthreads();
-  if (blockIdx.x == 0 && threadIdx.x == 0) *pt.round = round + 1u;
+  if (threadIdx.x == 0) *pt.round = round + 1u;
 }
 
 template <typename T>
 cudaError_t launch_pt_swap(const PtDevice& pt, const McParams* params, McCoef<T>* coef, const double* red,
                            cudaStream_t st) {
-  if (pt.nladders > 1024) return cudaErrorInvalidValue;
-  k_pt_swap<T><<<1, 1024, 0, st>>>(pt, params, coef, red);
+  k_pt_swap<T><<<1, 64, 0, st>>>(pt, params, coef, red);
   return cudaGetLastError();
 }
 template cudaError_t launch_pt_swap<float>(const PtDevice&, const McParams*, McCoef<float>*, const double*,

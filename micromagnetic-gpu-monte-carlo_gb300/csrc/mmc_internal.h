@@ -107,7 +107,7 @@ struct SweepCounters {
 template <typename T>
 cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                          const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat,
-                         cudaStream_t st, int nrep = 1);
+                         cudaStream_t st, int nrep = 1, cudaEvent_t* ev = nullptr);
 template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr,
                       int color, unsigned long long* acc, cudaStream_t st, int nrep = 1);

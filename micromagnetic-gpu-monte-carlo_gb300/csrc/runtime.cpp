@@ -141,31 +141,46 @@ void free_plan(PlanHost* ph) {
 
 size_t smem_limit() { return 200 * 1024; }
 
-// Launch shapes: enough CTAs to cover 2x the SM count where the shape allows,
-// within the shared-memory budget.
+// Launch shapes for `nrep` replicas.  The warp-level FFT gives each warp
+// 32 / B lines, so a CTA takes enough rows / columns to keep all its warps
+// busy, and column tiles are widened to whole 32-byte sectors when there are
+// enough CTAs to cover the SMs twice.
 DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz, size_t csize,
-                          int nsm) {
+                          int nsm, int nrep) {
   DemagTuning t;
-  const int rows = g.ny * g.nz;
-  auto xsm = [&](int r) {
-    return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize;
-  };
-  int r = 1;
-  while (r < 8 && (rows + 2 * r - 1) / (2 * r) >= 2 * nsm && xsm(2 * r) <= 96 * 1024) r *= 2;
-  t.x_rows_per_cta = r;
+  const long long rows = (long long)g.ny * g.nz;
+  const long long want = 2LL * nsm;
+  auto xsm = [&](int r) { return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize; };
   t.x_threads = px.n >= 512 ? 256 : 128;
+  int r = 1;
+  if (px.warp_a) {
+    const int lines = (t.x_threads / 32) * (32 / px.warp_b);  // lines the warps take in one round
+    r = std::max(1, lines / 2);
+  } else {
+    r = 4;
+  }
+  while (r > 1 && ((rows + r - 1) / r) * nrep < want) r /= 2;
+  while (r > 1 && xsm(r) > 96 * 1024) r /= 2;
+  t.x_rows_per_cta = r;
   auto csm = [&](const FftPlan& p, int tx) {
     return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * (p.n + 1)) * csize;
   };
   auto pick = [&](const FftPlan& p, int planes) {
-    int tx = 16;
-    while (tx > 1 && (((long long)(g.hx + tx - 1) / tx) * planes < 2 * nsm || csm(p, tx) > 96 * 1024)) tx /= 2;
+    int tx = 8;
+    while (tx > 1 && (((long long)(g.hx + tx - 1) / tx) * planes * nrep < want || csm(p, tx) > 96 * 1024)) tx /= 2;
     while (tx > 1 && csm(p, tx) > smem_limit()) tx /= 2;
     return tx;
   };
   t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz);
   t.col_tx_z = pick(pz, g.nyp);
-  t.col_threads = 256;
+  // threads: enough warps for the lines of one tile (3 components x tx columns)
+  auto threads_for = [&](const FftPlan& p, int tx) {
+    if (!p.warp_a) return 256;
+    const int lines_per_warp = 32 / p.warp_b;
+    const int warps = (3 * tx + lines_per_warp - 1) / lines_per_warp;
+    return std::max(64, std::min(512, 32 * warps));
+  };
+  t.col_threads = std::max(threads_for(py, t.col_tx), threads_for(pz, t.col_tx_z));
   return t;
 }
 
@@ -212,6 +227,7 @@ struct mmc_handle {
   int fused_band = 0;
   int fused_blocks = 0;
   GridBarrier* bar = nullptr;
+  int nsm = 0;
 };
 
 namespace {
@@ -351,6 +367,7 @@ int ensure_graph(mmc_handle* h, int nsw) {
   cudaError_t e = cudaSuccess;
   for (int s = 0; s < nsw && e == cudaSuccess; ++s) e = enqueue_sweep(h);
   cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) cudaGetLastError();  // do not leak the capture error to later calls
   if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("sweep capture: ") + cudaGetErrorString(e));
   if (e2 != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("sweep capture end: ") + cudaGetErrorString(e2));
   e = cudaGraphInstantiate(&h->gexec, graph, 0);
@@ -788,7 +805,8 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   if (launch_prepare<float>(optin) != cudaSuccess || launch_prepare<double>(optin) != cudaSuccess)
     return bail(fail(MMC_ERR_CUDA, "kernel attribute setup failed"));
   const size_t csize = 2 * h->tsize;
-  h->tun = choose_tuning(g, h->px.p, h->py.p, h->pz.p, csize, nsm);
+  h->tun = choose_tuning(g, h->px.p, h->py.p, h->pz.p, csize, nsm, 1);
+  h->nsm = nsm;
   // shared-memory feasibility of the per-sweep passes
   if (((size_t)((h->px.p.tw_total + 1) & ~1) + 2 * 2 * (size_t)h->px.p.n) * csize > smem_limit() ||
       ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)(h->py.p.n + 1)) * csize > smem_limit() ||
@@ -956,6 +974,7 @@ int anneal_loop(mmc_handle* h, const std::string& dir, int verbose) {
 struct mmc_batch {
   mmc_handle* base = nullptr;  // geometry, plans, tensor (replica 0's config)
   int R = 0;
+  DemagTuning tun{};
   std::vector<mmc_config> cfgs;
   std::vector<long long> seeds;
   std::vector<double> T;
@@ -1022,19 +1041,19 @@ int batch_upload_coefs(mmc_batch* b) {
   return MMC_OK;
 }
 
-cudaError_t batch_demag(mmc_batch* b) {
+cudaError_t batch_demag(mmc_batch* b, cudaEvent_t* ev = nullptr) {
   mmc_handle* h = b->base;
   if (h->prec == 32)
-    return launch_demag<float>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const float*)b->m, (float*)b->h, b->spec,
-                               h->khat, h->st, b->R);
-  return launch_demag<double>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const double*)b->m, (double*)b->h, b->spec,
-                              h->khat, h->st, b->R);
+    return launch_demag<float>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, (const float*)b->m, (float*)b->h, b->spec,
+                               h->khat, h->st, b->R, ev);
+  return launch_demag<double>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, (const double*)b->m, (double*)b->h, b->spec,
+                              h->khat, h->st, b->R, ev);
 }
 
-cudaError_t batch_sweep(mmc_batch* b) {
+cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
   mmc_handle* h = b->base;
   cudaError_t e;
-  if (h->cfg.cal_demag_flag && (e = batch_demag(b)) != cudaSuccess) return e;
+  if (h->cfg.cal_demag_flag && (e = batch_demag(b, ev)) != cudaSuccess) return e;
   for (int col = 0; col < h->g.ncolors; ++col) {
     e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h,
                                          b->ctr, col, b->acc, h->st, b->R)
@@ -1042,6 +1061,7 @@ cudaError_t batch_sweep(mmc_batch* b) {
                                           (const double*)b->h, b->ctr, col, b->acc, h->st, b->R);
     if (e != cudaSuccess) return e;
   }
+  if (ev && (e = cudaEventRecord(ev[4], h->st)) != cudaSuccess) return e;
   return launch_advance(b->ctr, 1, h->st);
 }
 
@@ -1076,6 +1096,7 @@ int batch_graph(mmc_batch* b, int len, bool pt) {
   if (pt && e == cudaSuccess) e = batch_energy_kernels(b);
   if (pt && e == cudaSuccess) e = batch_swap(b);
   cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) cudaGetLastError();
   if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
   if (e2 != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("batch capture end: ") + cudaGetErrorString(e2));
   e = cudaGraphInstantiate(&b->gexec, graph, 0);
@@ -1165,6 +1186,7 @@ int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out
   }
   mmc_handle* h = b->base;
   b->R = R;
+  b->tun = choose_tuning(h->g, h->px.p, h->py.p, h->pz.p, 2 * h->tsize, h->nsm, R);
   b->cfgs.assign(cfgs, cfgs + R);
   for (int r = 0; r < R; ++r) {
     b->seeds.push_back(cfgs[r].randomseed < 0 ? (long long)std::time(nullptr) + r : cfgs[r].randomseed);
@@ -1571,6 +1593,49 @@ int mmc_batch_run_sweeps(mmc_batch* b, long long stage, long long sweep0, long l
   b->stop.store(0);
   if (nsweeps == 0) return MMC_OK;
   return batch_run(b, stage, sweep0, nsweeps);
+}
+
+int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps, double out_ms[5]) {
+  if (!b || !out_ms) return fail(MMC_ERR_INVALID, "null argument");
+  if (!b->base->cfg.cal_demag_flag) return fail(MMC_ERR_STATE, "cal_demag_flag is off");
+  mmc_handle* h = b->base;
+  TRY(set_dev(h));
+  TRY(ensure_demag(h));
+  TRY(batch_sync_temperatures(b));
+  TRY(h->prec == 32 ? batch_upload_coefs<float>(b) : batch_upload_coefs<double>(b));
+  SweepCounters c0{(uint32_t)stage, (uint32_t)sweep0};
+  CU(cudaMemcpy(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice));
+  cudaEvent_t ev[5];
+  for (auto& e : ev) CU(cudaEventCreate(&e));
+  double acc[4] = {0, 0, 0, 0};
+  int status = MMC_OK;
+  for (long long s = 0; s < nsweeps && status == MMC_OK; ++s) {
+    cudaError_t e = batch_sweep(b, ev);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
+      float ms = 0;
+      e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
+      acc[k] += ms;
+    }
+    if (e != cudaSuccess) status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (status != MMC_OK) return status;
+  CU(cudaStreamSynchronize(h->st));
+  for (int k = 0; k < 4; ++k) out_ms[k] = acc[k];
+  out_ms[4] = acc[0] + acc[1] + acc[2] + acc[3];
+  b->proposed += (unsigned long long)nsweeps * (unsigned long long)h->g.n;
+  return MMC_OK;
+}
+
+int mmc_batch_launch_shape(mmc_batch* b, int out[5]) {
+  if (!b || !out) return fail(MMC_ERR_INVALID, "null argument");
+  out[0] = b->tun.x_rows_per_cta;
+  out[1] = b->tun.x_threads;
+  out[2] = b->tun.col_tx;
+  out[3] = b->tun.col_tx_z;
+  out[4] = b->tun.col_threads;
+  return MMC_OK;
 }
 
 int mmc_batch_last_run_ms(mmc_batch* b, double* ms) {

@@ -166,6 +166,9 @@ def lib(path=None):
                                                   ctypes.POINTER(ctypes.c_ulonglong)]),
         "mmc_batch_run_sweeps": (ctypes.c_int, [H, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong]),
         "mmc_batch_last_run_ms": (ctypes.c_int, [H, _dp]),
+        "mmc_batch_profile_sweeps": (ctypes.c_int, [H, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong,
+                                                    _dp]),
+        "mmc_batch_launch_shape": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int)]),
         "mmc_batch_request_stop": (None, [H]),
         "mmc_batch_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
         "mmc_batch_set_m": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
@@ -411,6 +414,16 @@ class Batch:
         v = ctypes.c_double()
         check(lib().mmc_batch_last_run_ms(self.h, ctypes.byref(v)))
         return v.value
+
+    def profile_sweeps(self, stage, sweep0, nsweeps):
+        out = np.zeros(5)
+        check(lib().mmc_batch_profile_sweeps(self.h, stage, sweep0, nsweeps, dptr(out)))
+        return out
+
+    def launch_shape(self):
+        out = (ctypes.c_int * 5)()
+        check(lib().mmc_batch_launch_shape(self.h, out))
+        return tuple(out)
 
     def energy(self):
         out = (Observables * self.R)()
