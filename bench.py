@@ -220,6 +220,11 @@ def run_ours(args):
     batch = M.Batch(cfgs, device=local)
     batch.build_demag(CACHE_DIR)
     setup_s = time.perf_counter() - t0
+    # launch shape: the fastest of all shapes on this device (bit-identical results)
+    batch.set_temperatures(np.full(R, stage_temperature(0)))
+    t0 = time.perf_counter()
+    tune_ms, tune_n = batch.autotune(8)
+    tune_s = time.perf_counter() - t0
     n = 65536
 
     def run_stage(k):
@@ -270,13 +275,22 @@ def run_ours(args):
     prof = batch.profile_sweeps(args.warmup, 0, prof_sweeps) / prof_sweeps  # ms per batch sweep
     s_ = 4
     hxp, nh = 130, 129 * 256
-    kbytes = {
-        "k_x_forward": R * (3 * s_ * n + 3 * 2 * s_ * nh),
-        "k_col_pass": R * 2 * (3 * 2 * s_ * nh) + 6 * 2 * s_ * nh,
-        "k_x_inverse": R * (3 * 2 * s_ * nh + 3 * s_ * n),
-        "k_mc_checker": R * n * 9 * s_,  # both colours: 36 B per trial
-    }
-    fam = dict(zip(["k_x_forward", "k_col_pass", "k_x_inverse", "k_mc_checker"], prof[:4]))
+    shape = batch.launch_shape()
+    if shape[5] > 0:  # film row kernel + column pass
+        kbytes = {
+            # m in and out, spectrum rows in and out (halo re-reads not counted)
+            "k_rows": R * (2 * 3 * s_ * n + 2 * 3 * 2 * s_ * nh),
+            "k_col_pass": R * 2 * (3 * 2 * s_ * nh) + 6 * 2 * s_ * nh,
+        }
+        fam = dict(zip(["k_rows", "k_col_pass"], prof[:2]))
+    else:
+        kbytes = {
+            "k_x_forward": R * (3 * s_ * n + 3 * 2 * s_ * nh),
+            "k_col_pass": R * 2 * (3 * 2 * s_ * nh) + 6 * 2 * s_ * nh,
+            "k_x_inverse": R * (3 * 2 * s_ * nh + 3 * s_ * n),
+            "k_mc_checker": R * n * 9 * s_,  # both colours: 36 B per trial
+        }
+        fam = dict(zip(["k_x_forward", "k_col_pass", "k_x_inverse", "k_mc_checker"], prof[:4]))
     dom = max(fam, key=fam.get)
     launches = 2 if dom == "k_mc_checker" else 1
     per_launch_ms = fam[dom] / launches
@@ -286,9 +300,9 @@ def run_ours(args):
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
                 "algorithmic_bytes_per_launch": bytes_launch, "avg_ms_per_launch": per_launch_ms,
-                "kernel_ms_per_batch_sweep": fam, "launch_shape": batch.launch_shape(),
-                "bytes_model": "x passes: 3*4*N real + 3*8*N_h complex per replica; column pass: 2 x 3*8*N_h "
-                               "per replica + 6*8*N_h shared tensor; sweep: 36 B per trial; N=65536, N_h=33024"}
+                "kernel_ms_per_batch_sweep": fam, "launch_shape": shape,
+                "bytes_model": "row kernel: m in/out 2*3*4*N + spectrum rows in/out 2*3*8*N_h per replica; "
+                               "column pass: 2*3*8*N_h per replica + 6*8*N_h shared tensor; N=65536, N_h=33024"}
     batch.close()
 
     # one lattice, FP32 (the film engine) and the plain FP64 path
@@ -321,10 +335,12 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": R * 3 * n * 8, "d2h_bytes_per_step": R * 3 * n * 8},
         "roofline": roofline,
         "clocks": clk.summary(),
-        "gpu_launches": args.steps * S * 6,
+        "gpu_launches": args.steps * (S * 3 if shape[5] > 0 else S * 6),
         "single_lattice_fp32": {"value": single_v, "unit": UNIT, "engine": single_engine},
         "fp64_plain": fp64_line,
         "setup_s": setup_s,
+        "autotune": {"candidates": tune_n, "best_ms_per_batch_sweep": tune_ms, "seconds": tune_s,
+                     "launch_shape": list(shape)},
     }
     if rank == 0 and not args.no_cpu:
         k6 = single.tensor()

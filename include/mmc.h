@@ -256,13 +256,26 @@ int mmc_batch_ladder_state(mmc_batch* b, int* replicas, unsigned long long count
 int mmc_batch_run_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps);
 int mmc_batch_last_run_ms(mmc_batch* b, double* ms);
 /* Runs nsweeps sweeps without graphs and times each kernel family with CUDA
- * events on the batch's stream (totals in ms): out_ms[0] forward x transform,
- * [1] column passes (y/z transforms with the tensor product), [2] inverse x
- * transform, [3] Metropolis colours, [4] sum. */
+ * events on the batch's stream (totals in ms).  One kernel per pass:
+ * out_ms[0] forward x transform, [1] column passes (y/z transforms with the
+ * tensor product), [2] inverse x transform, [3] Metropolis colours.  Film row
+ * kernel (launch shape out[5] > 0): [0] row kernel, [1] column pass, [2] = [3]
+ * = 0.  [4] = sum. */
 int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps, double out_ms[5]);
 /* Launch shape of the batch's pass kernels: rows per CTA and threads of the x
- * passes, kx columns per tile of the y and z passes, threads of the column passes. */
-int mmc_batch_launch_shape(mmc_batch* b, int out[5]);
+ * passes, kx columns per tile of the y and z passes, threads of the column
+ * passes, and the band of the film row kernel (0 when sweeps use one kernel
+ * per pass). */
+int mmc_batch_launch_shape(mmc_batch* b, int out[6]);
+/* Autotuner: times each launch shape this batch can run with (the film row
+ * kernel with each band that fits; the pass kernels with 1-16 rows per x-pass
+ * CTA and 1-8 kx columns per column-pass tile) for `sweeps` sweeps from the
+ * current state, keeps the fastest and restores m and the acceptance
+ * counters.  Every shape gives bit-identical results, so the choice changes
+ * only the speed.  best_ms_per_sweep and candidates may be NULL.  No
+ * counterpart in the reference, whose block shape is fixed in the source
+ * (src/main.cu:275-286). */
+int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int* candidates);
 void mmc_batch_request_stop(mmc_batch* b);
 /* Observables of every replica (out holds nrep entries). */
 int mmc_batch_energy(mmc_batch* b, mmc_observables* out);

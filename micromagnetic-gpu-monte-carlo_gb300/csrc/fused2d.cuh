@@ -4,15 +4,10 @@
 // consecutive rows and a fixed set of kx column pairs.  Per sweep there are two
 // phases separated by grid barriers:
 //
-//   row phase    : 16-byte cp.async copies of the m rows y0-2 .. y1+1 and of
-//                  the spectrum rows y0-1 .. y1 (band + one halo row per side),
-//                  overlapped with the Philox proposals of the sweep;
-//                  inverse x-FFT of those spectrum rows -> demag field h;
-//                  colour-0 Metropolis updates of band + halo rows (the halo
-//                  rows repeat, bit for bit, what their owners compute, so no
-//                  barrier is needed before colour 1);
-//                  colour-1 updates of the band rows;
-//                  store m, forward x-FFT of the band rows -> spectrum rows.
+//   row phase    : the shared row phase of rows.cuh -- inverse x-FFT of the
+//                  band's spectrum rows (plus one halo row per side), colour 0
+//                  on band + halo rows, colour 1 on the band rows, store m,
+//                  forward x-FFT of the band rows;
 //   column phase : for each owned kx pair: y-FFT, the 3x3 tensor product
 //                  (K^ . M^ / N, calHexchangeKernel of the reference,
 //                  src/demag_cu.cu:68-116) with K^ kept resident in shared
@@ -26,6 +21,7 @@
 // bounded: on timeout the kernel records an error and returns.
 #pragma once
 #include "kernels.cuh"
+#include "rows.cuh"
 
 namespace mmc {
 
@@ -37,12 +33,6 @@ struct GridBarrier {
   int err;  // 0 ok, 1 a barrier wait ran out of its budget
   int pad2;
 };
-
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ unsigned long long global_ns() {
   unsigned long long t;
@@ -82,9 +72,11 @@ struct Fused2D {
   Geom g;
   FftPlan px, py;
   const McCoef<T>* coef;
-  T* m;
+  T* m;   // m; holds the result after an even number of sweeps
+  T* m2;  // second copy of m; holds the result after an odd number
   T* h;
   C<T>* S;
+  C<T>* S2;
   const C<T>* K;
   unsigned long long* acc;
   GridBarrier* bar;
@@ -100,9 +92,11 @@ constexpr int FUSED_MAX_RES = 2;   // kx pairs whose K^ stays resident in shared
 constexpr int FUSED_TPOINTS = 9;   // timestamps per sweep
 constexpr int FUSED_TSWEEPS = 16;  // sweeps recorded
 
-// Shared-memory carve-up (bytes, 16-aligned).
+// Shared-memory carve-up (bytes, 16-aligned): the row phase's buffers (its
+// transform buffers sized for the column phase too), then the y twiddles, the
+// resident tensor spectrum and the column staging area.
 struct Fused2DLayout {
-  size_t twx, twy, kres, colraw, mrows, specraw, hrows, prop, fft, total;
+  size_t rowph, twy, kres, colraw, total;
   int npairs, items, resident;
 };
 
@@ -116,61 +110,42 @@ __host__ __device__ inline Fused2DLayout fused2d_layout(const Geom& g, const Fft
   L.npairs = g.hxp / 2;
   L.items = (L.npairs + nblocks - 1) / nblocks;
   L.resident = L.items <= FUSED_MAX_RES ? L.items : 0;
-  L.twx = align16((size_t)px.tw_total * cs);
+  L.rowph = row_phase_bytes<T>(g, px, band, true, (size_t)6 * (py.n + 1));
   L.twy = align16((size_t)py.tw_total * cs);
   L.kres = align16((size_t)(L.resident ? L.resident : 1) * 6 * py.n * 2 * cs);
   L.colraw = align16((size_t)3 * g.ny * 2 * cs);
-  L.mrows = align16((size_t)(band + 4) * 3 * g.nx * sizeof(T));
-  L.specraw = align16((size_t)(band + 2) * 3 * g.hxp * cs);
-  L.hrows = align16((size_t)(band + 2) * 3 * g.nx * sizeof(T));
-  L.prop = align16((size_t)(2 * band + 2) * ((g.nx + 1) / 2) * 4 * sizeof(T));
-  const size_t xl = (size_t)2 * (band + 2) * px.n;
-  const size_t yl = (size_t)6 * (py.n + 1);
-  L.fft = align16((xl > yl ? xl : yl) * cs);
-  L.total = L.twx + L.twy + L.kres + L.colraw + L.mrows + L.specraw + L.hrows + L.prop + 2 * L.fft;
+  L.total = L.rowph + L.twy + L.kres + L.colraw;
   return L;
 }
 
-__device__ __forceinline__ int fused_row(int r, int ny, int per) {
-  if (r < 0 || r >= ny) {
-    if (!per) return -1;
-    r = ((r % ny) + ny) % ny;
-  }
-  return r;
-}
-
 template <typename T>
-__global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(Fused2D<T> P) {
+__global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(const __grid_constant__ Fused2D<T> P) {
   using V = C<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_flag;
   __shared__ int s_rows[64];  // slot -> row (or -1); slot k holds row y0 - 2 + k
   __shared__ unsigned int s_acc;
   const Geom& g = P.g;
-  const int nx = g.nx, ny = g.ny, L = P.px.n, hx = g.hx, hxp = g.hxp, Ly = P.py.n;
-  const long long n = g.n, nspec = g.nspec;
+  const int ny = g.ny, hxp = g.hxp, Ly = P.py.n;
+  const long long nspec = g.nspec;
   const int G = gridDim.x;
   const Fused2DLayout lay = fused2d_layout<T>(g, P.px, P.py, P.band, G);
+  RowPhase<T> R;
+  R.g = g;
+  R.px = &P.px;
   unsigned char* ptr = smem_raw;
-  V* twx = reinterpret_cast<V*>(ptr);
-  ptr += lay.twx;
+  row_phase_carve<T>(R, ptr, P.band, true, (size_t)6 * (Ly + 1));
   V* twy = reinterpret_cast<V*>(ptr);
   ptr += lay.twy;
   V* kres = reinterpret_cast<V*>(ptr);  // [item][comp][ky][2]
   ptr += lay.kres;
   V* colraw = reinterpret_cast<V*>(ptr);  // [comp][y][2]
-  ptr += lay.colraw;
-  T* msm = reinterpret_cast<T*>(ptr);  // [slot][comp][x]
-  ptr += lay.mrows;
-  V* specraw = reinterpret_cast<V*>(ptr);  // [work][comp][kx]
-  ptr += lay.specraw;
-  T* hsm = reinterpret_cast<T*>(ptr);  // [work][comp][x]
-  ptr += lay.hrows;
-  Proposal<T>* prop = reinterpret_cast<Proposal<T>*>(ptr);
-  ptr += lay.prop;
-  V* fa = reinterpret_cast<V*>(ptr);
-  ptr += lay.fft;
-  V* fb = reinterpret_cast<V*>(ptr);
+  V* fa = R.fa;
+  V* fb = R.fb;
+  R.rows = s_rows;
+  R.h = P.h;
+  R.y0 = blockIdx.x * P.band;
+  R.nb = max(0, min(P.band, ny - R.y0));
 
   const McCoef<T> c = *P.coef;
   unsigned int target = 0;
@@ -179,20 +154,11 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(Fused2D<T> P) {
   auto stamp = [&](int sw, int point) {
     if (timed && sw >= 0 && sw < FUSED_TSWEEPS) P.tbuf[((size_t)sw * FUSED_TPOINTS + point) * 2 + tcol] = global_ns();
   };
-
-  const int y0 = blockIdx.x * P.band;
-  const int nb = max(0, min(P.band, ny - y0));  // own rows: slots 2 .. nb+1
-  const int nslots = nb + 4;
-  const int nwork = nb + 2;                     // work rows: slots 1 .. nb+2
-  const int half = (nx + 1) >> 1;
-  const size_t mstride = 3 * (size_t)nx;
-  const int elems = 16 / (int)sizeof(T);        // m values per 16-byte copy
-  const int per_m = nx / elems;                 // 16-byte copies per component row of m
-  const int ve = 16 / (int)sizeof(V);           // spectrum values per 16-byte copy
-  const int per_s = hxp / ve;                   // 16-byte copies per component row of S
-  if (threadIdx.x < nslots) s_rows[threadIdx.x] = fused_row(y0 - 2 + (int)threadIdx.x, ny, g.per[1]);
+  const int nb = R.nb;
+  const int ve = 16 / (int)sizeof(V);  // spectrum values per 16-byte copy
+  if (threadIdx.x < nb + 4) s_rows[threadIdx.x] = band_row(R.y0 - 2 + (int)threadIdx.x, ny, g.per[1]);
   if (threadIdx.x == 0) s_acc = 0;
-  load_twiddles<T>(P.px, twx);
+  load_twiddles<T>(P.px, R.twx);
   load_twiddles<T>(P.py, twy);
   // resident tensor spectrum of the owned kx pairs
   for (int it = 0; it < lay.resident; ++it) {
@@ -208,37 +174,8 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(Fused2D<T> P) {
   cp_async_wait_all();
   __syncthreads();
 
-  // forward x-FFT of the band rows held in msm -> spectrum rows in global memory
-  auto x_forward_band = [&]() {
-    for (int idx = threadIdx.x; idx < nb * L; idx += blockDim.x) {
-      const int rr = idx / L, x = idx - rr * L;
-      const T* row = msm + (size_t)(rr + 2) * mstride;
-      V a = cmk<V>(0, 0), b = cmk<V>(0, 0);
-      if (x < nx) {
-        a = cmk<V>(row[x], row[nx + x]);
-        b = cmk<V>(row[2 * nx + x], (T)0);
-      }
-      fa[(size_t)(2 * rr) * L + x] = a;
-      fa[(size_t)(2 * rr + 1) * L + x] = b;
-    }
-    __syncthreads();
-    V* res = fft_run<T, false>(fa, fb, 2 * nb, L, P.px, twx);
-    for (int idx = threadIdx.x; idx < nb * hx; idx += blockDim.x) {
-      const int rr = idx / hx, k = idx - rr * hx;
-      const V* la = res + (size_t)(2 * rr) * L;
-      const V* lb = la + L;
-      const int kn = k == 0 ? 0 : L - k;
-      const V A = la[k], B = la[kn];
-      const V A2 = lb[k], B2 = lb[kn];
-      const long long off = (long long)(y0 + rr) * hxp + k;
-      P.S[off] = cmk<V>((T)0.5 * (A.x + B.x), (T)0.5 * (A.y - B.y));
-      P.S[nspec + off] = cmk<V>((T)0.5 * (A.y + B.y), (T)-0.5 * (A.x - B.x));
-      P.S[2 * nspec + off] = cmk<V>((T)0.5 * (A2.x + B2.x), (T)0.5 * (A2.y - B2.y));
-    }
-  };
-
-  // y-FFT, tensor product, inverse y-FFT for the owned kx pairs
-  auto column_phase = [&](int sw) {
+  // y-FFT, tensor product, inverse y-FFT for the owned kx pairs of spectrum S
+  auto column_phase = [&](int sw, C<T>* S) {
     for (int it = 0; it < lay.items; ++it) {
       const int j = blockIdx.x + it * G;
       if (j >= lay.npairs) break;
@@ -246,7 +183,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(Fused2D<T> P) {
       for (int idx = threadIdx.x; idx < 3 * ny; idx += blockDim.x) {
         const int cc = idx / ny, y = idx - cc * ny;
         for (int q = 0; q < 2 / ve; ++q)
-          cp_async16(colraw + ((size_t)cc * ny + y) * 2 + q * ve, P.S + cc * nspec + (long long)y * hxp + kx0 + q * ve);
+          cp_async16(colraw + ((size_t)cc * ny + y) * 2 + q * ve, S + cc * nspec + (long long)y * hxp + kx0 + q * ve);
       }
       const V* kp = kres + (size_t)it * 6 * Ly * 2;
       if (!lay.resident) {  // stream K^ into kres (room for one item)
@@ -292,7 +229,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(Fused2D<T> P) {
       V* r = fft_run<T, true>(cur, oth, 6, Ly + 1, P.py, twy);
       for (int idx = threadIdx.x; idx < 3 * ny; idx += blockDim.x) {
         const int cc = idx / ny, y = idx - cc * ny;
-        V* dst = P.S + cc * nspec + (long long)y * hxp + kx0;
+        V* dst = S + cc * nspec + (long long)y * hxp + kx0;
         dst[0] = r[(size_t)(2 * cc) * (Ly + 1) + y];
         dst[1] = r[(size_t)(2 * cc + 1) * (Ly + 1) + y];
       }
@@ -301,154 +238,47 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(Fused2D<T> P) {
   };
 
   // prologue: spectrum of the initial m
-  for (int idx = threadIdx.x; idx < nb * 3 * per_m; idx += blockDim.x) {
-    const int rr = idx / (3 * per_m), rem = idx - rr * 3 * per_m;
-    const int cc = rem / per_m, q = rem - cc * per_m;
-    cp_async16(msm + (size_t)(rr + 2) * mstride + (size_t)cc * nx + q * elems,
-               P.m + cc * n + (long long)(y0 + rr) * nx + q * elems);
+  {
+    const int nx = g.nx;
+    const int elems = 16 / (int)sizeof(T), per_m = nx / elems;
+    for (int idx = threadIdx.x; idx < nb * 3 * per_m; idx += blockDim.x) {
+      const int rr = idx / (3 * per_m), rem = idx - rr * 3 * per_m;
+      const int cc = rem / per_m, q = rem - cc * per_m;
+      cp_async16(R.msm + (size_t)(rr + 2) * 3 * nx + (size_t)cc * nx + q * elems,
+                 P.m + cc * g.n + (long long)(R.y0 + rr) * nx + q * elems);
+    }
+    cp_async_wait_all();
+    __syncthreads();
   }
-  cp_async_wait_all();
-  __syncthreads();
-  x_forward_band();
+  R.So = P.S;
+  row_forward<T>(R);
   if (!grid_sync(P.bar, target, &s_flag)) return;
-  column_phase(-1);
+  column_phase(-1, P.S);
   if (!grid_sync(P.bar, target, &s_flag)) return;
 
   unsigned int my_acc = 0;
   for (int sw = 0; sw < P.nsweeps; ++sw) {
     const uint32_t sweep = P.sweep0 + (uint32_t)sw;
     const bool last = sw == P.nsweeps - 1;
+    // even sweeps (m, S) -> (m2, S2), odd sweeps back
+    R.m = (sw & 1) ? P.m2 : P.m;
+    R.mo = (sw & 1) ? P.m : P.m2;
+    R.S = (sw & 1) ? P.S2 : P.S;
+    R.So = (sw & 1) ? P.S : P.S2;
     stamp(sw, 0);
-    // m rows of every slot, spectrum rows of the work slots: 16-byte async copies
-    for (int idx = threadIdx.x; idx < nslots * 3 * per_m; idx += blockDim.x) {
-      const int slot = idx / (3 * per_m), rem = idx - slot * 3 * per_m;
-      const int r = s_rows[slot];
-      if (r < 0) continue;
-      const int cc = rem / per_m, q = rem - cc * per_m;
-      cp_async16(msm + (size_t)slot * mstride + (size_t)cc * nx + q * elems,
-                 P.m + cc * n + (long long)r * nx + q * elems);
-    }
-    for (int idx = threadIdx.x; idx < nwork * 3 * per_s; idx += blockDim.x) {
-      const int w = idx / (3 * per_s), rem = idx - w * 3 * per_s;
-      const int r = s_rows[w + 1];
-      if (r < 0) continue;
-      const int cc = rem / per_s, q = rem - cc * per_s;
-      cp_async16(specraw + ((size_t)w * 3 + cc) * hxp + q * ve, P.S + cc * nspec + (long long)r * hxp + q * ve);
-    }
-    // Philox proposals while the copies are in flight: colour 0 of the work
-    // rows, then colour 1 of the band rows
-    for (int idx = threadIdx.x; idx < (nwork + nb) * half; idx += blockDim.x) {
-      const int k = idx / half, j = idx - k * half;
-      const int color = k < nwork ? 0 : 1;
-      const int slot = color == 0 ? 1 + k : 2 + (k - nwork);
-      const int y = s_rows[slot];
-      if (y < 0) continue;
-      const int x = 2 * j + ((color + y) & 1);
-      if (x >= nx) continue;
-      prop[idx] = mc_propose<T>(c, (uint32_t)(x + nx * y), P.stage, sweep);
-    }
-    cp_async_wait_all();
-    __syncthreads();
+    row_load<T>(R, c, P.stage, sweep);
     stamp(sw, 1);
-    // inverse x-FFT of the work rows -> h
-    for (int idx = threadIdx.x; idx < nwork * L; idx += blockDim.x) {
-      const int w = idx / L, k = idx - w * L;
-      V A = cmk<V>(0, 0), B = cmk<V>(0, 0);
-      if (s_rows[w + 1] >= 0) {
-        const bool lo = k < hx;
-        const int kk = lo ? k : L - k;
-        const V* sr = specraw + (size_t)w * 3 * hxp;
-        V v0 = sr[kk], v1 = sr[hxp + kk], v2 = sr[2 * hxp + kk];
-        if (!lo) {
-          v0.y = -v0.y;
-          v1.y = -v1.y;
-          v2.y = -v2.y;
-        }
-        if (k == 0 || 2 * k == L) v0.y = v1.y = v2.y = 0;
-        A = cmk<V>(v0.x - v1.y, v0.y + v1.x);
-        B = v2;
-      }
-      fa[(size_t)(2 * w) * L + k] = A;
-      fa[(size_t)(2 * w + 1) * L + k] = B;
-    }
-    __syncthreads();
-    {
-      V* res = fft_run<T, true>(fa, fb, 2 * nwork, L, P.px, twx);
-      for (int idx = threadIdx.x; idx < nwork * nx; idx += blockDim.x) {
-        const int w = idx / nx, x = idx - w * nx;
-        const V a = res[(size_t)(2 * w) * L + x];
-        const V b = res[(size_t)(2 * w + 1) * L + x];
-        T* hr = hsm + (size_t)w * mstride;
-        hr[x] = a.x;
-        hr[nx + x] = a.y;
-        hr[2 * nx + x] = b.x;
-      }
-    }
-    __syncthreads();
+    row_field<T>(R);
     stamp(sw, 2);
-    // colour 0 on work rows, colour 1 on band rows
-    for (int color = 0; color < 2; ++color) {
-      const int kbase = color == 0 ? 0 : nwork;
-      const int kcnt = color == 0 ? nwork : nb;
-      for (int idx = threadIdx.x; idx < kcnt * half; idx += blockDim.x) {
-        const int k = kbase + idx / half, j = idx - (idx / half) * half;
-        const int slot = color == 0 ? 1 + k : 2 + (k - nwork);
-        const int y = s_rows[slot];
-        if (y < 0) continue;
-        const int x = 2 * j + ((color + y) & 1);
-        if (x >= nx) continue;
-        T* row = msm + (size_t)slot * mstride;
-        Nbrs<T> nbv;
-#pragma unroll
-        for (int s = 0; s < 2; ++s) {
-          int xx = x + (s ? 1 : -1);
-          bool ok = true;
-          if (xx < 0 || xx >= nx) {
-            if (g.per[0]) xx = xx < 0 ? xx + nx : xx - nx;
-            else ok = false;
-          }
-          if (xx == x) ok = false;
-          nbv.has[0][s] = ok;
-          const int xs = ok ? xx : x;
-          nbv.v[0][s][0] = row[xs];
-          nbv.v[0][s][1] = row[nx + xs];
-          nbv.v[0][s][2] = row[2 * nx + xs];
-          const int ns = slot + (s ? 1 : -1);
-          const bool oky = s_rows[ns] >= 0 && s_rows[ns] != y;
-          nbv.has[1][s] = oky;
-          const T* r2 = msm + (size_t)(oky ? ns : slot) * mstride;
-          nbv.v[1][s][0] = r2[x];
-          nbv.v[1][s][1] = r2[nx + x];
-          nbv.v[1][s][2] = r2[2 * nx + x];
-          nbv.has[2][s] = false;
-          nbv.v[2][s][0] = nbv.v[2][s][1] = nbv.v[2][s][2] = (T)0;
-        }
-        const T* hr = hsm + (size_t)(slot - 1) * mstride;
-        const Proposal<T> p = prop[k * half + j];
-        if (mc_accept<T>(c, nbv, row[x], row[nx + x], row[2 * nx + x], hr[x], hr[nx + x], hr[2 * nx + x], p)) {
-          row[x] = p.x;
-          row[nx + x] = p.y;
-          row[2 * nx + x] = p.z;
-          if (slot >= 2 && slot < 2 + nb) my_acc += 1;
-        }
-      }
-      __syncthreads();
-    }
+    my_acc += row_sweep<T>(R, c);
     stamp(sw, 3);
-    // store the band's m (and h after the last sweep)
-    for (int idx = threadIdx.x; idx < nb * (int)mstride; idx += blockDim.x) {
-      const int rr = idx / (int)mstride, rem = idx - rr * (int)mstride;
-      const int cc = rem / nx, x = rem - cc * nx;
-      const long long gi = cc * n + (long long)(y0 + rr) * nx + x;
-      P.m[gi] = msm[(size_t)(rr + 2) * mstride + rem];
-      if (last) P.h[gi] = hsm[(size_t)(rr + 1) * mstride + rem];
-    }
+    row_store<T>(R, last);
     if (last) break;
-    x_forward_band();
+    row_forward<T>(R);
     stamp(sw, 4);
     if (!grid_sync(P.bar, target, &s_flag)) return;
     stamp(sw, 5);
-    column_phase(sw);
+    column_phase(sw, R.So);
     stamp(sw, 7);
     if (!grid_sync(P.bar, target, &s_flag)) return;
     stamp(sw, 8);
@@ -467,11 +297,22 @@ size_t fused2d_smem_bytes(const Geom& g, const FftPlan& px, const FftPlan& py, i
   return fused2d_layout<T>(g, px, py, band, nblocks).total;
 }
 
+// The kernels' dynamic shared-memory limit is raised to the device's opt-in
+// maximum once, not to one lattice's need: the attribute is per kernel and
+// process-wide, so a later, smaller lattice must not lower it under an
+// earlier one.
+inline cudaError_t raise_smem_limit(const void* fn) {
+  int dev = 0, optin = 48 * 1024;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  return e;
+}
+
 template <typename T>
 cudaError_t fused2d_blocks_per_sm(const Geom& g, const FftPlan& px, const FftPlan& py, int band, int* out) {
   const size_t smem = fused2d_smem_bytes<T>(g, px, py, band);
-  cudaError_t e =
-      cudaFuncSetAttribute((const void*)k_fused2d<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit((const void*)k_fused2d<T>);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(out, (const void*)k_fused2d<T>, FUSED_THREADS, smem);
 }
@@ -485,8 +326,11 @@ cudaError_t launch_fused2d(const Geom& g, const FftPlan& px, const FftPlan& py, 
   P.py = py;
   P.coef = a.coef;
   P.m = a.m;
+  P.m2 = a.m2;
   P.h = a.h;
   P.S = reinterpret_cast<C<T>*>(a.spec);
+  P.S2 = reinterpret_cast<C<T>*>(a.spec2);
+  if (!a.m2 || !a.spec2 || a.m2 == a.m || a.spec2 == a.spec) return cudaErrorInvalidValue;
   P.K = reinterpret_cast<const C<T>*>(a.khat);
   P.acc = a.acc;
   P.bar = a.bar;
@@ -503,10 +347,42 @@ cudaError_t launch_fused2d(const Geom& g, const FftPlan& px, const FftPlan& py, 
   return cudaLaunchCooperativeKernel((const void*)k_fused2d<T>, dim3(nblocks), dim3(FUSED_THREADS), args, smem, st);
 }
 
+// ------------------------------------------------------- batched film sweeps
+template <typename T>
+size_t rows_smem_bytes(const Geom& g, const FftPlan& px, int band) {
+  return row_phase_bytes<T>(g, px, band, px.warp_a == 0);
+}
+
+template <typename T>
+cudaError_t rows_prepare(const Geom& g, const FftPlan& px, int band, int* blocks_per_sm) {
+  const size_t smem = rows_smem_bytes<T>(g, px, band);
+  cudaError_t e = raise_smem_limit((const void*)k_rows<T>);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, (const void*)k_rows<T>, 256, smem);
+}
+
+template <typename T>
+cudaError_t launch_rows(const Geom& g, const FftPlan& px, const McCoef<T>* coef, const T* m, T* mo, T* h,
+                        const void* spec, void* spec_out, unsigned long long* acc, const SweepCounters* ctr, int band,
+                        int nrep, bool with_h, bool do_forward, cudaStream_t st) {
+  if (m == mo || spec == spec_out) return cudaErrorInvalidValue;  // halo rows must not be overwritten
+  const size_t smem = rows_smem_bytes<T>(g, px, band);
+  dim3 grid((g.ny + band - 1) / band, 1, nrep);
+  k_rows<T><<<grid, 256, smem, st>>>(g, px, coef, m, mo, h, reinterpret_cast<const C<T>*>(spec),
+                                     reinterpret_cast<C<T>*>(spec_out), acc, ctr, band, with_h ? 1 : 0,
+                                     do_forward ? 1 : 0);
+  return cudaGetLastError();
+}
+
 #define MMC_INSTANTIATE_FUSED(T)                                                                                \
   template size_t fused2d_smem_bytes<T>(const Geom&, const FftPlan&, const FftPlan&, int);                     \
   template cudaError_t fused2d_blocks_per_sm<T>(const Geom&, const FftPlan&, const FftPlan&, int, int*);       \
   template cudaError_t launch_fused2d<T>(const Geom&, const FftPlan&, const FftPlan&, const FusedArgs<T>&, int, \
-                                         cudaStream_t);
+                                         cudaStream_t);                                                        \
+  template size_t rows_smem_bytes<T>(const Geom&, const FftPlan&, int);                                        \
+  template cudaError_t rows_prepare<T>(const Geom&, const FftPlan&, int, int*);                                \
+  template cudaError_t launch_rows<T>(const Geom&, const FftPlan&, const McCoef<T>*, const T*, T*, T*,        \
+                                      const void*, void*, unsigned long long*, const SweepCounters*, int, int, bool, \
+                                      bool, cudaStream_t);
 
 }  // namespace mmc

@@ -41,17 +41,29 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrow
   V* bufA = tw + ((p.tw_total + 1) & ~1);
   V* bufB = bufA + (long long)rows_per_cta * npairs * L;
   load_twiddles<T>(p, tw);
-  for (int idx = threadIdx.x; idx < nr * L; idx += blockDim.x) {
-    const int rr = idx / L, x = idx - rr * L;
-    const long long rbase = (long long)(row0 + rr) * xdata + x;
-    for (int pr = 0; pr < npairs; ++pr) {
-      const int ca = 2 * pr, cb = 2 * pr + 1;
-      T va = 0, vb = 0;
-      if (x < xdata) {
-        va = in[ca * in_cstride + rbase];
-        if (cb < ncomp) vb = in[cb * in_cstride + rbase];
+  // loads are issued four elements per thread at a time, before any store, so
+  // their latencies overlap
+  const int total = nr * L;
+  for (int base = threadIdx.x; base < total; base += 4 * blockDim.x) {
+    T v[4][6];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int idx = base + u * blockDim.x;
+      const int rr = idx / L, x = idx - rr * L;
+      const bool ok = idx < total && x < xdata;
+      const long long rbase = (long long)(row0 + rr) * xdata + x;
+#pragma unroll
+      for (int c = 0; c < 6; ++c) v[u][c] = (ok && c < ncomp) ? in[c * in_cstride + rbase] : (T)0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int idx = base + u * blockDim.x;
+      if (idx < total) {
+        const int rr = idx / L, x = idx - rr * L;
+#pragma unroll
+        for (int pr = 0; pr < 3; ++pr)
+          if (pr < npairs) bufA[(long long)(rr * npairs + pr) * L + x] = cmk<V>(v[u][2 * pr], v[u][2 * pr + 1]);
       }
-      bufA[(long long)(rr * npairs + pr) * L + x] = cmk<V>(va, vb);
     }
   }
   __syncthreads();
@@ -88,22 +100,34 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
   V* bufA = tw + ((p.tw_total + 1) & ~1);
   V* bufB = bufA + (long long)rows_per_cta * 2 * L;
   load_twiddles<T>(p, tw);
-  for (int idx = threadIdx.x; idx < nr * L; idx += blockDim.x) {
-    const int rr = idx / L, k = idx - rr * L;
-    const int row = row0 + rr;
-    const int y = row % yout, z = row / yout;
-    const long long base = ((long long)z * nyp + y) * pitch;
-    V v[3];
-    const bool lo = k < hx;
-    const long long kk = lo ? k : L - k;
-    for (int c = 0; c < 3; ++c) {
-      V s = S[c * nspec + base + kk];
-      if (!lo) s.y = -s.y;
-      if (k == 0 || 2 * k == L) s.y = 0;  // bins that are real for a real output
-      v[c] = s;
+  const int total = nr * L;
+  for (int base0 = threadIdx.x; base0 < total; base0 += 4 * blockDim.x) {
+    V v[4][3];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int idx = base0 + u * blockDim.x;
+      const int rr = idx / L, k = idx - rr * L;
+      const int row = row0 + rr;
+      const int y = row % yout, z = row / yout;
+      const long long base = ((long long)z * nyp + y) * pitch;
+      const long long kk = k < hx ? k : L - k;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) v[u][c] = idx < total ? S[c * nspec + base + kk] : cmk<V>(0, 0);
     }
-    bufA[(long long)(rr * 2) * L + k] = cmk<V>(v[0].x - v[1].y, v[0].y + v[1].x);
-    bufA[(long long)(rr * 2 + 1) * L + k] = v[2];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int idx = base0 + u * blockDim.x;
+      if (idx < total) {
+        const int rr = idx / L, k = idx - rr * L;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          if (k >= hx) v[u][c].y = -v[u][c].y;
+          if (k == 0 || 2 * k == L) v[u][c].y = 0;  // bins that are real for a real output
+        }
+        bufA[(long long)(rr * 2) * L + k] = cmk<V>(v[u][0].x - v[u][1].y, v[u][0].y + v[u][1].x);
+        bufA[(long long)(rr * 2 + 1) * L + k] = v[u][2];
+      }
+    }
   }
   __syncthreads();
   V* res = fft_run<T, true>(bufA, bufB, nr * 2, L, p, tw);
@@ -141,14 +165,52 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
   const int nlines = ncomp * ntx;
   V* bufA = tw + ((p.tw_total + 1) & ~1);
   V* bufB = bufA + (long long)ncomp * tx * stride;
+  V* ktile = bufB + (long long)ncomp * tx * stride;  // [comp][pos][t] when PASS_MUL
   load_twiddles<T>(p, tw);
-  for (int idx = threadIdx.x; idx < ncomp * L * ntx; idx += blockDim.x) {
-    const int t = idx % ntx;
-    const int rest = idx / ntx;
-    const int pos = rest % L, c = rest / L;
-    V val = cmk<V>(0, 0);
-    if (pos < load_lim) val = S[c * nspec + pbase + pos * pos_stride + t];
-    bufA[(long long)(c * ntx + t) * stride + pos] = val;
+  // the tensor tile goes to shared memory asynchronously while the forward
+  // transform runs (16-byte copies when the tile rows are 16-byte aligned)
+  const bool kasync = (flags & PASS_MUL) && (((long long)ntx * sizeof(V)) % 16 == 0) && ((kx0 * sizeof(V)) % 16 == 0) &&
+                      ((plane_stride * sizeof(V)) % 16 == 0) && ((pos_stride * sizeof(V)) % 16 == 0);
+  if (flags & PASS_MUL) {
+    const int per = (int)(ntx * sizeof(V) / 16);
+    if (kasync) {
+      for (int idx = threadIdx.x; idx < 6 * L * per; idx += blockDim.x) {
+        const int q = idx % per, rest = idx / per;
+        const int pos = rest % L, c = rest / L;
+        const int e = 16 / (int)sizeof(V);
+        const unsigned sd = (unsigned)__cvta_generic_to_shared(ktile + ((long long)c * L + pos) * ntx + q * e);
+        const V* src = khat + c * nspec + pbase + pos * pos_stride + q * e;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sd), "l"(src) : "memory");
+      }
+    } else {
+      for (int idx = threadIdx.x; idx < 6 * L * ntx; idx += blockDim.x) {
+        const int t = idx % ntx, rest = idx / ntx;
+        const int pos = rest % L, c = rest / L;
+        ktile[((long long)c * L + pos) * ntx + t] = khat[c * nspec + pbase + pos * pos_stride + t];
+      }
+    }
+  }
+  const int total = ncomp * L * ntx;
+  for (int base = threadIdx.x; base < total; base += 4 * blockDim.x) {
+    V v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int idx = base + u * blockDim.x;
+      const int t = idx % ntx;
+      const int rest = idx / ntx;
+      const int pos = rest % L, c = rest / L;
+      v[u] = (idx < total && pos < load_lim) ? S[c * nspec + pbase + pos * pos_stride + t] : cmk<V>(0, 0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int idx = base + u * blockDim.x;
+      if (idx < total) {
+        const int t = idx % ntx;
+        const int rest = idx / ntx;
+        const int pos = rest % L, c = rest / L;
+        bufA[(long long)(c * ntx + t) * stride + pos] = v[u];
+      }
+    }
   }
   __syncthreads();
   V* cur = bufA;
@@ -161,11 +223,14 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
     }
   }
   if (flags & PASS_MUL) {
+    if (kasync) asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
     for (int idx = threadIdx.x; idx < L * ntx; idx += blockDim.x) {
       const int t = idx % ntx, pos = idx / ntx;
-      const long long ka = pbase + pos * pos_stride + t;
-      const V kxx = khat[ka], kxy = khat[nspec + ka], kxz = khat[2 * nspec + ka];
-      const V kyy = khat[3 * nspec + ka], kyz = khat[4 * nspec + ka], kzz = khat[5 * nspec + ka];
+      const V* kk = ktile + (long long)pos * ntx + t;
+      const long long ks = (long long)L * ntx;
+      const V kxx = kk[0], kxy = kk[ks], kxz = kk[2 * ks];
+      const V kyy = kk[3 * ks], kyz = kk[4 * ks], kzz = kk[5 * ks];
       V* px = cur + (long long)(0 * ntx + t) * stride + pos;
       V* py = cur + (long long)(1 * ntx + t) * stride + pos;
       V* pz = cur + (long long)(2 * ntx + t) * stride + pos;
@@ -637,8 +702,9 @@ __global__ void k_khat_store(long long count, const double2* __restrict__ src, C
 inline size_t x_pass_smem(const FftPlan& p, int lines_per_row, int rows, size_t csize) {
   return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)rows * lines_per_row * p.n) * csize;
 }
-inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize) {
-  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)ncomp * tx * (p.n + 1)) * csize;
+inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize, bool mul) {
+  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)ncomp * tx * (p.n + 1) + (mul ? 6 * (size_t)p.n * tx : 0)) *
+         csize;
 }
 
 // Raises the dynamic shared-memory limit of the FFT pass kernels to the
@@ -673,7 +739,7 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
                          int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
                          int flags, T inv_n, int tx, int threads, cudaStream_t st, int nrep = 1,
                          long long s_rstride = 0) {
-  size_t sm = col_pass_smem(p, ncomp, tx, sizeof(C<T>));
+  size_t sm = col_pass_smem(p, ncomp, tx, sizeof(C<T>), (flags & PASS_MUL) != 0);
   dim3 grid((hx + tx - 1) / tx, planes, nrep);
   k_col_pass<T><<<grid, threads, sm, st>>>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
                                            store_lim, flags, inv_n, tx, s_rstride);
@@ -793,6 +859,14 @@ cudaError_t launch_init(const Geom& g, uint64_t seed, T* m, cudaStream_t st) {
   return init_impl<T>(g, seed, m, st);
 }
 template <typename T>
+cudaError_t launch_col_pass_2d(const Geom& g, const FftPlan& py, const DemagTuning& tun, void* spec,
+                               const void* khat, cudaStream_t st, int nrep) {
+  const T inv_n = (T)(1.0 / (double)g.np);
+  return run_col_pass<T>(py, 3, reinterpret_cast<C<T>*>(spec), g.nspec, reinterpret_cast<const C<T>*>(khat), g.hx, 1,
+                         (long long)g.nyp * g.hxp, g.hxp, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV, inv_n,
+                         tun.col_tx, tun.col_threads, st, nrep, 3 * g.nspec);
+}
+template <typename T>
 cudaError_t launch_prepare(int max_dyn_smem) {
   return prepare_impl<T>(max_dyn_smem);
 }
@@ -827,6 +901,8 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
                                        cudaStream_t);                                                          \
   template cudaError_t launch_init<T>(const Geom&, uint64_t, T*, cudaStream_t);                               \
   template cudaError_t launch_prepare<T>(int);                                                                \
+  template cudaError_t launch_col_pass_2d<T>(const Geom&, const FftPlan&, const DemagTuning&, void*, const void*, \
+                                             cudaStream_t, int);                                              \
   template cudaError_t launch_from_f64<T>(long long, const double*, T*, cudaStream_t);                        \
   template cudaError_t launch_to_f64<T>(long long, const T*, double*, cudaStream_t);                          \
   template cudaError_t launch_khat_store<T>(long long, const double2*, void*, cudaStream_t);

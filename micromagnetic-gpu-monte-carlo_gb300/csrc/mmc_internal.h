@@ -146,8 +146,10 @@ template <typename T>
 struct FusedArgs {
   const McCoef<T>* coef;
   T* m;
+  T* m2;  // second copy of m: the result of an odd sweep count lands here
   T* h;
   void* spec;
+  void* spec2;
   const void* khat;
   unsigned long long* acc;
   GridBarrier* bar;
@@ -165,6 +167,20 @@ template <typename T>
 cudaError_t launch_fused2d(const Geom& g, const FftPlan& px, const FftPlan& py, const FusedArgs<T>& a, int nblocks,
                            cudaStream_t st);
 size_t grid_barrier_bytes();
+
+// Batched film sweeps (fused2d.cuh / rows.cuh): the row kernel (inverse x
+// transform, both colours, forward x transform) and the 2-D column pass.
+template <typename T>
+size_t rows_smem_bytes(const Geom& g, const FftPlan& px, int band);
+template <typename T>
+cudaError_t rows_prepare(const Geom& g, const FftPlan& px, int band, int* blocks_per_sm);
+template <typename T>
+cudaError_t launch_rows(const Geom& g, const FftPlan& px, const McCoef<T>* coef, const T* m, T* mo, T* h,
+                        const void* spec, void* spec_out, unsigned long long* acc, const SweepCounters* ctr, int band,
+                        int nrep, bool with_h, bool do_forward, cudaStream_t st);
+template <typename T>
+cudaError_t launch_col_pass_2d(const Geom& g, const FftPlan& py, const DemagTuning& tun, void* spec,
+                               const void* khat, cudaStream_t st, int nrep);
 
 // Parallel tempering across the replicas of a batch (kernels_f64.cu).
 // replica_at[l * K + k] is the replica holding temperature temps[l * K + k] of

@@ -145,6 +145,18 @@ size_t smem_limit() { return 200 * 1024; }
 // 32 / B lines, so a CTA takes enough rows / columns to keep all its warps
 // busy, and column tiles are widened to whole 32-byte sectors when there are
 // enough CTAs to cover the SMs twice.
+// threads of a column pass: enough warps for the lines of one tile (3
+// components x tx columns)
+int col_threads_for(const Geom& g, const FftPlan& py, const FftPlan& pz, int tx, int tx_z) {
+  auto threads_for = [&](const FftPlan& p, int t) {
+    if (!p.warp_a) return 256;
+    const int lines_per_warp = 32 / p.warp_b;
+    const int warps = (3 * t + lines_per_warp - 1) / lines_per_warp;
+    return std::max(64, std::min(512, 32 * warps));
+  };
+  return g.nzp == 1 ? threads_for(py, tx) : std::max(threads_for(py, tx), threads_for(pz, tx_z));
+}
+
 DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz, size_t csize,
                           int nsm, int nrep) {
   DemagTuning t;
@@ -163,7 +175,7 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   while (r > 1 && xsm(r) > 96 * 1024) r /= 2;
   t.x_rows_per_cta = r;
   auto csm = [&](const FftPlan& p, int tx) {
-    return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * (p.n + 1)) * csize;
+    return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * (p.n + 1) + 6 * (size_t)p.n * tx) * csize;
   };
   auto pick = [&](const FftPlan& p, int planes) {
     int tx = 8;
@@ -173,15 +185,17 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   };
   t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz);
   t.col_tx_z = pick(pz, g.nyp);
-  // threads: enough warps for the lines of one tile (3 components x tx columns)
-  auto threads_for = [&](const FftPlan& p, int tx) {
-    if (!p.warp_a) return 256;
-    const int lines_per_warp = 32 / p.warp_b;
-    const int warps = (3 * tx + lines_per_warp - 1) / lines_per_warp;
-    return std::max(64, std::min(512, 32 * warps));
-  };
-  t.col_threads = std::max(threads_for(py, t.col_tx), threads_for(pz, t.col_tx_z));
+  t.col_threads = col_threads_for(g, py, pz, t.col_tx, t.col_tx_z);
   return t;
+}
+
+// Shared memory of an x pass with r rows per CTA, of a column pass with tx
+// columns per CTA (bytes).
+size_t x_pass_smem(const FftPlan& px, int r, size_t csize) {
+  return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize;
+}
+size_t col_pass_smem(const FftPlan& p, int tx, size_t csize) {
+  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * (p.n + 1) + 6 * (size_t)p.n * tx) * csize;
 }
 
 }  // namespace
@@ -227,6 +241,8 @@ struct mmc_handle {
   int fused_band = 0;
   int fused_blocks = 0;
   GridBarrier* bar = nullptr;
+  void* m2 = nullptr;     // film engine: second copy of m (3n T)
+  void* spec2 = nullptr;  // film engine: second spectrum (3*nspec complex T)
   int nsm = 0;
 };
 
@@ -393,8 +409,10 @@ cudaError_t fused_chunk(mmc_handle* h, long long stage, long long sweep0, int ns
   FusedArgs<T> a;
   a.coef = (const McCoef<T>*)h->coef;
   a.m = (T*)h->m;
+  a.m2 = (T*)h->m2;
   a.h = (T*)h->h;
   a.spec = h->spec;
+  a.spec2 = h->spec2;
   a.khat = h->khat;
   a.acc = h->acc;
   a.bar = h->bar;
@@ -403,7 +421,11 @@ cudaError_t fused_chunk(mmc_handle* h, long long stage, long long sweep0, int ns
   a.sweep0 = (uint32_t)sweep0;
   a.nsweeps = ns;
   a.band = h->fused_band;
-  return launch_fused2d<T>(h->g, h->px.p, h->py.p, a, h->fused_blocks, h->st);
+  cudaError_t e = launch_fused2d<T>(h->g, h->px.p, h->py.p, a, h->fused_blocks, h->st);
+  // an odd sweep count leaves the result in the second copy
+  if (e == cudaSuccess && (ns & 1))
+    e = cudaMemcpyAsync(h->m, h->m2, 3 * (size_t)h->g.n * sizeof(T), cudaMemcpyDeviceToDevice, h->st);
+  return e;
 }
 
 int run_fused(mmc_handle* h, long long stage, long long sweep0, long long nsweeps) {
@@ -470,6 +492,8 @@ int setup_engine(mmc_handle* h, int nsm) {
       CU(cudaMalloc(&p, grid_barrier_bytes()));
       CU(cudaMemset(p, 0, grid_barrier_bytes()));
       h->bar = (GridBarrier*)p;
+      CU(cudaMalloc(&h->m2, 3 * (size_t)g.n * h->tsize));
+      CU(cudaMalloc(&h->spec2, 3 * (size_t)g.nspec * 2 * h->tsize));
       return MMC_OK;
     }
   }
@@ -739,8 +763,8 @@ void destroy_impl(mmc_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
-  void* bufs[] = {h->m,   h->h,   h->spec,    h->khat,    h->coef,    h->partials,   h->red,
-                  h->acc, h->ctr, h->stage64, h->field64, (void*)h->bar, (void*)h->ecoef};
+  void* bufs[] = {h->m,   h->h,   h->spec,    h->khat,    h->coef,          h->partials,     h->red,
+                  h->acc, h->ctr, h->stage64, h->field64, (void*)h->bar, (void*)h->ecoef, h->m2, h->spec2};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->red_host) cudaFreeHost(h->red_host);
@@ -975,6 +999,8 @@ struct mmc_batch {
   mmc_handle* base = nullptr;  // geometry, plans, tensor (replica 0's config)
   int R = 0;
   DemagTuning tun{};
+  int rows_band = 0;  // > 0: film sweeps run as row kernel + column pass
+  std::vector<int> row_bands;  // bands the row kernel can run with on this device
   std::vector<mmc_config> cfgs;
   std::vector<long long> seeds;
   std::vector<double> T;
@@ -982,6 +1008,8 @@ struct mmc_batch {
   void* m = nullptr;
   void* h = nullptr;
   void* spec = nullptr;
+  void* m2 = nullptr;     // row kernel path: second copies of m and of the spectrum
+  void* spec2 = nullptr;
   void* coef = nullptr;
   EnCoef* ecoef = nullptr;
   double* partials = nullptr;
@@ -1020,7 +1048,7 @@ void batch_free(mmc_batch* b) {
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   void* bufs[] = {b->params,   b->m,           b->h,          b->spec,        b->coef,   b->ecoef,
                   b->partials, b->red,         b->acc,        b->ctr,         b->d_replica_at,
-                  b->d_temps,  b->d_replica_T, b->d_round,    b->d_counts};
+                  b->d_temps,  b->d_replica_T, b->d_round,    b->d_counts,    b->m2,     b->spec2};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (b->red_host) cudaFreeHost(b->red_host);
@@ -1050,6 +1078,52 @@ cudaError_t batch_demag(mmc_batch* b, cudaEvent_t* ev = nullptr) {
                               h->khat, h->st, b->R, ev);
 }
 
+// The second copies of m and of the spectrum that the row kernel path needs.
+int batch_alloc_rows(mmc_batch* b) {
+  const mmc_handle* h = b->base;
+  const size_t ts = h->tsize;
+  if (!b->m2) CU(cudaMalloc(&b->m2, (size_t)b->R * 3 * h->g.n * ts));
+  if (!b->spec2) CU(cudaMalloc(&b->spec2, (size_t)b->R * 3 * h->g.nspec * 2 * ts));
+  return MMC_OK;
+}
+
+// Film sweep as two launches: the row kernel (m, spec) -> (m2, spec2) on even
+// parity, back on odd, then the column pass on the written spectrum.  Requires
+// the read spectrum to hold K^.M^/N of the read m (the previous sweep's column
+// pass, or batch_demag).  ev (optional): [0] before the row kernel, [1] before
+// the column pass, [2] after it.
+cudaError_t batch_sweep_rows(mmc_batch* b, int parity, cudaEvent_t* ev = nullptr) {
+  mmc_handle* h = b->base;
+  void* mi = parity ? b->m2 : b->m;
+  void* mo = parity ? b->m : b->m2;
+  void* si = parity ? b->spec2 : b->spec;
+  void* so = parity ? b->spec : b->spec2;
+  cudaError_t e;
+  if (ev && (e = cudaEventRecord(ev[0], h->st)) != cudaSuccess) return e;
+  e = h->prec == 32 ? launch_rows<float>(h->g, h->px.p, (const McCoef<float>*)b->coef, (const float*)mi, (float*)mo,
+                                         (float*)b->h, si, so, b->acc, b->ctr, b->rows_band, b->R, false, true, h->st)
+                    : launch_rows<double>(h->g, h->px.p, (const McCoef<double>*)b->coef, (const double*)mi,
+                                          (double*)mo, (double*)b->h, si, so, b->acc, b->ctr, b->rows_band, b->R,
+                                          false, true, h->st);
+  if (e != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[1], h->st)) != cudaSuccess) return e;
+  e = h->prec == 32 ? launch_col_pass_2d<float>(h->g, h->py.p, b->tun, so, h->khat, h->st, b->R)
+                    : launch_col_pass_2d<double>(h->g, h->py.p, b->tun, so, h->khat, h->st, b->R);
+  if (e != cudaSuccess) return e;
+  if (ev && (e = cudaEventRecord(ev[2], h->st)) != cudaSuccess) return e;
+  return launch_advance(b->ctr, 1, h->st);
+}
+
+// After an odd number of row-kernel sweeps the state sits in the second
+// copies; move it back so m and spec are current again.
+cudaError_t batch_rows_settle(mmc_batch* b) {
+  mmc_handle* h = b->base;
+  cudaError_t e = cudaMemcpyAsync(b->m, b->m2, (size_t)b->R * 3 * h->g.n * h->tsize, cudaMemcpyDeviceToDevice, h->st);
+  if (e != cudaSuccess) return e;
+  return cudaMemcpyAsync(b->spec, b->spec2, (size_t)b->R * 3 * h->g.nspec * 2 * h->tsize, cudaMemcpyDeviceToDevice,
+                         h->st);
+}
+
 cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
   mmc_handle* h = b->base;
   cudaError_t e;
@@ -1063,6 +1137,19 @@ cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
   }
   if (ev && (e = cudaEventRecord(ev[4], h->st)) != cudaSuccess) return e;
   return launch_advance(b->ctr, 1, h->st);
+}
+
+// k sweeps; on the row kernel path they alternate between the two copies and
+// end in m and spec.
+cudaError_t batch_sweeps(mmc_batch* b, long long k) {
+  cudaError_t e = cudaSuccess;
+  if (b->rows_band > 0) {
+    for (long long q = 0; q < k && e == cudaSuccess; ++q) e = batch_sweep_rows(b, (int)(q & 1));
+    if (e == cudaSuccess && (k & 1)) e = batch_rows_settle(b);
+    return e;
+  }
+  for (long long q = 0; q < k && e == cudaSuccess; ++q) e = batch_sweep(b);
+  return e;
 }
 
 cudaError_t batch_energy_kernels(mmc_batch* b) {
@@ -1092,7 +1179,7 @@ int batch_graph(mmc_batch* b, int len, bool pt) {
   cudaGraph_t graph;
   CU(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
-  for (int s = 0; s < len && e == cudaSuccess; ++s) e = batch_sweep(b);
+  e = batch_sweeps(b, len);
   if (pt && e == cudaSuccess) e = batch_energy_kernels(b);
   if (pt && e == cudaSuccess) e = batch_swap(b);
   cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
@@ -1120,6 +1207,7 @@ int batch_run(mmc_batch* b, long long stage, long long sweep0, long long nsweeps
   SweepCounters c0{(uint32_t)stage, (uint32_t)sweep0};
   CU(cudaMemcpy(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice));
   CU(cudaEventRecord(h->ev[0], h->st));
+  if (b->rows_band > 0) CU(batch_demag(b));  // the row kernel starts from the spectrum of m
   long long done = 0;
   const int I = b->interval;
   int launches = 0;
@@ -1139,7 +1227,7 @@ int batch_run(mmc_batch* b, long long stage, long long sweep0, long long nsweeps
         done += I;
       } else {
         const long long k = std::min(to_boundary, nsweeps - done);
-        for (long long q = 0; q < k; ++q) CU(batch_sweep(b));
+        CU(batch_sweeps(b, k));
         done += k;
         if (k == to_boundary) {
           CU(batch_energy_kernels(b));
@@ -1156,7 +1244,8 @@ int batch_run(mmc_batch* b, long long stage, long long sweep0, long long nsweeps
       done += G;
       TRY(check_stop());
     }
-    for (; done < nsweeps; ++done) CU(batch_sweep(b));
+    CU(batch_sweeps(b, nsweeps - done));
+    done = nsweeps;
   }
   CU(cudaEventRecord(h->ev[1], h->st));
   CU(cudaStreamSynchronize(h->st));
@@ -1165,6 +1254,91 @@ int batch_run(mmc_batch* b, long long stage, long long sweep0, long long nsweeps
   b->last_ms = ms;
   b->proposed += (unsigned long long)nsweeps * (unsigned long long)h->g.n;
   return batch_sync_temperatures(b);
+}
+
+// Times every launch shape the batch can run with -- the row kernel with each
+// band that fits, the pass kernels with each x-pass row count and column-pass
+// width -- for `sweeps` sweeps from the current state, keeps the fastest and
+// puts the state back.  All shapes give bit-identical results.
+int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
+  mmc_handle* h = b->base;
+  TRY(ensure_demag(h));
+  TRY(batch_sync_temperatures(b));
+  TRY(h->prec == 32 ? batch_upload_coefs<float>(b) : batch_upload_coefs<double>(b));
+  struct Cand {
+    int rows_band;
+    DemagTuning tun;
+  };
+  std::vector<Cand> cands;
+  const Geom& g = h->g;
+  const size_t cs = 2 * h->tsize;
+  const DemagTuning base = choose_tuning(g, h->px.p, h->py.p, h->pz.p, cs, h->nsm, b->R);
+  if (h->cfg.cal_demag_flag)
+    for (int bd : b->row_bands) cands.push_back({bd, base});
+  cands.push_back({0, base});
+  if (h->cfg.cal_demag_flag) {
+    const long long rows = (long long)g.ny * g.nz;
+    for (int r : {1, 2, 4, 8, 16}) {
+      if (r > rows || x_pass_smem(h->px.p, r, cs) > smem_limit()) continue;
+      for (int tx : {1, 2, 4, 8}) {
+        if (tx > g.hx || col_pass_smem(h->py.p, tx, cs) > smem_limit()) continue;
+        if (r == base.x_rows_per_cta && tx == base.col_tx) continue;
+        DemagTuning t = base;
+        t.x_rows_per_cta = r;
+        t.col_tx = tx;
+        t.col_threads = col_threads_for(g, h->py.p, h->pz.p, tx, t.col_tx_z);
+        cands.push_back({0, t});
+      }
+    }
+  }
+  const size_t mbytes = (size_t)b->R * 3 * g.n * h->tsize;
+  void* saved = nullptr;
+  CU(cudaMalloc(&saved, mbytes));
+  std::vector<unsigned long long> acc0(b->R);
+  cudaError_t e = cudaMemcpyAsync(saved, b->m, mbytes, cudaMemcpyDeviceToDevice, h->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(acc0.data(), b->acc, b->R * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  int best = -1;
+  float best_t = 0;
+  int status = MMC_OK;
+  for (size_t i = 0; i < cands.size() && e == cudaSuccess && status == MMC_OK; ++i) {
+    if (cands[i].rows_band > 0 && (status = batch_alloc_rows(b)) != MMC_OK) break;
+    b->rows_band = cands[i].rows_band;
+    b->tun = cands[i].tun;
+    SweepCounters c0{0, 0};
+    e = cudaMemcpyAsync(b->m, saved, mbytes, cudaMemcpyDeviceToDevice, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess && b->rows_band > 0) e = batch_demag(b);
+    if (e == cudaSuccess) e = batch_sweeps(b, 2);  // warm-up
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev[0], h->st);
+    if (e == cudaSuccess) e = batch_sweeps(b, sweeps);
+    if (e == cudaSuccess) e = cudaEventRecord(h->ev[1], h->st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[1]);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+    if (e == cudaSuccess && (best < 0 || ms < best_t)) {
+      best = (int)i;
+      best_t = ms;
+    }
+  }
+  if (e == cudaSuccess && best >= 0) {
+    b->rows_band = cands[best].rows_band;
+    b->tun = cands[best].tun;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b->m, saved, mbytes, cudaMemcpyDeviceToDevice, h->st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(b->acc, acc0.data(), b->R * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+  cudaFree(saved);
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->graph_len = 0;
+  if (status != MMC_OK) return status;
+  CU(e);
+  if (best_ms) *best_ms = best_t / sweeps;
+  if (ncand) *ncand = (int)cands.size();
+  return MMC_OK;
 }
 
 int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out) {
@@ -1187,6 +1361,35 @@ int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out
   mmc_handle* h = b->base;
   b->R = R;
   b->tun = choose_tuning(h->g, h->px.p, h->py.p, h->pz.p, 2 * h->tsize, h->nsm, R);
+  {
+    const Geom& gg = h->g;
+    const bool film = h->cfg.cal_demag_flag && gg.nz == 1 && gg.nzp == 1 && gg.ncolors == 2 &&
+                      ((size_t)gg.nx * h->tsize) % 16 == 0 && ((size_t)gg.hxp * 2 * h->tsize) % 16 == 0;
+    int optin = 48 * 1024;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
+    if (film) {
+      const int bands[] = {4, 2, 8, 1};
+      for (int bd : bands) {
+        const size_t sm = h->prec == 32 ? rows_smem_bytes<float>(gg, h->px.p, bd)
+                                        : rows_smem_bytes<double>(gg, h->px.p, bd);
+        if (sm > (size_t)optin || bd > 60) continue;
+        int per_sm = 0;
+        cudaError_t e = h->prec == 32 ? rows_prepare<float>(gg, h->px.p, bd, &per_sm)
+                                      : rows_prepare<double>(gg, h->px.p, bd, &per_sm);
+        if (e == cudaSuccess && per_sm >= 1) b->row_bands.push_back(bd);
+      }
+      cudaGetLastError();
+    }
+    // the row kernel path on request; the autotuner may pick it as well
+    if (cfgs[0].sweep_engine == MMC_ENGINE_FUSED) {
+      if (b->row_bands.empty()) {
+        batch_free(b);
+        return fail(MMC_ERR_UNSUPPORTED,
+                    "the row-kernel batch path needs films (nz = 1) with demag, two colours and 16-byte rows");
+      }
+      b->rows_band = b->row_bands[0];
+    }
+  }
   b->cfgs.assign(cfgs, cfgs + R);
   for (int r = 0; r < R; ++r) {
     b->seeds.push_back(cfgs[r].randomseed < 0 ? (long long)std::time(nullptr) + r : cfgs[r].randomseed);
@@ -1210,6 +1413,7 @@ int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out
   if ((st = alloc(&b->m, (size_t)R * 3 * g.n * ts)) != MMC_OK) return bail(st);
   if ((st = alloc(&b->h, (size_t)R * 3 * g.n * ts)) != MMC_OK) return bail(st);
   if (h->cfg.cal_demag_flag && (st = alloc(&b->spec, (size_t)R * 3 * g.nspec * cs)) != MMC_OK) return bail(st);
+  if (b->rows_band > 0 && (st = batch_alloc_rows(b)) != MMC_OK) return bail(st);
   if ((st = alloc(&b->coef, R * sizeof(McCoef<double>))) != MMC_OK) return bail(st);
   if ((st = alloc((void**)&b->ecoef, R * sizeof(EnCoef))) != MMC_OK) return bail(st);
   if ((st = alloc((void**)&b->partials, (size_t)R * h->npartials * NQ * sizeof(double))) != MMC_OK) return bail(st);
@@ -1609,7 +1813,22 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
   for (auto& e : ev) CU(cudaEventCreate(&e));
   double acc[4] = {0, 0, 0, 0};
   int status = MMC_OK;
-  for (long long s = 0; s < nsweeps && status == MMC_OK; ++s) {
+  if (b->rows_band > 0) {
+    // film sweeps: [0] row kernel, [1] column pass
+    cudaError_t e = batch_demag(b);
+    for (long long s = 0; s < nsweeps && e == cudaSuccess; ++s) {
+      e = batch_sweep_rows(b, (int)(s & 1), ev);
+      if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
+      float x = 0, y = 0;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&x, ev[0], ev[1]);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&y, ev[1], ev[2]);
+      acc[0] += x;
+      acc[1] += y;
+    }
+    if (e == cudaSuccess && (nsweeps & 1)) e = batch_rows_settle(b);
+    if (e != cudaSuccess) status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
+  }
+  for (long long s = 0; b->rows_band == 0 && s < nsweeps && status == MMC_OK; ++s) {
     cudaError_t e = batch_sweep(b, ev);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
     for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
@@ -1628,8 +1847,16 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
   return MMC_OK;
 }
 
-int mmc_batch_launch_shape(mmc_batch* b, int out[5]) {
+int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int* candidates) {
+  if (!b) return fail(MMC_ERR_INVALID, "null batch");
+  if (sweeps < 1 || sweeps > 100000) return fail(MMC_ERR_INVALID, "sweeps must be in [1, 100000]");
+  TRY(set_dev(b->base));
+  return batch_autotune(b, sweeps, best_ms_per_sweep, candidates);
+}
+
+int mmc_batch_launch_shape(mmc_batch* b, int out[6]) {
   if (!b || !out) return fail(MMC_ERR_INVALID, "null argument");
+  out[5] = b->rows_band;
   out[0] = b->tun.x_rows_per_cta;
   out[1] = b->tun.x_threads;
   out[2] = b->tun.col_tx;

@@ -169,6 +169,7 @@ def lib(path=None):
         "mmc_batch_profile_sweeps": (ctypes.c_int, [H, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong,
                                                     _dp]),
         "mmc_batch_launch_shape": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int)]),
+        "mmc_batch_autotune": (ctypes.c_int, [H, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_int)]),
         "mmc_batch_request_stop": (None, [H]),
         "mmc_batch_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
         "mmc_batch_set_m": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
@@ -420,8 +421,16 @@ class Batch:
         check(lib().mmc_batch_profile_sweeps(self.h, stage, sweep0, nsweeps, dptr(out)))
         return out
 
+    def autotune(self, sweeps=8):
+        """Times every launch shape for `sweeps` sweeps, keeps the fastest;
+        returns (best ms per sweep, candidates tried)."""
+        ms = ctypes.c_double()
+        n = ctypes.c_int()
+        check(lib().mmc_batch_autotune(self.h, int(sweeps), ctypes.byref(ms), ctypes.byref(n)))
+        return ms.value, n.value
+
     def launch_shape(self):
-        out = (ctypes.c_int * 5)()
+        out = (ctypes.c_int * 6)()
         check(lib().mmc_batch_launch_shape(self.h, out))
         return tuple(out)
 

@@ -33,6 +33,50 @@ def test_batch_replicas_equal_single_runs(M, prec, geom):
         assert o.e_total == pytest.approx(obs[r].e_total, rel=1e-12 if prec == 64 else 1e-6)
 
 
+@pytest.mark.parametrize("prec", [32, 64])
+def test_batch_row_kernel_equals_pass_kernels(M, prec):
+    """Film batches run as row kernel + column pass; more CTAs than fit on the
+    device at once, so bands read halo rows written by earlier waves unless the
+    two copies of m and the spectrum keep them apart.  Odd sweep counts end in
+    the second copy and are moved back."""
+    kw = dict(nx=128, ny=128, pbc_x=2, pbc_y=2)
+    rows = cfgs_for(M, 12, prec, sweep_engine=2, **kw)
+    plain = cfgs_for(M, 12, prec, sweep_engine=1, **kw)
+    with M.Batch(rows) as a, M.Batch(plain) as b:
+        assert a.launch_shape()[5] > 0 and b.launch_shape()[5] == 0
+        # a smaller lattice created later must not lower the first one's
+        # shared-memory limit
+        with M.Batch(cfgs_for(M, 2, prec, sweep_engine=2, nx=16, ny=8)) as small:
+            small.run_sweeps(1, 0, 3)
+        for s0, n in ((0, 33), (33, 64), (97, 1)):
+            a.run_sweeps(1, s0, n)
+            b.run_sweeps(1, s0, n)
+        for r in range(12):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        ea, eb = a.energy(), b.energy()
+        assert [o.accepted for o in ea] == [o.accepted for o in eb]
+
+
+@pytest.mark.parametrize("geom", [dict(nx=64, ny=48, pbc_x=2, pbc_y=2), dict(nx=12, ny=10, nz=3, pbc_x=0, pbc_y=0)])
+def test_batch_autotune_keeps_state_and_results(M, geom):
+    """The autotuner runs sweeps with every launch shape, then restores m and
+    the counters: a tuned batch continues exactly as an untuned one."""
+    cfgs = cfgs_for(M, 5, 32, **geom)
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        a.run_sweeps(0, 0, 5)
+        b.run_sweeps(0, 0, 5)
+        m0 = [a.get_m(r) for r in range(5)]
+        ms, n = a.autotune(4)
+        assert ms > 0 and n >= 2
+        for r in range(5):
+            assert np.array_equal(a.get_m(r), m0[r])
+        a.run_sweeps(0, 5, 41)
+        b.run_sweeps(0, 5, 41)
+        for r in range(5):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), (r, a.launch_shape())
+        assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
+
+
 def test_batch_temperatures_and_chunking(M):
     cfgs = cfgs_for(M, 4, 32)
     with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
