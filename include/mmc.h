@@ -177,6 +177,37 @@ int mmc_compute_demag(mmc_handle* h);
 int mmc_demag_scratch_bytes(mmc_handle* h, size_t* bytes);
 int mmc_demag_apply(mmc_handle* h, const void* mdev, void* hdev, void* scratch, size_t scratch_bytes,
                     void* stream);
+/* Size of the device array behind mmc_demag_apply_static(): 16 MiB, enough
+ * for the spectrum of any lattice with 3 * nspec * 2 * sizeof(real) at most
+ * this size (a 1024 x 1024 periodic film in FP32, 512 x 512 open in FP64). */
+#define MMC_DEMAG_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
+/* mmc_demag_apply() for callers that cannot allocate device memory at the
+ * point of the call: code that runs inside a device-memory budget owned by
+ * another allocator (a framework's caching pool that has claimed the free
+ * memory), or a latency-bound loop where cudaMalloc/cudaFree would
+ * synchronise the device.  No counterpart in the reference, which keeps its
+ * FFT buffers for the whole run (src/main.cu:689-712, 744-755); this entry point and
+ * mmc_demag_apply share its transforms.
+ *
+ * The spectrum lives in a file-scope array of MMC_DEMAG_STATIC_SCRATCH_BYTES
+ * that the CUDA runtime reserves when it loads the library's module on a
+ * device; nothing is allocated per call, and the tensor is not built here.
+ * Rules:
+ *   - build the tensor first (mmc_build_demag or any field/run call): building
+ *     allocates, so an unbuilt tensor is MMC_ERR_STATE;
+ *   - lattices whose spectrum (mmc_demag_scratch_bytes) exceeds the array are
+ *     MMC_ERR_INVALID: use mmc_demag_apply with caller scratch;
+ *   - the first call on a device looks the array up (cudaGetSymbolAddress),
+ *     which may load the module there: make that first call before any stream
+ *     capture;
+ *   - every call on a device, from every handle, uses the same array: calls
+ *     that overlap in time (different streams, threads or handles without an
+ *     ordering between them) race on it; calls on one stream are ordered and
+ *     safe.  The array needs no initial contents: each call writes every value
+ *     it reads.
+ * mdev, hdev and stream are as for mmc_demag_apply (NULL stream = the
+ * handle's own stream); the work is enqueued, not waited for. */
+int mmc_demag_apply_static(mmc_handle* h, const void* mdev, void* hdev, void* stream);
 
 /* Per-term effective field in A/m for the current m, the DEBUG_H_FIELD dumps of
  * src/main.cu:965-1086.  MMC_TERM_DEMAG and MMC_TERM_TOTAL use the demag field

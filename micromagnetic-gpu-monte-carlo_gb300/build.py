@@ -37,6 +37,7 @@ UNITS = [
     ("kernels_f32.cu", ["-fmad=true"], "nvcc"),
     ("kernels_f64.cu", ["-fmad=false"], "nvcc"),
     ("newell.cu", ["-fmad=false"], "nvcc"),
+    ("demag_static.cu", [], "nvcc"),
     ("runtime.cpp", [], "g++"),
     ("ini.cpp", [], "g++"),
     ("ovf.cpp", [], "g++"),

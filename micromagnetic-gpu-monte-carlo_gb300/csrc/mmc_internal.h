@@ -167,6 +167,9 @@ template <typename T>
 cudaError_t launch_fused2d(const Geom& g, const FftPlan& px, const FftPlan& py, const FusedArgs<T>& a, int nblocks,
                            cudaStream_t st);
 size_t grid_barrier_bytes();
+// Address of the static spectrum array of mmc_demag_apply_static() on
+// `device` (the current device); looked up on the first call per device.
+cudaError_t demag_static_scratch(int device, void** out);
 
 // Batched film sweeps (fused2d.cuh / rows.cuh): the row kernel (inverse x
 // transform, both colours, forward x transform) and the 2-D column pass.

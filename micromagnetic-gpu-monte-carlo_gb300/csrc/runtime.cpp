@@ -1601,6 +1601,29 @@ int mmc_demag_apply(mmc_handle* h, const void* mdev, void* hdev, void* scratch, 
   return MMC_OK;
 }
 
+int mmc_demag_apply_static(mmc_handle* h, const void* mdev, void* hdev, void* stream) {
+  if (!h || !mdev || !hdev) return fail(MMC_ERR_INVALID, "null argument");
+  if (!h->cfg.cal_demag_flag) return fail(MMC_ERR_STATE, "cal_demag_flag is off");
+  const size_t need = 3 * (size_t)h->g.nspec * 2 * h->tsize;
+  if (need > (size_t)MMC_DEMAG_STATIC_SCRATCH_BYTES)
+    return fail(MMC_ERR_INVALID, "this lattice's spectrum needs " + std::to_string(need) +
+                                     " bytes, more than the static array's " +
+                                     std::to_string((size_t)MMC_DEMAG_STATIC_SCRATCH_BYTES) +
+                                     "; use mmc_demag_apply with caller scratch");
+  if (!h->demag_built)
+    return fail(MMC_ERR_STATE, "demag tensor not built: call mmc_build_demag first (building allocates)");
+  TRY(set_dev(h));
+  void* scratch = nullptr;
+  CU(demag_static_scratch(h->device, &scratch));
+  cudaStream_t st = stream ? (cudaStream_t)stream : h->st;
+  cudaError_t e = h->prec == 32 ? launch_demag<float>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const float*)mdev,
+                                                      (float*)hdev, scratch, h->khat, st)
+                                : launch_demag<double>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const double*)mdev,
+                                                       (double*)hdev, scratch, h->khat, st);
+  CU(e);
+  return MMC_OK;
+}
+
 int mmc_selftest_philox(int device, long long n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out,
                         uint32_t* out_curand) {
   if (n < 0 || (n > 0 && !ctr)) return fail(MMC_ERR_INVALID, "bad argument");

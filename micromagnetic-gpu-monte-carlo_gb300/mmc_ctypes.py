@@ -137,6 +137,7 @@ def lib(path=None):
         "mmc_demag_scratch_bytes": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_size_t)]),
         "mmc_demag_apply": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                            ctypes.c_void_p]),
+        "mmc_demag_apply_static": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
         "mmc_get_field": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
         "mmc_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
         "mmc_run_sweeps": (ctypes.c_int, [H, ctypes.c_double, ctypes.c_longlong, ctypes.c_longlong,
@@ -344,6 +345,11 @@ class Lattice:
 
     def demag_apply(self, mdev, hdev, scratch, scratch_bytes, stream=None):
         check(lib().mmc_demag_apply(self.h, mdev, hdev, scratch, scratch_bytes, stream))
+
+    def demag_apply_static(self, mdev, hdev, stream=None):
+        """mmc_demag_apply with the spectrum in the library's static device
+        array (no allocation; the tensor must be built already)."""
+        check(lib().mmc_demag_apply_static(self.h, mdev, hdev, stream))
 
 
 def header_functions(header=HEADER):
