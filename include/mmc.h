@@ -218,6 +218,27 @@ int mmc_get_field(mmc_handle* h, int term, double* hx, double* hy, double* hz);
  * src/effective_H.h:35-43, src/main.cu:902-956).  Recomputes the demag field
  * first.  Resets the acceptance counters. */
 int mmc_energy(mmc_handle* h, mmc_observables* out);
+/* Gradient of the total energy (the five terms of mmc_energy) with respect to
+ * m and to the material scalars -- the adjoint the reference does not have
+ * (its energy kernel, src/effective_H.h:35-43, computes values only).  The
+ * three components of every cell are treated as free variables:
+ * dE/dm_i = -mu0 Ms V H_i, with the demag part of H the convolution with the
+ * symmetrised tensor (K(r) + K(-r)) / 2 (spectrum Re K^), which is what the
+ * energy's derivative needs when periodic images make K slightly
+ * non-symmetric.  dE_dm: 3 n doubles (x block, y block, z block; x fastest
+ * within a block) or NULL.  dE_dparams: d/d(Aex, Dind, Ku1, Ms, Bextx, Bexty,
+ * Bextz) in SI units (J per J/m, J per J/m^2, J per J/m^3, J per A/m, J per T).
+ * Accumulated in FP64 from the working-precision m. */
+int mmc_grad(mmc_handle* h, double* dE_dm, double dE_dparams[7]);
+/* Energy minimisation from the current m: projected steepest descent on the
+ * unit sphere (direction P = t - (t.m) m with t = H / Ms, m renormalised every
+ * step) with alternating Barzilai-Borwein step lengths, until
+ * max_i |m_i x H_i| / Ms < torque_tol or max_iter updates.  H uses the
+ * symmetrised demag field, so P is the projected negative gradient of the
+ * energy.  iters receives the updates made, max_torque the last torque (either
+ * may be NULL); not reaching torque_tol is not an error -- check max_torque.
+ * No counterpart in the reference. */
+int mmc_relax(mmc_handle* h, double torque_tol, long long max_iter, long long* iters, double* max_torque);
 
 /* nsweeps Metropolis sweeps at `temperature` (mcKernel2, src/mc_sampling.h:27-41,
  * launched src/main.cu:1101-1120), each preceded by a demag refresh when

@@ -301,11 +301,15 @@ size_t fused2d_smem_bytes(const Geom& g, const FftPlan& px, const FftPlan& py, i
 // maximum once, not to one lattice's need: the attribute is per kernel and
 // process-wide, so a later, smaller lattice must not lower it under an
 // earlier one.
+// The opt-in maximum covers static and dynamic shared memory together.
 inline cudaError_t raise_smem_limit(const void* fn) {
   int dev = 0, optin = 48 * 1024;
+  cudaFuncAttributes fa{};
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, fn);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes);
   return e;
 }
 

@@ -142,7 +142,10 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
   }
 }
 
-enum : int { PASS_FWD = 1, PASS_MUL = 2, PASS_INV = 4 };
+// PASS_SYM (with PASS_MUL): multiply by the real part of K^ only, i.e. by the
+// spectrum of (K(r) + K(-r)) / 2 -- the symmetrised tensor of the energy's
+// adjoint.
+enum : int { PASS_FWD = 1, PASS_MUL = 2, PASS_INV = 4, PASS_SYM = 8 };
 
 // Complex FFT along a strided axis (y or z) of tiles of `tx` consecutive kx
 // columns.  Element (c, pos, col) lives at S[c*nspec + plane*plane_stride +
@@ -229,8 +232,9 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
       const int t = idx % ntx, pos = idx / ntx;
       const V* kk = ktile + (long long)pos * ntx + t;
       const long long ks = (long long)L * ntx;
-      const V kxx = kk[0], kxy = kk[ks], kxz = kk[2 * ks];
-      const V kyy = kk[3 * ks], kyz = kk[4 * ks], kzz = kk[5 * ks];
+      V kxx = kk[0], kxy = kk[ks], kxz = kk[2 * ks];
+      V kyy = kk[3 * ks], kyz = kk[4 * ks], kzz = kk[5 * ks];
+      if (flags & PASS_SYM) kxx.y = kxy.y = kxz.y = kyy.y = kyz.y = kzz.y = (T)0;
       V* px = cur + (long long)(0 * ntx + t) * stride + pos;
       V* py = cur + (long long)(1 * ntx + t) * stride + pos;
       V* pz = cur + (long long)(2 * ntx + t) * stride + pos;
@@ -508,65 +512,62 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// Per-cell terms of the energy reduction: q[0..4] the five energies with the
+// prefactors of e, q[5..7] m, q[8] (with_q) the solid angle of the two
+// triangles of the plaquette at (x, y).
 template <typename T>
-__global__ void __launch_bounds__(256) k_energy(Geom g, const EnCoef* __restrict__ ep, const T* __restrict__ m,
-                                                const T* __restrict__ h, double* __restrict__ partials) {
-  const EnCoef e = ep[blockIdx.z];
-  m += blockIdx.z * 3 * g.n;
-  if (h) h += blockIdx.z * 3 * g.n;
-  partials += (long long)blockIdx.z * gridDim.x * NQ;
-  __shared__ double red[NQ][8];
+__device__ __forceinline__ void energy_terms_at(const Geom& g, const EnCoef& e, const T* __restrict__ m,
+                                                const T* __restrict__ h, long long i, bool with_q, double q[NQ]) {
   const long long n = g.n;
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  double q[NQ];
-#pragma unroll
-  for (int k = 0; k < NQ; ++k) q[k] = 0;
-  if (i < n) {
-    const T* mx = m;
-    const T* my = m + n;
-    const T* mz = m + 2 * n;
-    const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
-    const double ax = mx[i], ay = my[i], az = mz[i];
-    for (int a = 0; a < 3; ++a) {
-      const long long j = nbr_idx(g, x, y, z, a, 1);
-      if (j < 0) continue;
-      const double ddx = (double)mx[j] - ax, ddy = (double)my[j] - ay, ddz = (double)mz[j] - az;
-      q[0] += e.aexV_d2[a] * (ddx * ddx + ddy * ddy + ddz * ddz);
-    }
-    const long long xp = nbr_idx(g, x, y, z, 0, 1), xm = nbr_idx(g, x, y, z, 0, -1);
-    const long long yp = nbr_idx(g, x, y, z, 1, 1), ym = nbr_idx(g, x, y, z, 1, -1);
-    const double dxmz = (xp >= 0 ? (double)mz[xp] : 0.0) - (xm >= 0 ? (double)mz[xm] : 0.0);
-    const double dxmx = (xp >= 0 ? (double)mx[xp] : 0.0) - (xm >= 0 ? (double)mx[xm] : 0.0);
-    const double dymz = (yp >= 0 ? (double)mz[yp] : 0.0) - (ym >= 0 ? (double)mz[ym] : 0.0);
-    const double dymy = (yp >= 0 ? (double)my[yp] : 0.0) - (ym >= 0 ? (double)my[ym] : 0.0);
-    q[1] = -(ax * e.dV_2d[0] * dxmz + ay * e.dV_2d[1] * dymz - az * (e.dV_2d[0] * dxmx + e.dV_2d[1] * dymy));
-    const double mu = ax * e.u[0] + ay * e.u[1] + az * e.u[2];
-    q[2] = -e.kuV * mu * mu;
-    q[3] = -(ax * e.msVB[0] + ay * e.msVB[1] + az * e.msVB[2]);
-    if (e.demag != 0.0 && h)
-      q[4] = -e.demag * (ax * (double)h[i] + ay * (double)h[n + i] + az * (double)h[2 * n + i]);
-    q[5] = ax;
-    q[6] = ay;
-    q[7] = az;
-    const long long i2 = nbr_idx(g, x, y, z, 0, 1);
-    const long long i4 = nbr_idx(g, x, y, z, 1, 1);
-    if (i2 >= 0 && i4 >= 0) {
-      const int x2 = (int)(i2 % g.nx);
-      const long long i3 = nbr_idx(g, x2, y, z, 1, 1);
-      const long long tri[2][3] = {{i, i2, i3}, {i, i3, i4}};
-      for (int t = 0; t < 2; ++t) {
-        const long long a = tri[t][0], b = tri[t][1], cc = tri[t][2];
-        const double pax = mx[a], pay = my[a], paz = mz[a];
-        const double pbx = mx[b], pby = my[b], pbz = mz[b];
-        const double pcx = mx[cc], pcy = my[cc], pcz = mz[cc];
-        const double trip =
-            pax * (pby * pcz - pbz * pcy) + pay * (pbz * pcx - pbx * pcz) + paz * (pbx * pcy - pby * pcx);
-        const double den = 1.0 + (pax * pbx + pay * pby + paz * pbz) + (pbx * pcx + pby * pcy + pbz * pcz) +
-                           (pcx * pax + pcy * pay + pcz * paz);
-        q[8] += 2.0 * atan2(trip, den);
-      }
+  const T* mx = m;
+  const T* my = m + n;
+  const T* mz = m + 2 * n;
+  const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
+  const double ax = mx[i], ay = my[i], az = mz[i];
+  for (int a = 0; a < 3; ++a) {
+    const long long j = nbr_idx(g, x, y, z, a, 1);
+    if (j < 0) continue;
+    const double ddx = (double)mx[j] - ax, ddy = (double)my[j] - ay, ddz = (double)mz[j] - az;
+    q[0] += e.aexV_d2[a] * (ddx * ddx + ddy * ddy + ddz * ddz);
+  }
+  const long long xp = nbr_idx(g, x, y, z, 0, 1), xm = nbr_idx(g, x, y, z, 0, -1);
+  const long long yp = nbr_idx(g, x, y, z, 1, 1), ym = nbr_idx(g, x, y, z, 1, -1);
+  const double dxmz = (xp >= 0 ? (double)mz[xp] : 0.0) - (xm >= 0 ? (double)mz[xm] : 0.0);
+  const double dxmx = (xp >= 0 ? (double)mx[xp] : 0.0) - (xm >= 0 ? (double)mx[xm] : 0.0);
+  const double dymz = (yp >= 0 ? (double)mz[yp] : 0.0) - (ym >= 0 ? (double)mz[ym] : 0.0);
+  const double dymy = (yp >= 0 ? (double)my[yp] : 0.0) - (ym >= 0 ? (double)my[ym] : 0.0);
+  q[1] = -(ax * e.dV_2d[0] * dxmz + ay * e.dV_2d[1] * dymz - az * (e.dV_2d[0] * dxmx + e.dV_2d[1] * dymy));
+  const double mu = ax * e.u[0] + ay * e.u[1] + az * e.u[2];
+  q[2] = -e.kuV * mu * mu;
+  q[3] = -(ax * e.msVB[0] + ay * e.msVB[1] + az * e.msVB[2]);
+  if (e.demag != 0.0 && h) q[4] = -e.demag * (ax * (double)h[i] + ay * (double)h[n + i] + az * (double)h[2 * n + i]);
+  q[5] = ax;
+  q[6] = ay;
+  q[7] = az;
+  if (!with_q) return;
+  const long long i2 = nbr_idx(g, x, y, z, 0, 1);
+  const long long i4 = nbr_idx(g, x, y, z, 1, 1);
+  if (i2 >= 0 && i4 >= 0) {
+    const int x2 = (int)(i2 % g.nx);
+    const long long i3 = nbr_idx(g, x2, y, z, 1, 1);
+    const long long tri[2][3] = {{i, i2, i3}, {i, i3, i4}};
+    for (int t = 0; t < 2; ++t) {
+      const long long a = tri[t][0], b = tri[t][1], cc = tri[t][2];
+      const double pax = mx[a], pay = my[a], paz = mz[a];
+      const double pbx = mx[b], pby = my[b], pbz = mz[b];
+      const double pcx = mx[cc], pcy = my[cc], pcz = mz[cc];
+      const double trip =
+          pax * (pby * pcz - pbz * pcy) + pay * (pbz * pcx - pbx * pcz) + paz * (pbx * pcy - pby * pcx);
+      const double den = 1.0 + (pax * pbx + pay * pby + paz * pbz) + (pbx * pcx + pby * pcy + pbz * pcz) +
+                         (pcx * pax + pcy * pay + pcz * paz);
+      q[8] += 2.0 * atan2(trip, den);
     }
   }
+}
+
+// Block sums of q[0..NQ) in a fixed order -> partials[blockIdx.x * NQ + k].
+__device__ __forceinline__ void block_sum_nq(const double q[NQ], double* __restrict__ partials) {
+  __shared__ double red[NQ][8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < NQ; ++k) {
@@ -579,6 +580,21 @@ __global__ void __launch_bounds__(256) k_energy(Geom g, const EnCoef* __restrict
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[threadIdx.x][w];
     partials[(long long)blockIdx.x * NQ + threadIdx.x] = s;
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_energy(Geom g, const EnCoef* __restrict__ ep, const T* __restrict__ m,
+                                                const T* __restrict__ h, double* __restrict__ partials) {
+  const EnCoef e = ep[blockIdx.z];
+  m += blockIdx.z * 3 * g.n;
+  if (h) h += blockIdx.z * 3 * g.n;
+  partials += (long long)blockIdx.z * gridDim.x * NQ;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double q[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) q[k] = 0;
+  if (i < g.n) energy_terms_at<T>(g, e, m, h, i, true, q);
+  block_sum_nq(q, partials);
 }
 
 static __global__ void __launch_bounds__(256) k_reduce_partials(const double* __restrict__ partials, int nblocks,
@@ -603,12 +619,11 @@ static __global__ void __launch_bounds__(256) k_reduce_partials(const double* __
 
 // =========================================================== effective field
 // Per-term H in A/m (the DEBUG_H_FIELD dumps of src/main.cu:965-1086).
+// H of one term (0-4) or of all (5) at cell i, A/m.
 template <typename T>
-__global__ void k_field(Geom g, HCoef c, int term, const T* __restrict__ m, const T* __restrict__ h,
-                        double* __restrict__ out) {
+__device__ __forceinline__ void field_at(const Geom& g, const HCoef& c, int term, const T* __restrict__ m,
+                                         const T* __restrict__ h, long long i, double f[3]) {
   const long long n = g.n;
-  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
   const T* mx = m;
   const T* my = m + n;
   const T* mz = m + 2 * n;
@@ -653,9 +668,23 @@ __global__ void k_field(Geom g, HCoef c, int term, const T* __restrict__ m, cons
     f1 += c.ms * (double)h[n + i];
     f2 += c.ms * (double)h[2 * n + i];
   }
-  out[i] = f0;
-  out[n + i] = f1;
-  out[2 * n + i] = f2;
+  f[0] = f0;
+  f[1] = f1;
+  f[2] = f2;
+}
+
+// Per-term H in A/m (the DEBUG_H_FIELD dumps of src/main.cu:965-1086).
+template <typename T>
+__global__ void k_field(Geom g, HCoef c, int term, const T* __restrict__ m, const T* __restrict__ h,
+                        double* __restrict__ out) {
+  const long long n = g.n;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double f[3];
+  field_at<T>(g, c, term, m, h, i, f);
+  out[i] = f[0];
+  out[n + i] = f[1];
+  out[2 * n + i] = f[2];
 }
 
 // =========================================================== init / utility
@@ -755,7 +784,7 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
 template <typename T>
 cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                        const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st,
-                       int nrep, cudaEvent_t* ev) {
+                       int nrep, cudaEvent_t* ev, int mul_flags = 0) {
   C<T>* S = reinterpret_cast<C<T>*>(spec);
   const C<T>* K = reinterpret_cast<const C<T>*>(khat);
   const long long ns = g.nspec;
@@ -768,13 +797,15 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
   if (ev) MMC_TRY(cudaEventRecord(ev[1], st));
   const long long ystride = g.hxp, yplane = (long long)g.nyp * g.hxp;
   if (g.nzp == 1) {
-    MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV,
-                            inv_n, tun.col_tx, tun.col_threads, st, nrep, sr));
+    MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny,
+                            PASS_FWD | PASS_MUL | PASS_INV | mul_flags, inv_n, tun.col_tx, tun.col_threads, st, nrep,
+                            sr));
   } else {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.ny, g.nyp, PASS_FWD, inv_n, tun.col_tx,
                             tun.col_threads, st, nrep, sr));
     MMC_TRY(run_col_pass<T>(pz, 3, S, ns, K, g.hx, g.nyp, ystride, yplane, g.nz, g.nz,
-                            PASS_FWD | PASS_MUL | PASS_INV, inv_n, tun.col_tx_z, tun.col_threads, st, nrep, sr));
+                            PASS_FWD | PASS_MUL | PASS_INV | mul_flags, inv_n, tun.col_tx_z, tun.col_threads, st, nrep,
+                            sr));
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.nyp, g.ny, PASS_INV, inv_n, tun.col_tx,
                             tun.col_threads, st, nrep, sr));
   }
@@ -840,6 +871,11 @@ cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, co
   return demag_impl<T>(g, px, py, pz, tun, m, h, spec, khat, st, nrep, ev);
 }
 template <typename T>
+cudaError_t launch_demag_sym(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
+                             const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st) {
+  return demag_impl<T>(g, px, py, pz, tun, m, h, spec, khat, st, 1, nullptr, PASS_SYM);
+}
+template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
                       unsigned long long* acc, cudaStream_t st, int nrep) {
   return mc_impl<T>(g, c, m, h, ctr, color, acc, st, nrep);
@@ -893,6 +929,8 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
   template cudaError_t launch_demag<T>(const Geom&, const FftPlan&, const FftPlan&, const FftPlan&,           \
                                        const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t, int, \
                                        cudaEvent_t*);                                                          \
+  template cudaError_t launch_demag_sym<T>(const Geom&, const FftPlan&, const FftPlan&, const FftPlan&,       \
+                                           const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t); \
   template cudaError_t launch_mc<T>(const Geom&, const McCoef<T>*, T*, const T*, const SweepCounters*, int,   \
                                     unsigned long long*, cudaStream_t, int);                                  \
   template cudaError_t launch_energy<T>(const Geom&, const EnCoef*, const T*, const T*, double*, int, double*, \

@@ -6,11 +6,13 @@
 
 #include "coef.h"
 #include "fused2d.cuh"
+#include "grad.cuh"
 #include "kernels.cuh"
 
 namespace mmc {
 MMC_INSTANTIATE_LAUNCHERS(double)
 MMC_INSTANTIATE_FUSED(double)
+MMC_INSTANTIATE_GRAD(double)
 
 int energy_partials_count(const Geom& g) { return energy_blocks(g); }
 

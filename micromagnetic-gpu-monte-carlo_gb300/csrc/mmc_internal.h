@@ -119,6 +119,22 @@ cudaError_t launch_field(const Geom& g, const HCoef& c, int term, const T* m, co
                          cudaStream_t st);
 template <typename T>
 cudaError_t launch_init(const Geom& g, uint64_t seed, T* m, cudaStream_t st);
+// Gradient and relaxation (grad.cuh).  launch_demag_sym convolves with the
+// symmetrised tensor (spectrum Re K^).  launch_grad writes dE/dm (3n doubles,
+// may be null) and 9 sums to out (see k_grad); launch_relax_eval writes
+// [s.s, s.y, y.y, max torque] to out.
+template <typename T>
+cudaError_t launch_demag_sym(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
+                             const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat, cudaStream_t st);
+template <typename T>
+cudaError_t launch_grad(const Geom& g, const HCoef& c, const EnCoef& eu, double gscale, const T* m, const T* hs,
+                        double* grad, double* partials, int npartials, double* out, cudaStream_t st);
+template <typename T>
+cudaError_t launch_relax_eval(const Geom& g, const HCoef& c, double inv_ms, const T* m, const T* hs, double* P,
+                              const double* s, bool first, double* partials, int npartials, double* out,
+                              cudaStream_t st);
+template <typename T>
+cudaError_t launch_relax_update(const Geom& g, T* m, const double* P, double tau, double* s, cudaStream_t st);
 // Raises the dynamic shared-memory limit of every pass kernel (once per device).
 template <typename T>
 cudaError_t launch_prepare(int max_dyn_smem);

@@ -241,6 +241,9 @@ struct mmc_handle {
   int fused_band = 0;
   int fused_blocks = 0;
   GridBarrier* bar = nullptr;
+  void* hsym = nullptr;      // 3n T, symmetrised demag field of the gradient (allocated on first use)
+  double* relax_p = nullptr;  // 3n doubles, relaxation direction
+  double* relax_s = nullptr;  // 3n doubles, last relaxation step
   void* m2 = nullptr;     // film engine: second copy of m (3n T)
   void* spec2 = nullptr;  // film engine: second spectrum (3*nspec complex T)
   int nsm = 0;
@@ -724,6 +727,98 @@ int set_m_impl(mmc_handle* h, const double* mx, const double* my, const double* 
   return MMC_OK;
 }
 
+// ------------------------------------------------------------ gradient
+// The demag field with the symmetrised tensor, into h->hsym.
+int demag_sym(mmc_handle* h) {
+  if (!h->hsym) CU(cudaMalloc(&h->hsym, 3 * (size_t)h->g.n * h->tsize));
+  CU(h->prec == 32 ? launch_demag_sym<float>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const float*)h->m,
+                                             (float*)h->hsym, h->spec, h->khat, h->st)
+                   : launch_demag_sym<double>(h->g, h->px.p, h->py.p, h->pz.p, h->tun, (const double*)h->m,
+                                              (double*)h->hsym, h->spec, h->khat, h->st));
+  return MMC_OK;
+}
+
+int grad_impl(mmc_handle* h, double* grad, double dparams[7]) {
+  TRY(ensure_demag(h));
+  const mmc_config& c = h->cfg;
+  const bool dm = c.cal_demag_flag != 0;
+  if (dm) TRY(demag_sym(h));
+  const HCoef k = make_h_coef(h);
+  // prefactors of the energy terms at unit Aex, Dind, Ku1 and d/dMs
+  EnCoef eu = make_en_coef(h);
+  const double V = c.dx * c.dy * c.dz;
+  const double d[3] = {c.dx, c.dy, c.dz};
+  const double mu0 = 4e-7 * pi_of(&c);
+  for (int a = 0; a < 3; ++a) eu.aexV_d2[a] = V / (d[a] * d[a]);
+  eu.dV_2d[0] = V / (2.0 * d[0]);
+  eu.dV_2d[1] = V / (2.0 * d[1]);
+  eu.kuV = V;
+  eu.msVB[0] = V * c.Bextx;
+  eu.msVB[1] = V * c.Bexty;
+  eu.msVB[2] = V * c.Bextz;
+  eu.demag = dm ? mu0 * c.ms * V : 0.0;
+  const double gscale = -mu0 * c.ms * V;
+  double* gdev = grad ? h->field64 : nullptr;
+  CU(h->prec == 32 ? launch_grad<float>(h->g, k, eu, gscale, (const float*)h->m, dm ? (const float*)h->hsym : nullptr,
+                                        gdev, h->partials, h->npartials, h->red, h->st)
+                   : launch_grad<double>(h->g, k, eu, gscale, (const double*)h->m,
+                                         dm ? (const double*)h->hsym : nullptr, gdev, h->partials, h->npartials,
+                                         h->red, h->st));
+  CU(cudaMemcpyAsync(h->red_host, h->red, NQ * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  if (grad) CU(cudaMemcpyAsync(grad, h->field64, 3 * (size_t)h->g.n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  TRY(sync_check(h));
+  const double* r = h->red_host;
+  dparams[0] = r[0];
+  dparams[1] = r[1];
+  dparams[2] = r[2];
+  dparams[3] = r[3] + r[4];
+  for (int a = 0; a < 3; ++a) dparams[4 + a] = -c.ms * V * r[5 + a];
+  return MMC_OK;
+}
+
+// Projected steepest descent with Barzilai-Borwein steps (see grad.cuh) until
+// max |m x H| / Ms < tol or max_iter updates.
+int relax_impl(mmc_handle* h, double tol, long long max_iter, long long* iters, double* torque) {
+  TRY(ensure_demag(h));
+  const size_t n3 = 3 * (size_t)h->g.n;
+  if (!h->relax_p) CU(cudaMalloc(&h->relax_p, n3 * sizeof(double)));
+  if (!h->relax_s) CU(cudaMalloc(&h->relax_s, n3 * sizeof(double)));
+  const bool dm = h->cfg.cal_demag_flag != 0;
+  const HCoef k = make_h_coef(h);
+  const double inv_ms = 1.0 / h->cfg.ms;
+  const double tau0 = 1e-3;
+  double tau = tau0, tq = 0;
+  long long it = 0;
+  for (;; ++it) {
+    if (h->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
+    if (dm) TRY(demag_sym(h));
+    CU(h->prec == 32 ? launch_relax_eval<float>(h->g, k, inv_ms, (const float*)h->m,
+                                                dm ? (const float*)h->hsym : nullptr, h->relax_p, h->relax_s,
+                                                it == 0, h->partials, h->npartials, h->red, h->st)
+                     : launch_relax_eval<double>(h->g, k, inv_ms, (const double*)h->m,
+                                                 dm ? (const double*)h->hsym : nullptr, h->relax_p, h->relax_s,
+                                                 it == 0, h->partials, h->npartials, h->red, h->st));
+    CU(cudaMemcpyAsync(h->red_host, h->red, 4 * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+    TRY(sync_check(h));
+    const double ss = h->red_host[0], sy = h->red_host[1], yy = h->red_host[2];
+    tq = h->red_host[3];
+    if (!std::isfinite(tq) || !std::isfinite(ss + sy + yy))
+      return fail(MMC_ERR_INVALID, "relaxation produced a non-finite torque");
+    if (tq < tol || it >= max_iter) break;
+    if (it > 0) {
+      // alternate the two Barzilai-Borwein step lengths; keep the last one
+      // when the curvature estimate is not positive
+      const double t = (it & 1) ? ss / sy : sy / yy;
+      if (std::isfinite(t) && t > 0) tau = t;
+    }
+    CU(h->prec == 32 ? launch_relax_update<float>(h->g, (float*)h->m, h->relax_p, tau, h->relax_s, h->st)
+                     : launch_relax_update<double>(h->g, (double*)h->m, h->relax_p, tau, h->relax_s, h->st));
+  }
+  if (iters) *iters = it;
+  if (torque) *torque = tq;
+  return MMC_OK;
+}
+
 int energy_impl(mmc_handle* h, mmc_observables* out) {
   TRY(ensure_demag(h));
   if (h->cfg.cal_demag_flag) CU(demag(h));
@@ -764,7 +859,8 @@ void destroy_impl(mmc_handle* h) {
   cudaSetDevice(h->device);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
   void* bufs[] = {h->m,   h->h,   h->spec,    h->khat,    h->coef,          h->partials,     h->red,
-                  h->acc, h->ctr, h->stage64, h->field64, (void*)h->bar, (void*)h->ecoef, h->m2, h->spec2};
+                  h->acc, h->ctr, h->stage64, h->field64, (void*)h->bar, (void*)h->ecoef, h->m2, h->spec2,
+                  h->hsym, h->relax_p, h->relax_s};
   for (void* b : bufs)
     if (b) cudaFree(b);
   if (h->red_host) cudaFreeHost(h->red_host);
@@ -1659,6 +1755,20 @@ int mmc_get_field(mmc_handle* h, int term, double* hx, double* hy, double* hz) {
   CU(cudaMemcpyAsync(hy, h->field64 + n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   CU(cudaMemcpyAsync(hz, h->field64 + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
   return sync_check(h);
+}
+
+int mmc_grad(mmc_handle* h, double* dE_dm, double dE_dparams[7]) {
+  if (!h || !dE_dparams) return fail(MMC_ERR_INVALID, "null argument");
+  TRY(set_dev(h));
+  return grad_impl(h, dE_dm, dE_dparams);
+}
+
+int mmc_relax(mmc_handle* h, double torque_tol, long long max_iter, long long* iters, double* max_torque) {
+  if (!h) return fail(MMC_ERR_INVALID, "null handle");
+  if (!(torque_tol > 0) || max_iter < 0) return fail(MMC_ERR_INVALID, "torque_tol must be > 0, max_iter >= 0");
+  TRY(set_dev(h));
+  h->stop.store(0);
+  return relax_impl(h, torque_tol, max_iter, iters, max_torque);
 }
 
 int mmc_energy(mmc_handle* h, mmc_observables* out) {

@@ -138,6 +138,9 @@ def lib(path=None):
         "mmc_demag_apply": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                            ctypes.c_void_p]),
         "mmc_demag_apply_static": (ctypes.c_int, [H, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+        "mmc_grad": (ctypes.c_int, [H, _dp, _dp]),
+        "mmc_relax": (ctypes.c_int, [H, ctypes.c_double, ctypes.c_longlong, ctypes.POINTER(ctypes.c_longlong),
+                                     _dp]),
         "mmc_get_field": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
         "mmc_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
         "mmc_run_sweeps": (ctypes.c_int, [H, ctypes.c_double, ctypes.c_longlong, ctypes.c_longlong,
@@ -345,6 +348,20 @@ class Lattice:
 
     def demag_apply(self, mdev, hdev, scratch, scratch_bytes, stream=None):
         check(lib().mmc_demag_apply(self.h, mdev, hdev, scratch, scratch_bytes, stream))
+
+    def grad(self, with_m=True):
+        """(dE/dm as float64 (3, n) or None, dE/d(Aex, Dind, Ku1, Ms, Bx, By, Bz))."""
+        g = np.zeros((3, self.n)) if with_m else None
+        dp = np.zeros(7)
+        check(lib().mmc_grad(self.h, dptr(g) if with_m else None, dptr(dp)))
+        return g, dp
+
+    def relax(self, torque_tol=1e-6, max_iter=100000):
+        """Projected-gradient relaxation; returns (updates, final max torque)."""
+        it = ctypes.c_longlong()
+        tq = ctypes.c_double()
+        check(lib().mmc_relax(self.h, float(torque_tol), int(max_iter), ctypes.byref(it), ctypes.byref(tq)))
+        return it.value, tq.value
 
     def demag_apply_static(self, mdev, hdev, stream=None):
         """mmc_demag_apply with the spectrum in the library's static device

@@ -672,4 +672,59 @@ double orc_energy_total(const mmc_config* c, const double* m, const double* hd) 
   return o[0] + o[1] + o[2] + o[3] + o[4];
 }
 
+
+// Gradient of the total energy (orc_energy's five terms) with respect to m,
+// treating the three components of every cell as free variables, and with
+// respect to the scalars (Aex, Dind, Ku1, Ms, Bx, By, Bz).  The bilinear
+// exchange and DMI energies have symmetric operators and Zeeman/anisotropy are
+// local, so dE/dm_i = -mu0 Ms V H_i for those terms.  The demag energy
+// -mu0 Ms^2 V/2 sum m.(K*m) has gradient -mu0 Ms^2 V/2 (K*m + K'*m) with
+// K'(r) = K(-r); K' differs from K only through the far periodic image on even
+// axes, and both are convolved here.  grad: 3n doubles (may be NULL);
+// dparams: 7 doubles.
+int orc_grad(const mmc_config* c, const double* k6, const double* m, double* grad, double dparams[7]) {
+  Lat L = lat_of(c);
+  Params p = params_of(c);
+  const long n = L.n(), np = L.np();
+  std::vector<double> hs;
+  if (p.demag) {
+    if (!k6) return 1;
+    std::vector<double> h(3 * n), h2(3 * n), kr(6 * np);
+    // K'(x, y, z) = K(-x, -y, -z) on the padded grid
+    for (int z = 0; z < L.nzp; ++z)
+      for (int y = 0; y < L.nyp; ++y)
+        for (int x = 0; x < L.nxp; ++x) {
+          const long o = x + (long)L.nxp * (y + (long)L.nyp * z);
+          const long r = (L.nxp - x) % L.nxp + (long)L.nxp * ((L.nyp - y) % L.nyp + (long)L.nyp * ((L.nzp - z) % L.nzp));
+          for (int k = 0; k < 6; ++k) kr[k * np + o] = k6[k * np + r];
+        }
+    orc_demag_fft(c, k6, m, h.data());
+    orc_demag_fft(c, kr.data(), m, h2.data());
+    hs.resize(3 * n);
+    for (long i = 0; i < 3 * n; ++i) hs[i] = 0.5 * (h[i] + h2[i]);
+  }
+  if (grad) {
+    std::vector<double> H(3 * n);
+    orc_field(c, MMC_TERM_TOTAL, m, p.demag ? hs.data() : nullptr, H.data());
+    const double s = -p.mu0 * p.ms * p.V;
+    for (long i = 0; i < 3 * n; ++i) grad[i] = s * H[i];
+  }
+  // the energy is linear in Aex, Dind and Ku1: their derivatives are the
+  // energies at unit strength
+  mmc_config u = *c;
+  u.Aex = 1.0;
+  u.Dind = 1.0;
+  u.Ku1 = 1.0;
+  double eu[9], e[9];
+  orc_energy(&u, m, p.demag ? hs.data() : nullptr, eu);
+  orc_energy(c, m, p.demag ? hs.data() : nullptr, e);
+  dparams[0] = eu[0];
+  dparams[1] = eu[1];
+  dparams[2] = eu[2];
+  // Zeeman is linear and demag quadratic in Ms
+  dparams[3] = (e[3] + 2.0 * e[4]) / p.ms;
+  for (int k = 0; k < 3; ++k) dparams[4 + k] = -p.ms * p.V * e[5 + k] * (double)n;
+  return 0;
+}
+
 }  // extern "C"

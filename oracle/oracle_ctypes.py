@@ -55,6 +55,7 @@ def lib():
         "orc_demag_fft": (ctypes.c_int, [C, _dp, _dp, _dp]),
         "orc_field": (ctypes.c_int, [C, ctypes.c_int, _dp, _dp, _dp]),
         "orc_energy": (ctypes.c_int, [C, _dp, _dp, _dp]),
+        "orc_grad": (ctypes.c_int, [C, _dp, _dp, _dp, _dp]),
         "orc_sweeps": (ctypes.c_int, [C, _dp, ctypes.c_double, ctypes.c_longlong, ctypes.c_longlong,
                                       ctypes.c_longlong, _dp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int,
                                       ctypes.c_int]),
@@ -149,6 +150,16 @@ def energy(cfg, m, hd=None):
     hp = _p(np.ascontiguousarray(hd, dtype=np.float64)) if hd is not None else None
     lib().orc_energy(_c(cfg), _p(m), hp, _p(out))
     return out
+
+
+def grad(cfg, k6, m):
+    """(dE/dm as float64 (3, n), dE/d(Aex, Dind, Ku1, Ms, Bx, By, Bz))."""
+    m = np.ascontiguousarray(m, dtype=np.float64)
+    g = np.zeros_like(m)
+    dp = np.zeros(7)
+    kp = _p(np.ascontiguousarray(k6)) if k6 is not None else None
+    assert lib().orc_grad(_c(cfg), kp, _p(m), _p(g), _p(dp)) == 0
+    return g, dp
 
 
 def sweeps(cfg, k6, T, stage, sweep0, nsweeps, m, demag_mode=1, nthreads=0):

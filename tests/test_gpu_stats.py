@@ -1,0 +1,57 @@
+"""Full anneals over 32 seeds: FP32 bulk against FP64.
+
+The FP64 path makes the oracle's decisions bit for bit (test_gpu_parity), so
+32 FP64 anneals stand for 32 oracle anneals; 32 FP32 anneals must agree with
+them within statistical error in the final energy density, <m_z> and
+topological charge.  Workload: the 64x64x1 film with PBC 20 images, T from
+1400 K to 40 K by x0.90 per stage, 1000 sweeps per stage, seeds 1..32."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+MATERIAL = dict(nx=64, ny=64, nz=1, dx=1e-9, dy=1e-9, dz=0.8e-9, ms=1.6e6, Aex=16e-12, Dind=6e-3, Ku1=2e6,
+                anisUx=0, anisUy=0, anisUz=1, Bextx=0, Bexty=0, Bextz=0.3, pbc_x=20, pbc_y=20, pbc_z=0,
+                Temperature_start=1400.0, Temperature_end=40.0, Temperature_step=0.9, Temperature_use_exp=1,
+                circle_per_stage=1000)
+SEEDS = list(range(1, 33))
+
+
+def stage_temperatures():
+    """The stage loop's schedule (T *= step while T > T_end), in FP64."""
+    out, T = [], MATERIAL["Temperature_start"]
+    while T > MATERIAL["Temperature_end"]:
+        out.append(T)
+        T *= MATERIAL["Temperature_step"]
+    return out
+
+
+def anneal(M, prec, tmp):
+    cfgs = [M.Config.defaults(precision=prec, randomseed=s, **MATERIAL) for s in SEEDS]
+    with M.Batch(cfgs) as b:
+        b.build_demag(str(tmp))
+        for k, T in enumerate(stage_temperatures()):
+            b.set_temperatures(np.full(len(SEEDS), T))
+            b.run_sweeps(k, 0, MATERIAL["circle_per_stage"])
+        obs = b.energy()
+    n = MATERIAL["nx"] * MATERIAL["ny"]
+    V = MATERIAL["dx"] * MATERIAL["dy"] * MATERIAL["dz"]
+    e = np.array([o.e_total / (n * V) for o in obs])  # J/m^3
+    mz = np.array([o.m[2] for o in obs])
+    q = np.array([o.q for o in obs])
+    return e, mz, q
+
+
+def test_full_anneal_statistics_fp32_vs_fp64(M, tmp_path_factory):
+    tmp = tmp_path_factory.mktemp("tensor")
+    e32, mz32, q32 = anneal(M, 32, tmp)
+    e64, mz64, q64 = anneal(M, 64, tmp)
+    assert len(stage_temperatures()) == 34
+    for name, a, b in (("energy density", e32, e64), ("<m_z>", mz32, mz64), ("Q", q32, q64)):
+        se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+        diff = abs(a.mean() - b.mean())
+        print(f"{name}: fp32 {a.mean():.6g} +- {a.std(ddof=1):.3g}, fp64 {b.mean():.6g} +- {b.std(ddof=1):.3g}, "
+              f"|diff| / se = {diff / se if se > 0 else 0:.2f}")
+        assert diff <= 4 * se + 1e-12 * abs(b.mean()), name
+    # the annealed states are ordered: low energy, skyrmion / stripe mixture
+    assert e64.mean() < 0
