@@ -316,18 +316,40 @@ int mmc_batch_last_run_ms(mmc_batch* b, double* ms);
 int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps, double out_ms[5]);
 /* Launch shape of the batch's pass kernels: rows per CTA and threads of the x
  * passes, kx columns per tile of the y and z passes, threads of the column
- * passes, and the band of the film row kernel (0 when sweeps use one kernel
- * per pass). */
-int mmc_batch_launch_shape(mmc_batch* b, int out[6]);
+ * passes, the band of the film row kernel (0 when sweeps use one kernel per
+ * pass), and whether both Metropolis colours of a film sweep run as one tile
+ * launch (1) or one launch per colour (0). */
+int mmc_batch_launch_shape(mmc_batch* b, int out[7]);
 /* Autotuner: times each launch shape this batch can run with (the film row
  * kernel with each band that fits; the pass kernels with 1-16 rows per x-pass
- * CTA and 1-8 kx columns per column-pass tile) for `sweeps` sweeps from the
+ * CTA and 1-8 kx columns per column-pass tile, each with both Metropolis
+ * forms) for `sweeps` sweeps from the
  * current state, keeps the fastest and restores m and the acceptance
  * counters.  Every shape gives bit-identical results, so the choice changes
  * only the speed.  best_ms_per_sweep and candidates may be NULL.  No
  * counterpart in the reference, whose block shape is fixed in the source
  * (src/main.cu:275-286). */
 int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int* candidates);
+/* Sets the launch shape (the seven values of mmc_batch_launch_shape), e.g. one
+ * an earlier autotune chose.  Values outside the ranges the autotuner tries,
+ * or a row-kernel band that does not fit this batch, are rejected.  Results do
+ * not depend on the shape.  No counterpart in the reference. */
+int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[7]);
+
+/* Replica farms: batches of different lattice sizes advanced together.  One
+ * call runs nsweeps sweeps of every batch (each with its own temperatures,
+ * ladders and launch shape); the batches' graphs are enqueued in turn on their
+ * own streams so the GPU runs them concurrently.  The farm does not own the
+ * batches, which must live on one device; results equal separate
+ * mmc_batch_run_sweeps calls.  last_run_ms is host wall time of the whole
+ * call.  No counterpart in the reference, which runs one lattice per process
+ * (src/main.cu:97-105). */
+typedef struct mmc_farm mmc_farm;
+int mmc_farm_create(mmc_batch* const* batches, int nbatches, mmc_farm** out);
+void mmc_farm_destroy(mmc_farm* f);
+int mmc_farm_run_sweeps(mmc_farm* f, long long stage, long long sweep0, long long nsweeps);
+int mmc_farm_last_run_ms(mmc_farm* f, double* ms);
+void mmc_farm_request_stop(mmc_farm* f);
 void mmc_batch_request_stop(mmc_batch* b);
 /* Observables of every replica (out holds nrep entries). */
 int mmc_batch_energy(mmc_batch* b, mmc_observables* out);

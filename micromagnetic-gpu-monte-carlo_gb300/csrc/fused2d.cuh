@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(const __grid_const
     const int j = blockIdx.x + it * G;
     if (j >= lay.npairs) break;
     for (int idx = threadIdx.x; idx < 6 * Ly; idx += blockDim.x) {
-      const int cc = idx / Ly, ky = idx - cc * Ly;
+      const int cc = P.py.dn.div(idx), ky = idx - cc * Ly;
       for (int q = 0; q < 2 / ve; ++q)
         cp_async16(kres + (((size_t)it * 6 + cc) * Ly + ky) * 2 + q * ve,
                    P.K + cc * nspec + (long long)ky * hxp + 2 * j + q * ve);
@@ -181,14 +181,14 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(const __grid_const
       if (j >= lay.npairs) break;
       const int kx0 = 2 * j;
       for (int idx = threadIdx.x; idx < 3 * ny; idx += blockDim.x) {
-        const int cc = idx / ny, y = idx - cc * ny;
+        const int cc = g.dny.div(idx), y = idx - cc * ny;
         for (int q = 0; q < 2 / ve; ++q)
           cp_async16(colraw + ((size_t)cc * ny + y) * 2 + q * ve, S + cc * nspec + (long long)y * hxp + kx0 + q * ve);
       }
       const V* kp = kres + (size_t)it * 6 * Ly * 2;
       if (!lay.resident) {  // stream K^ into kres (room for one item)
         for (int idx = threadIdx.x; idx < 6 * Ly; idx += blockDim.x) {
-          const int cc = idx / Ly, ky = idx - cc * Ly;
+          const int cc = P.py.dn.div(idx), ky = idx - cc * Ly;
           for (int q = 0; q < 2 / ve; ++q)
             cp_async16(kres + ((size_t)cc * Ly + ky) * 2 + q * ve, P.K + cc * nspec + (long long)ky * hxp + kx0 + q * ve);
         }
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(const __grid_const
       if (it == 0) stamp(sw, 6);
       // lines (comp, t) of length Ly with stride Ly + 1
       for (int idx = threadIdx.x; idx < 6 * Ly; idx += blockDim.x) {
-        const int line = idx / Ly, pos = idx - line * Ly;
+        const int line = P.py.dn.div(idx), pos = idx - line * Ly;
         const int cc = line >> 1, t = line & 1;
         fa[(size_t)line * (Ly + 1) + pos] = pos < ny ? colraw[((size_t)cc * ny + pos) * 2 + t] : cmk<V>(0, 0);
       }
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(const __grid_const
       V* cur = fft_run<T, false>(fa, fb, 6, Ly + 1, P.py, twy);
       V* oth = cur == fa ? fb : fa;
       for (int idx = threadIdx.x; idx < 2 * Ly; idx += blockDim.x) {
-        const int t = idx / Ly, pos = idx - t * Ly;
+        const int t = P.py.dn.div(idx), pos = idx - t * Ly;
         const V* kk = kp + (size_t)pos * 2 + t;
         const size_t ks = (size_t)Ly * 2;
         const V kxx = kk[0], kxy = kk[ks], kxz = kk[2 * ks], kyy = kk[3 * ks], kyz = kk[4 * ks], kzz = kk[5 * ks];
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(const __grid_const
       __syncthreads();
       V* r = fft_run<T, true>(cur, oth, 6, Ly + 1, P.py, twy);
       for (int idx = threadIdx.x; idx < 3 * ny; idx += blockDim.x) {
-        const int cc = idx / ny, y = idx - cc * ny;
+        const int cc = g.dny.div(idx), y = idx - cc * ny;
         V* dst = S + cc * nspec + (long long)y * hxp + kx0;
         dst[0] = r[(size_t)(2 * cc) * (Ly + 1) + y];
         dst[1] = r[(size_t)(2 * cc + 1) * (Ly + 1) + y];

@@ -26,9 +26,10 @@ namespace mmc {
 
 // Real rows in[c][row][x] (x < xdata, zero up to p.n) -> S[c][z][y][kx], kx < hx.
 template <typename T>
-__global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrows, const T* __restrict__ in,
-                            long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
-                            int rows_per_cta, long long in_rstride, long long s_rstride) {
+__global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
+                            long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, FastDiv dhx,
+                            int pitch, int rows_per_cta, long long in_rstride, long long s_rstride) {
+  const int hx = (int)dhx.d, ydata = (int)dyd.d;
   using V = C<T>;
   in += blockIdx.z * in_rstride;  // replica of a batch
   S += blockIdx.z * s_rstride;
@@ -49,7 +50,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrow
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int idx = base + u * blockDim.x;
-      const int rr = idx / L, x = idx - rr * L;
+      const int rr = p.dn.div(idx), x = idx - rr * L;
       const bool ok = idx < total && x < xdata;
       const long long rbase = (long long)(row0 + rr) * xdata + x;
 #pragma unroll
@@ -59,7 +60,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrow
     for (int u = 0; u < 4; ++u) {
       const int idx = base + u * blockDim.x;
       if (idx < total) {
-        const int rr = idx / L, x = idx - rr * L;
+        const int rr = p.dn.div(idx), x = idx - rr * L;
 #pragma unroll
         for (int pr = 0; pr < 3; ++pr)
           if (pr < npairs) bufA[(long long)(rr * npairs + pr) * L + x] = cmk<V>(v[u][2 * pr], v[u][2 * pr + 1]);
@@ -69,14 +70,14 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrow
   __syncthreads();
   V* res = fft_run<T, false>(bufA, bufB, nr * npairs, L, p, tw);
   for (int idx = threadIdx.x; idx < nr * npairs * hx; idx += blockDim.x) {
-    const int k = idx % hx;
-    const int rest = idx / hx;
-    const int pr = rest % npairs, rr = rest / npairs;
+    const int rest = dhx.div(idx);
+    const int k = idx - rest * hx;
+    const int rr = npairs == 2 ? rest >> 1 : rest / npairs, pr = rest - rr * npairs;
     const V* line = res + (long long)(rr * npairs + pr) * L;
     const V A = line[k];
     const V B = line[k == 0 ? 0 : L - k];
     const int row = row0 + rr;
-    const int y = row % ydata, z = row / ydata;
+    const int z = dyd.div(row), y = row - z * ydata;
     const long long off = ((long long)z * nyp + y) * pitch + k;
     const int ca = 2 * pr, cb = 2 * pr + 1;
     S[ca * nspec + off] = cmk<V>((T)0.5 * (A.x + B.x), (T)0.5 * (A.y - B.y));
@@ -87,8 +88,9 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, int ydata, int nrow
 // Half spectra S[0..2][z][y][kx] -> real rows out[c][row][x], x < xout.
 template <typename T>
 __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
-                            int xout, int yout, int nrows, T* __restrict__ out, long long out_cstride,
+                            FastDiv dxo, FastDiv dyo, int nrows, T* __restrict__ out, long long out_cstride,
                             int rows_per_cta, long long s_rstride, long long out_rstride) {
+  const int xout = (int)dxo.d, yout = (int)dyo.d;
   using V = C<T>;
   S += blockIdx.z * s_rstride;
   out += blockIdx.z * out_rstride;
@@ -106,9 +108,9 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int idx = base0 + u * blockDim.x;
-      const int rr = idx / L, k = idx - rr * L;
+      const int rr = p.dn.div(idx), k = idx - rr * L;
       const int row = row0 + rr;
-      const int y = row % yout, z = row / yout;
+      const int z = dyo.div(row), y = row - z * yout;
       const long long base = ((long long)z * nyp + y) * pitch;
       const long long kk = k < hx ? k : L - k;
 #pragma unroll
@@ -118,7 +120,7 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
     for (int u = 0; u < 4; ++u) {
       const int idx = base0 + u * blockDim.x;
       if (idx < total) {
-        const int rr = idx / L, k = idx - rr * L;
+        const int rr = p.dn.div(idx), k = idx - rr * L;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           if (k >= hx) v[u][c].y = -v[u][c].y;
@@ -132,7 +134,7 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
   __syncthreads();
   V* res = fft_run<T, true>(bufA, bufB, nr * 2, L, p, tw);
   for (int idx = threadIdx.x; idx < nr * xout; idx += blockDim.x) {
-    const int rr = idx / xout, x = idx - rr * xout;
+    const int rr = dxo.div(idx), x = idx - rr * xout;
     const long long o = (long long)(row0 + rr) * xout + x;
     const V a = res[(long long)(rr * 2) * L + x];
     const V b = res[(long long)(rr * 2 + 1) * L + x];
@@ -174,12 +176,14 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
   // transform runs (16-byte copies when the tile rows are 16-byte aligned)
   const bool kasync = (flags & PASS_MUL) && (((long long)ntx * sizeof(V)) % 16 == 0) && ((kx0 * sizeof(V)) % 16 == 0) &&
                       ((plane_stride * sizeof(V)) % 16 == 0) && ((pos_stride * sizeof(V)) % 16 == 0);
+  const FastDiv dt((uint32_t)ntx);  // index arithmetic without run-time division
   if (flags & PASS_MUL) {
     const int per = (int)(ntx * sizeof(V) / 16);
     if (kasync) {
+      const FastDiv dper((uint32_t)per);
       for (int idx = threadIdx.x; idx < 6 * L * per; idx += blockDim.x) {
-        const int q = idx % per, rest = idx / per;
-        const int pos = rest % L, c = rest / L;
+        const int rest = dper.div(idx), q = idx - rest * per;
+        const int c = p.dn.div(rest), pos = rest - c * L;
         const int e = 16 / (int)sizeof(V);
         const unsigned sd = (unsigned)__cvta_generic_to_shared(ktile + ((long long)c * L + pos) * ntx + q * e);
         const V* src = khat + c * nspec + pbase + pos * pos_stride + q * e;
@@ -187,8 +191,8 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
       }
     } else {
       for (int idx = threadIdx.x; idx < 6 * L * ntx; idx += blockDim.x) {
-        const int t = idx % ntx, rest = idx / ntx;
-        const int pos = rest % L, c = rest / L;
+        const int rest = dt.div(idx), t = idx - rest * ntx;
+        const int c = p.dn.div(rest), pos = rest - c * L;
         ktile[((long long)c * L + pos) * ntx + t] = khat[c * nspec + pbase + pos * pos_stride + t];
       }
     }
@@ -199,18 +203,16 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int idx = base + u * blockDim.x;
-      const int t = idx % ntx;
-      const int rest = idx / ntx;
-      const int pos = rest % L, c = rest / L;
+      const int rest = dt.div(idx), t = idx - rest * ntx;
+      const int c = p.dn.div(rest), pos = rest - c * L;
       v[u] = (idx < total && pos < load_lim) ? S[c * nspec + pbase + pos * pos_stride + t] : cmk<V>(0, 0);
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int idx = base + u * blockDim.x;
       if (idx < total) {
-        const int t = idx % ntx;
-        const int rest = idx / ntx;
-        const int pos = rest % L, c = rest / L;
+        const int rest = dt.div(idx), t = idx - rest * ntx;
+        const int c = p.dn.div(rest), pos = rest - c * L;
         bufA[(long long)(c * ntx + t) * stride + pos] = v[u];
       }
     }
@@ -229,7 +231,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
     if (kasync) asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
     for (int idx = threadIdx.x; idx < L * ntx; idx += blockDim.x) {
-      const int t = idx % ntx, pos = idx / ntx;
+      const int pos = dt.div(idx), t = idx - pos * ntx;
       const V* kk = ktile + (long long)pos * ntx + t;
       const long long ks = (long long)L * ntx;
       V kxx = kk[0], kxy = kk[ks], kxz = kk[2 * ks];
@@ -259,10 +261,10 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
       cur = r;
     }
   }
+  const FastDiv dsl((uint32_t)store_lim);
   for (int idx = threadIdx.x; idx < ncomp * store_lim * ntx; idx += blockDim.x) {
-    const int t = idx % ntx;
-    const int rest = idx / ntx;
-    const int pos = rest % store_lim, c = rest / store_lim;
+    const int rest = dt.div(idx), t = idx - rest * ntx;
+    const int c = dsl.div(rest), pos = rest - c * store_lim;
     S[c * nspec + pbase + pos * pos_stride + t] = cur[(long long)(c * ntx + t) * stride + pos];
   }
 }
@@ -476,9 +478,9 @@ __global__ void __launch_bounds__(256, 4) k_mc_checker(Geom g, const McCoef<T>* 
   const long long nrows = (long long)g.ny * g.nz;
   bool accepted = false;
   if (t < nrows * hxc) {
-    const int row = (int)(t / hxc);
-    const int j = (int)(t - (long long)row * hxc);
-    const int y = row % g.ny, z = row / g.ny;
+    const int row = g.dhxc.div((int)t);
+    const int j = (int)t - row * hxc;
+    const int z = g.dny.div(row), y = row - z * g.ny;
     const int x = 2 * j + ((color + y + z) & 1);
     if (x < g.nx) accepted = mc_trial<T>(g, c, m, h, ctr->stage, ctr->sweep, x, y, z);
   }
@@ -500,6 +502,153 @@ __global__ void __launch_bounds__(256, 4) k_mc_general(Geom g, const McCoef<T>* 
     if (cell_color(g, x, y, z) == color) accepted = mc_trial<T>(g, c, m, h, ctr->stage, ctr->sweep, x, y, z);
   }
   count_accepts(accepted, acc);
+}
+
+// Both colours of a two-colour film sweep (nz = 1) in one launch.  A CTA owns
+// an MCT x MCT tile of one replica and holds, in shared memory, m on the tile
+// plus a 2-cell margin and h on the tile plus a 1-cell margin.  Colour 0 runs
+// on the tile and on the ring of cells next to it (without the corners): the
+// ring cells belong to neighbouring tiles, and this CTA repeats, bit for bit,
+// the decisions their owners make -- same inputs, same Philox counter -- so
+// that colour 1 on the tile sees exactly the colour-0 state of the two-launch
+// sweep.  Only tile cells are written back and counted.  Periodic axes must be
+// whole tiles and at least two tiles long, so the margin never wraps onto the
+// tile itself.
+constexpr int MCT = 32;
+
+// One 4- or 8-byte global -> shared copy through the async path (no register
+// round trip, so a thread can have many in flight).
+template <typename T>
+__device__ __forceinline__ void cp_async_elem(T* smem, const T* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+constexpr int MCT_B = MCT + 4;  // m box side
+constexpr int MCT_H = MCT + 2;  // h box side
+
+__host__ __device__ inline bool mc_tile_ok(const Geom& g) {
+  return g.nz == 1 && g.ncolors == 2 && (!g.per[0] || (g.nx % MCT == 0 && g.nx >= 2 * MCT)) &&
+         (!g.per[1] || (g.ny % MCT == 0 && g.ny >= 2 * MCT));
+}
+template <typename T>
+__host__ __device__ inline size_t mc_tile_smem() {
+  return (size_t)3 * (MCT_B * MCT_B + MCT_H * MCT_H) * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mc_tile(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m,
+                                                 const T* __restrict__ h, const SweepCounters* __restrict__ ctr,
+                                                 unsigned long long* acc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);  // [comp][by][bx], MCT_B^2 per component
+  T* sh = sm + 3 * MCT_B * MCT_B;           // [comp][hy][hx], MCT_H^2 per component
+  __shared__ int colx[MCT_B], rowy[MCT_B];  // box column / row -> lattice x / y, -1 outside an open edge
+  const McCoef<T> c = cp[blockIdx.z];
+  const long long n = g.n;
+  m += blockIdx.z * 3 * n;
+  h += blockIdx.z * 3 * n;
+  acc += blockIdx.z;
+  const uint32_t stage = ctr->stage, sweep = ctr->sweep;
+  const int x0 = blockIdx.x * MCT, y0 = blockIdx.y * MCT;
+  if (threadIdx.x < MCT_B) {
+    int v = x0 - 2 + (int)threadIdx.x;
+    if (v < 0 || v >= g.nx) v = g.per[0] ? (v + g.nx) % g.nx : -1;
+    colx[threadIdx.x] = v;
+    int w = y0 - 2 + (int)threadIdx.x;
+    if (w < 0 || w >= g.ny) w = g.per[1] ? (w + g.ny) % g.ny : -1;
+    rowy[threadIdx.x] = w;
+  }
+  __syncthreads();
+  constexpr int BB = MCT_B * MCT_B, HH = MCT_H * MCT_H;
+  // asynchronous element copies, all in flight at once; cells outside an open
+  // edge are zero
+  for (int idx = threadIdx.x; idx < 3 * BB; idx += blockDim.x) {
+    const int cc = idx / BB, r = idx - cc * BB, by = r / MCT_B, bx = r - by * MCT_B;
+    const int gx = colx[bx], gy = rowy[by];
+    if (gx >= 0 && gy >= 0)
+      cp_async_elem<T>(sm + idx, m + cc * n + (long long)gy * g.nx + gx);
+    else
+      sm[idx] = (T)0;
+  }
+  const bool with_h = c.cd != (T)0;
+  for (int idx = threadIdx.x; idx < 3 * HH; idx += blockDim.x) {
+    const int cc = idx / HH, r = idx - cc * HH, hy = r / MCT_H, hx = r - hy * MCT_H;
+    const int gx = colx[hx + 1], gy = rowy[hy + 1];
+    if (with_h && gx >= 0 && gy >= 0)
+      cp_async_elem<T>(sh + idx, h + cc * n + (long long)gy * g.nx + gx);
+    else
+      sh[idx] = (T)0;
+  }
+  asm volatile("cp.async.wait_all;" ::: "memory");
+  __syncthreads();
+  // one trial at box cell (bx, by); returns whether it was accepted
+  auto trial = [&](int bx, int by) -> bool {
+    const int gx = colx[bx], gy = rowy[by];
+    if (gx < 0 || gy < 0) return false;
+    Nbrs<T> nb;
+    T* own = sm + by * MCT_B + bx;
+#pragma unroll
+    for (int s = 0; s < 2; ++s) {
+      const int ex = bx + (s ? 1 : -1), ey = by + (s ? 1 : -1);
+      const bool okx = colx[ex] >= 0, oky = rowy[ey] >= 0;
+      nb.has[0][s] = okx;
+      nb.has[1][s] = oky;
+      nb.has[2][s] = false;
+      const T* px = okx ? sm + by * MCT_B + ex : own;
+      const T* py = oky ? sm + ey * MCT_B + bx : own;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        nb.v[0][s][k] = px[k * BB];
+        nb.v[1][s][k] = py[k * BB];
+        nb.v[2][s][k] = own[k * BB];
+      }
+    }
+    const T* hp = sh + (by - 1) * MCT_H + (bx - 1);
+    const Proposal<T> p = mc_propose<T>(c, (uint32_t)(gx + g.nx * gy), stage, sweep);
+    if (mc_accept<T>(c, nb, own[0], own[BB], own[2 * BB], hp[0], hp[HH], hp[2 * HH], p)) {
+      own[0] = p.x;
+      own[BB] = p.y;
+      own[2 * BB] = p.z;
+      return true;
+    }
+    return false;
+  };
+  // the colour of box cell (bx, by) is (bx + by) & 1: x0 - 2 and y0 - 2 are even
+  // and periodic axes have even length
+  unsigned int mine = 0;
+  // colour 0 on box rows 1 .. MCT + 2 (tile rows -1 .. MCT), box columns
+  // 1 .. MCT + 2, without the four corners
+  constexpr int HALF0 = (MCT + 2) / 2;
+  for (int idx = threadIdx.x; idx < (MCT + 2) * HALF0; idx += blockDim.x) {
+    const int by = 1 + idx / HALF0, k = idx - (by - 1) * HALF0;
+    const int bx = 1 + 2 * k + ((by + 1) & 1);
+    const bool edge_row = by == 1 || by == MCT + 2;
+    if (edge_row && (bx == 1 || bx == MCT + 2)) continue;
+    const bool acc_ok = trial(bx, by);
+    if (acc_ok && by >= 2 && by < MCT + 2 && bx >= 2 && bx < MCT + 2) ++mine;
+  }
+  __syncthreads();
+  // colour 1 on the tile
+  constexpr int HALF1 = MCT / 2;
+  for (int idx = threadIdx.x; idx < MCT * HALF1; idx += blockDim.x) {
+    const int by = 2 + idx / HALF1, k = idx - (by - 2) * HALF1;
+    const int bx = 2 + 2 * k + ((by + 1) & 1);
+    if (trial(bx, by)) ++mine;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 3 * MCT * MCT; idx += blockDim.x) {
+    const int cc = idx / (MCT * MCT), r = idx - cc * MCT * MCT, ty = r / MCT, tx = r - ty * MCT;
+    const int gx = colx[tx + 2], gy = rowy[ty + 2];
+    if (gx >= 0 && gy >= 0 && x0 + tx < g.nx && y0 + ty < g.ny)
+      m[cc * n + (long long)gy * g.nx + gx] = sm[cc * BB + (ty + 2) * MCT_B + tx + 2];
+  }
+  unsigned int v = mine;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, (unsigned long long)v);
 }
 
 // =========================================================== energy
@@ -747,6 +896,8 @@ cudaError_t prepare_impl(int max_dyn_smem) {
                                     max_dyn_smem));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_col_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     max_dyn_smem));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)mc_tile_smem<T>()));
   return cudaSuccess;
 }
 
@@ -758,8 +909,8 @@ cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int
   const int lines = (ncomp + 1) / 2;
   size_t sm = x_pass_smem(p, lines, rpc, sizeof(C<T>));
   dim3 grid((nrows + rpc - 1) / rpc, 1, nrep);
-  k_x_forward<T><<<grid, threads, sm, st>>>(p, ncomp, xdata, ydata, nrows, in, in_cstride, S, nspec, nyp, hx, pitch,
-                                            rpc, in_rstride, s_rstride);
+  k_x_forward<T><<<grid, threads, sm, st>>>(p, ncomp, xdata, FastDiv((uint32_t)ydata), nrows, in, in_cstride, S, nspec,
+                                            nyp, FastDiv((uint32_t)hx), pitch, rpc, in_rstride, s_rstride);
   return cudaGetLastError();
 }
 
@@ -813,8 +964,8 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
   const int rpc = tun.x_rows_per_cta;
   size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
   dim3 grid((rows + rpc - 1) / rpc, 1, nrep);
-  k_x_inverse<T><<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.nx, g.ny, rows, h, g.n, rpc, sr,
-                                                  mr);
+  k_x_inverse<T><<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx, g.dny, rows, h, g.n, rpc,
+                                                  sr, mr);
   MMC_TRY(cudaGetLastError());
   if (ev) MMC_TRY(cudaEventRecord(ev[3], st));
   return cudaSuccess;
@@ -822,8 +973,17 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
 
 template <typename T>
 cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
-                    unsigned long long* acc, cudaStream_t st, int nrep) {
+                    unsigned long long* acc, cudaStream_t st, int nrep, int tile) {
   const int threads = 256;
+  if (color < 0) {  // every colour: one tile launch for films (tile != 0), else one launch per colour
+    if (tile && mc_tile_ok(g)) {
+      dim3 grid((unsigned)((g.nx + MCT - 1) / MCT), (unsigned)((g.ny + MCT - 1) / MCT), nrep);
+      k_mc_tile<T><<<grid, threads, mc_tile_smem<T>(), st>>>(g, c, m, h, ctr, acc);
+      return cudaGetLastError();
+    }
+    for (int col = 0; col < g.ncolors; ++col) MMC_TRY(mc_impl<T>(g, c, m, h, ctr, col, acc, st, nrep, 0));
+    return cudaSuccess;
+  }
   if (g.ncolors == 2) {
     const long long total = (long long)g.ny * g.nz * ((g.nx + 1) / 2);
     dim3 grid((unsigned)((total + threads - 1) / threads), 1, nrep);
@@ -877,8 +1037,8 @@ cudaError_t launch_demag_sym(const Geom& g, const FftPlan& px, const FftPlan& py
 }
 template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
-                      unsigned long long* acc, cudaStream_t st, int nrep) {
-  return mc_impl<T>(g, c, m, h, ctr, color, acc, st, nrep);
+                      unsigned long long* acc, cudaStream_t st, int nrep, int tile) {
+  return mc_impl<T>(g, c, m, h, ctr, color, acc, st, nrep, tile);
 }
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials, int npartials,
@@ -932,7 +1092,7 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
   template cudaError_t launch_demag_sym<T>(const Geom&, const FftPlan&, const FftPlan&, const FftPlan&,       \
                                            const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t); \
   template cudaError_t launch_mc<T>(const Geom&, const McCoef<T>*, T*, const T*, const SweepCounters*, int,   \
-                                    unsigned long long*, cudaStream_t, int);                                  \
+                                    unsigned long long*, cudaStream_t, int, int);                             \
   template cudaError_t launch_energy<T>(const Geom&, const EnCoef*, const T*, const T*, double*, int, double*, \
                                         cudaStream_t, int);                                                    \
   template cudaError_t launch_field<T>(const Geom&, const HCoef&, int, const T*, const T*, double*,            \

@@ -5,6 +5,31 @@
 
 namespace mmc {
 
+// Division by a run-time invariant d >= 1 as a multiply-high, an add and a
+// shift (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994): with l = ceil(log2 d) and
+// m = floor(2^32 (2^l - d) / d) + 1, n / d = (umulhi(m, n) + n) >> l for
+// 0 <= n < 2^31.  The kernels' index arithmetic divides by lattice and
+// transform sizes that are only known at run time.
+#ifdef __CUDACC__
+#define MMC_HD __host__ __device__
+#else
+#define MMC_HD
+#endif
+struct FastDiv {
+  uint32_t d = 1, m = 1, l = 0;
+  FastDiv() = default;
+  MMC_HD explicit FastDiv(uint32_t dd) : d(dd ? dd : 1) {
+    l = 0;
+    while ((1ull << l) < d) ++l;
+    m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
+  }
+#ifdef __CUDACC__
+  __device__ __forceinline__ int div(int n) const { return (int)((__umulhi(m, (uint32_t)n) + (uint32_t)n) >> l); }
+  __device__ __forceinline__ int mod(int n) const { return n - div(n) * (int)d; }
+#endif
+};
+
 constexpr int FFT_MAX_STAGES = 24;
 constexpr int FFT_MAX_RADIX = 31;  // largest prime factor an FFT length may have
 
@@ -26,6 +51,7 @@ struct FftPlan {
   // roots exp(-2 pi i j / n) at full_off.
   int warp_a, warp_b;
   int full_off;
+  FastDiv dn;  // n
   const double2* tw64;
   const float2* tw32;
 };
@@ -45,6 +71,7 @@ struct Geom {
   long long n;     // nx*ny*nz
   long long np;    // nxp*nyp*nzp
   long long nspec; // hxp*nyp*nzp
+  FastDiv dnx, dny, dhx, dhxc;  // nx, ny, hx, (nx + 1) / 2
 };
 
 // Metropolis coefficients, all in units of kT (see the sweep kernel).
@@ -91,6 +118,7 @@ struct DemagTuning {
   int col_tx;      // kx columns per tile in the y pass
   int col_tx_z;    // kx columns per tile in the z pass
   int col_threads;
+  int mc_tile;     // 1: both colours of a film sweep in one tile launch
 };
 
 // Device counters read by the sweep kernels: [stage, sweep].
@@ -108,9 +136,14 @@ template <typename T>
 cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                          const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat,
                          cudaStream_t st, int nrep = 1, cudaEvent_t* ev = nullptr);
+// color < 0: every colour of the sweep (films with tile != 0: one fused tile
+// launch, else one launch per colour).
 template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr,
-                      int color, unsigned long long* acc, cudaStream_t st, int nrep = 1);
+                      int color, unsigned long long* acc, cudaStream_t st, int nrep = 1, int tile = 0);
+// Whether a lattice can use the fused two-colour tile sweep, and its tile side.
+bool mc_tile_eligible(const Geom& g);
+constexpr int MC_TILE_SIDE = 32;
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials,
                           int npartials, double* out, cudaStream_t st, int nrep = 1);

@@ -108,22 +108,23 @@ __device__ __forceinline__ void row_load(const RowPhase<T>& R, const McCoef<T>& 
   const size_t mstride = 3 * (size_t)nx;
   const int elems = 16 / (int)sizeof(T), per_m = nx / elems;
   const int ve = 16 / (int)sizeof(V), per_s = hxp / ve;
+  const FastDiv d3m((uint32_t)(3 * per_m)), dm((uint32_t)per_m), d3s((uint32_t)(3 * per_s)), ds((uint32_t)per_s);
   for (int idx = threadIdx.x; idx < nslots * 3 * per_m; idx += blockDim.x) {
-    const int slot = idx / (3 * per_m), rem = idx - slot * 3 * per_m;
+    const int slot = d3m.div(idx), rem = idx - slot * 3 * per_m;
     const int r = R.rows[slot];
     if (r < 0) continue;
-    const int cc = rem / per_m, q = rem - cc * per_m;
+    const int cc = dm.div(rem), q = rem - cc * per_m;
     cp_async16(R.msm + (size_t)slot * mstride + (size_t)cc * nx + q * elems, R.m + cc * n + (long long)r * nx + q * elems);
   }
   for (int idx = threadIdx.x; idx < nwork * 3 * per_s; idx += blockDim.x) {
-    const int w = idx / (3 * per_s), rem = idx - w * 3 * per_s;
+    const int w = d3s.div(idx), rem = idx - w * 3 * per_s;
     const int r = R.rows[w + 1];
     if (r < 0) continue;
-    const int cc = rem / per_s, q = rem - cc * per_s;
+    const int cc = ds.div(rem), q = rem - cc * per_s;
     cp_async16(R.specraw + ((size_t)w * 3 + cc) * hxp + q * ve, R.S + cc * nspec + (long long)r * hxp + q * ve);
   }
   for (int idx = threadIdx.x; idx < (nwork + R.nb) * half; idx += blockDim.x) {
-    const int k = idx / half, j = idx - k * half;
+    const int k = R.g.dhxc.div(idx), j = idx - k * half;
     const int color = k < nwork ? 0 : 1;
     const int slot = color == 0 ? 1 + k : 2 + (k - nwork);
     const int y = R.rows[slot];
@@ -144,7 +145,7 @@ __device__ __forceinline__ void row_field(const RowPhase<T>& R) {
   const int nwork = R.nb + 2;
   const size_t mstride = 3 * (size_t)nx;
   for (int idx = threadIdx.x; idx < nwork * L; idx += blockDim.x) {
-    const int w = idx / L, k = idx - w * L;
+    const int w = R.px->dn.div(idx), k = idx - w * L;
     V A = cmk<V>(0, 0), B = cmk<V>(0, 0);
     if (R.rows[w + 1] >= 0) {
       const bool lo = k < hx;
@@ -166,7 +167,7 @@ __device__ __forceinline__ void row_field(const RowPhase<T>& R) {
   __syncthreads();
   V* res = fft_run<T, true>(R.fa, R.fb, 2 * nwork, L, *R.px, R.twx);
   for (int idx = threadIdx.x; idx < nwork * nx; idx += blockDim.x) {
-    const int w = idx / nx, x = idx - w * nx;
+    const int w = R.g.dnx.div(idx), x = idx - w * nx;
     const V a = res[(size_t)(2 * w) * L + x];
     const V b = res[(size_t)(2 * w + 1) * L + x];
     T* hr = R.hsm + (size_t)w * mstride;
@@ -189,7 +190,8 @@ __device__ __forceinline__ unsigned int row_sweep(const RowPhase<T>& R, const Mc
     const int kbase = color == 0 ? 0 : nwork;
     const int kcnt = color == 0 ? nwork : R.nb;
     for (int idx = threadIdx.x; idx < kcnt * half; idx += blockDim.x) {
-      const int k = kbase + idx / half, j = idx - (idx / half) * half;
+      const int kq = R.g.dhxc.div(idx);
+      const int k = kbase + kq, j = idx - kq * half;
       const int slot = color == 0 ? 1 + k : 2 + (k - nwork);
       const int y = R.rows[slot];
       if (y < 0) continue;
@@ -241,9 +243,10 @@ __device__ __forceinline__ void row_store(const RowPhase<T>& R, bool with_h) {
   const int nx = R.g.nx;
   const long long n = R.g.n;
   const size_t mstride = 3 * (size_t)nx;
+  const FastDiv dms((uint32_t)mstride);
   for (int idx = threadIdx.x; idx < R.nb * (int)mstride; idx += blockDim.x) {
-    const int rr = idx / (int)mstride, rem = idx - rr * (int)mstride;
-    const int cc = rem / nx, x = rem - cc * nx;
+    const int rr = dms.div(idx), rem = idx - rr * (int)mstride;
+    const int cc = R.g.dnx.div(rem), x = rem - cc * nx;
     const long long gi = cc * n + (long long)(R.y0 + rr) * nx + x;
     R.mo[gi] = R.msm[(size_t)(rr + 2) * mstride + rem];
     if (with_h) R.h[gi] = R.hsm[(size_t)(rr + 1) * mstride + rem];
@@ -258,7 +261,7 @@ __device__ __forceinline__ void row_forward(const RowPhase<T>& R) {
   const long long nspec = R.g.nspec;
   const size_t mstride = 3 * (size_t)nx;
   for (int idx = threadIdx.x; idx < R.nb * L; idx += blockDim.x) {
-    const int rr = idx / L, x = idx - rr * L;
+    const int rr = R.px->dn.div(idx), x = idx - rr * L;
     const T* row = R.msm + (size_t)(rr + 2) * mstride;
     V a = cmk<V>(0, 0), b = cmk<V>(0, 0);
     if (x < nx) {
@@ -271,7 +274,7 @@ __device__ __forceinline__ void row_forward(const RowPhase<T>& R) {
   __syncthreads();
   V* res = fft_run<T, false>(R.fa, R.fb, 2 * R.nb, L, *R.px, R.twx);
   for (int idx = threadIdx.x; idx < R.nb * hx; idx += blockDim.x) {
-    const int rr = idx / hx, k = idx - rr * hx;
+    const int rr = R.g.dhx.div(idx), k = idx - rr * hx;
     const V* la = res + (size_t)(2 * rr) * L;
     const V* lb = la + L;
     const int kn = k == 0 ? 0 : L - k;

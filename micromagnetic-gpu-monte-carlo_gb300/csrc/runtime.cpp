@@ -105,6 +105,7 @@ int make_plan(int n, PlanHost* ph) {
   // warp-level transform for power-of-two lengths up to 256: n = A * B
   p.warp_a = p.warp_b = 0;
   p.full_off = 0;
+  p.dn = FastDiv((uint32_t)n);
   const int wa[4][3] = {{256, 16, 16}, {128, 16, 8}, {64, 8, 8}, {32, 8, 4}};
   for (const auto& w : wa)
     if (n == w[0]) {
@@ -186,6 +187,10 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz);
   t.col_tx_z = pick(pz, g.nyp);
   t.col_threads = col_threads_for(g, py, pz, t.col_tx, t.col_tx_z);
+  // the fused two-colour sweep when there are enough tiles to fill the device
+  const long long tiles = (long long)((g.nx + MC_TILE_SIDE - 1) / MC_TILE_SIDE) *
+                          ((g.ny + MC_TILE_SIDE - 1) / MC_TILE_SIDE) * nrep;
+  t.mc_tile = mc_tile_eligible(g) && tiles >= 2LL * nsm ? 1 : 0;
   return t;
 }
 
@@ -356,9 +361,9 @@ cudaError_t demag(mmc_handle* h) {
 cudaError_t mc_color(mmc_handle* h, int color) {
   if (h->prec == 32)
     return launch_mc<float>(h->g, (const McCoef<float>*)h->coef, (float*)h->m, (const float*)h->h, h->ctr, color,
-                            h->acc, h->st);
+                            h->acc, h->st, 1, h->tun.mc_tile);
   return launch_mc<double>(h->g, (const McCoef<double>*)h->coef, (double*)h->m, (const double*)h->h, h->ctr, color,
-                           h->acc, h->st);
+                           h->acc, h->st, 1, h->tun.mc_tile);
 }
 
 // Enqueues one full sweep: demag refresh, every colour, counter advance.
@@ -368,10 +373,8 @@ cudaError_t enqueue_sweep(mmc_handle* h) {
     e = demag(h);
     if (e != cudaSuccess) return e;
   }
-  for (int c = 0; c < h->g.ncolors; ++c) {
-    e = mc_color(h, c);
-    if (e != cudaSuccess) return e;
-  }
+  e = mc_color(h, -1);
+  if (e != cudaSuccess) return e;
   return launch_advance(h->ctr, 1, h->st);
 }
 
@@ -552,7 +555,7 @@ int profile_sweeps_impl(mmc_handle* h, double T_K, long long stage, long long sw
     CU(cudaEventRecord(a, h->st));
     if (h->cfg.cal_demag_flag) CU(demag(h));
     CU(cudaEventRecord(b, h->st));
-    for (int col = 0; col < h->g.ncolors; ++col) CU(mc_color(h, col));
+    CU(mc_color(h, -1));
     CU(cudaEventRecord(c, h->st));
     CU(launch_advance(h->ctr, 1, h->st));
     CU(cudaEventSynchronize(c));
@@ -913,6 +916,10 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   g.n = (long long)g.nx * g.ny * g.nz;
   g.np = (long long)g.nxp * g.nyp * g.nzp;
   g.nspec = (long long)g.hxp * g.nyp * g.nzp;
+  g.dnx = FastDiv((uint32_t)g.nx);
+  g.dny = FastDiv((uint32_t)g.ny);
+  g.dhx = FastDiv((uint32_t)g.hx);
+  g.dhxc = FastDiv((uint32_t)((g.nx + 1) / 2));
   int st;
   if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(MMC_ERR_CUDA, "stream creation failed"));
@@ -1224,13 +1231,11 @@ cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
   mmc_handle* h = b->base;
   cudaError_t e;
   if (h->cfg.cal_demag_flag && (e = batch_demag(b, ev)) != cudaSuccess) return e;
-  for (int col = 0; col < h->g.ncolors; ++col) {
-    e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h,
-                                         b->ctr, col, b->acc, h->st, b->R)
-                      : launch_mc<double>(h->g, (const McCoef<double>*)b->coef, (double*)b->m,
-                                          (const double*)b->h, b->ctr, col, b->acc, h->st, b->R);
-    if (e != cudaSuccess) return e;
-  }
+  e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h, b->ctr,
+                                       -1, b->acc, h->st, b->R, b->tun.mc_tile)
+                    : launch_mc<double>(h->g, (const McCoef<double>*)b->coef, (double*)b->m, (const double*)b->h,
+                                        b->ctr, -1, b->acc, h->st, b->R, b->tun.mc_tile);
+  if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[4], h->st)) != cudaSuccess) return e;
   return launch_advance(b->ctr, 1, h->st);
 }
@@ -1295,7 +1300,16 @@ int batch_sync_temperatures(mmc_batch* b) {
   return MMC_OK;
 }
 
-int batch_run(mmc_batch* b, long long stage, long long sweep0, long long nsweeps) {
+// A run of nsweeps sweeps enqueued in pieces (a graph of 32 sweeps, or of one
+// swap interval followed by the swap pass), so that the pieces of several
+// batches can be interleaved on their own streams (mmc_farm_run_sweeps).
+struct BatchRun {
+  long long stage = 0, sweep0 = 0, nsweeps = 0, done = 0;
+  long long pieces = 0;
+};
+constexpr int BATCH_GRAPH_SWEEPS = 32;
+
+int batch_run_begin(mmc_batch* b, BatchRun& r, long long stage, long long sweep0, long long nsweeps) {
   mmc_handle* h = b->base;
   TRY(ensure_demag(h));
   TRY(batch_sync_temperatures(b));
@@ -1304,52 +1318,66 @@ int batch_run(mmc_batch* b, long long stage, long long sweep0, long long nsweeps
   CU(cudaMemcpy(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice));
   CU(cudaEventRecord(h->ev[0], h->st));
   if (b->rows_band > 0) CU(batch_demag(b));  // the row kernel starts from the spectrum of m
-  long long done = 0;
+  r = BatchRun{stage, sweep0, nsweeps, 0, 0};
+  if (b->interval == 0 && nsweeps >= BATCH_GRAPH_SWEEPS) TRY(batch_graph(b, BATCH_GRAPH_SWEEPS, false));
+  return MMC_OK;
+}
+
+int batch_run_piece(mmc_batch* b, BatchRun& r, bool* finished) {
+  mmc_handle* h = b->base;
   const int I = b->interval;
-  int launches = 0;
-  auto check_stop = [&]() -> int {
-    if (b->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
-    if (++launches % 64 == 0) CU(cudaStreamSynchronize(h->st));
-    return MMC_OK;
-  };
-  if (I > 0) {
-    // sweeps up to the next multiple of the swap interval, then a swap pass
-    while (done < nsweeps) {
-      const long long s = sweep0 + done;
+  if (r.done < r.nsweeps) {
+    if (I > 0) {
+      // sweeps up to the next multiple of the swap interval, then a swap pass
+      const long long s = r.sweep0 + r.done;
       const long long to_boundary = I - (s % I);
-      if (to_boundary <= nsweeps - done && to_boundary == I) {
+      if (to_boundary <= r.nsweeps - r.done && to_boundary == I) {
         TRY(batch_graph(b, I, true));
         CU(cudaGraphLaunch(b->gexec, h->st));
-        done += I;
+        r.done += I;
       } else {
-        const long long k = std::min(to_boundary, nsweeps - done);
+        const long long k = std::min(to_boundary, r.nsweeps - r.done);
         CU(batch_sweeps(b, k));
-        done += k;
+        r.done += k;
         if (k == to_boundary) {
           CU(batch_energy_kernels(b));
           CU(batch_swap(b));
         }
       }
-      TRY(check_stop());
-    }
-  } else {
-    const int G = 32;
-    if (nsweeps >= G) TRY(batch_graph(b, G, false));
-    while (nsweeps - done >= G) {
+    } else if (r.nsweeps - r.done >= BATCH_GRAPH_SWEEPS) {
       CU(cudaGraphLaunch(b->gexec, h->st));
-      done += G;
-      TRY(check_stop());
+      r.done += BATCH_GRAPH_SWEEPS;
+    } else {
+      CU(batch_sweeps(b, r.nsweeps - r.done));
+      r.done = r.nsweeps;
     }
-    CU(batch_sweeps(b, nsweeps - done));
-    done = nsweeps;
+    ++r.pieces;
   }
+  *finished = r.done >= r.nsweeps;
+  return MMC_OK;
+}
+
+int batch_run_end(mmc_batch* b, const BatchRun& r) {
+  mmc_handle* h = b->base;
   CU(cudaEventRecord(h->ev[1], h->st));
   CU(cudaStreamSynchronize(h->st));
   float ms = 0;
   CU(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
   b->last_ms = ms;
-  b->proposed += (unsigned long long)nsweeps * (unsigned long long)h->g.n;
+  b->proposed += (unsigned long long)r.nsweeps * (unsigned long long)h->g.n;
   return batch_sync_temperatures(b);
+}
+
+int batch_run(mmc_batch* b, long long stage, long long sweep0, long long nsweeps) {
+  BatchRun r;
+  TRY(batch_run_begin(b, r, stage, sweep0, nsweeps));
+  for (bool fin = false; !fin;) {
+    TRY(batch_run_piece(b, r, &fin));
+    if (b->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
+    // bound the queued work so that a stop request takes effect quickly
+    if (r.pieces % 64 == 0) CU(cudaStreamSynchronize(b->base->st));
+  }
+  return batch_run_end(b, r);
 }
 
 // Times every launch shape the batch can run with -- the row kernel with each
@@ -1386,6 +1414,16 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
         cands.push_back({0, t});
       }
     }
+  }
+  // the other Metropolis form for every pass-kernel shape
+  if (mc_tile_eligible(g)) {
+    const size_t nk = cands.size();
+    for (size_t i = 0; i < nk; ++i)
+      if (cands[i].rows_band == 0) {
+        Cand c2 = cands[i];
+        c2.tun.mc_tile = 1 - c2.tun.mc_tile;
+        cands.push_back(c2);
+      }
   }
   const size_t mbytes = (size_t)b->R * 3 * g.n * h->tsize;
   void* saved = nullptr;
@@ -1980,6 +2018,32 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
   return MMC_OK;
 }
 
+int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[7]) {
+  if (!b || !shape) return fail(MMC_ERR_INVALID, "null argument");
+  mmc_handle* h = b->base;
+  const Geom& g = h->g;
+  const size_t cs = 2 * h->tsize;
+  DemagTuning t{shape[0], shape[1], shape[2], shape[3], shape[4], shape[6]};
+  const int band = shape[5];
+  auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+  if (!pow2(t.x_rows_per_cta) || t.x_rows_per_cta > 16 || x_pass_smem(h->px.p, t.x_rows_per_cta, cs) > smem_limit() ||
+      !pow2(t.col_tx) || t.col_tx > 8 || col_pass_smem(h->py.p, t.col_tx, cs) > smem_limit() || !pow2(t.col_tx_z) ||
+      t.col_tx_z > 8 || col_pass_smem(h->pz.p, t.col_tx_z, cs) > smem_limit() ||
+      (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
+      t.col_threads % 32 != 0 || (t.mc_tile != 0 && t.mc_tile != 1) || (t.mc_tile && !mc_tile_eligible(g)))
+    return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
+  if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())
+    return fail(MMC_ERR_UNSUPPORTED, "row-kernel band not available for this batch");
+  TRY(set_dev(h));
+  if (band > 0) TRY(batch_alloc_rows(b));
+  b->tun = t;
+  b->rows_band = band;
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->graph_len = 0;
+  return MMC_OK;
+}
+
 int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int* candidates) {
   if (!b) return fail(MMC_ERR_INVALID, "null batch");
   if (sweeps < 1 || sweeps > 100000) return fail(MMC_ERR_INVALID, "sweeps must be in [1, 100000]");
@@ -1987,9 +2051,10 @@ int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int*
   return batch_autotune(b, sweeps, best_ms_per_sweep, candidates);
 }
 
-int mmc_batch_launch_shape(mmc_batch* b, int out[6]) {
+int mmc_batch_launch_shape(mmc_batch* b, int out[7]) {
   if (!b || !out) return fail(MMC_ERR_INVALID, "null argument");
   out[5] = b->rows_band;
+  out[6] = b->tun.mc_tile;
   out[0] = b->tun.x_rows_per_cta;
   out[1] = b->tun.x_threads;
   out[2] = b->tun.col_tx;
@@ -2002,6 +2067,76 @@ int mmc_batch_last_run_ms(mmc_batch* b, double* ms) {
   if (!b || !ms) return fail(MMC_ERR_INVALID, "null argument");
   *ms = b->last_ms;
   return MMC_OK;
+}
+
+// =================================================================== farms
+// Several batches (one per lattice size, say) advanced together: their pieces
+// are enqueued in turn on their own streams, so the GPU runs them
+// concurrently.  The farm does not own its batches.
+struct mmc_farm {
+  std::vector<mmc_batch*> batches;
+  double last_ms = 0;
+  std::atomic<int> stop{0};
+};
+
+int mmc_farm_create(mmc_batch* const* batches, int nbatches, mmc_farm** out) {
+  if (!batches || !out || nbatches < 1) return fail(MMC_ERR_INVALID, "need at least one batch");
+  *out = nullptr;
+  for (int i = 0; i < nbatches; ++i) {
+    if (!batches[i]) return fail(MMC_ERR_INVALID, "null batch");
+    if (batches[i]->base->device != batches[0]->base->device)
+      return fail(MMC_ERR_INVALID, "the batches of a farm must share one device");
+    for (int j = 0; j < i; ++j)
+      if (batches[j] == batches[i]) return fail(MMC_ERR_INVALID, "a batch appears twice");
+  }
+  mmc_farm* f = new mmc_farm();
+  f->batches.assign(batches, batches + nbatches);
+  *out = f;
+  return MMC_OK;
+}
+
+void mmc_farm_destroy(mmc_farm* f) { delete f; }
+
+int mmc_farm_run_sweeps(mmc_farm* f, long long stage, long long sweep0, long long nsweeps) {
+  if (!f) return fail(MMC_ERR_INVALID, "null farm");
+  if (nsweeps < 0 || stage < 0 || sweep0 < 0) return fail(MMC_ERR_INVALID, "negative counter");
+  TRY(set_dev(f->batches[0]->base));
+  f->stop.store(0);
+  const auto t0 = std::chrono::steady_clock::now();
+  const size_t nb = f->batches.size();
+  std::vector<BatchRun> runs(nb);
+  for (size_t i = 0; i < nb; ++i) {
+    f->batches[i]->stop.store(0);
+    TRY(batch_run_begin(f->batches[i], runs[i], stage, sweep0, nsweeps));
+  }
+  std::vector<char> fin(nb, 0);
+  for (long long round = 1;; ++round) {
+    bool all = true;
+    for (size_t i = 0; i < nb; ++i) {
+      if (fin[i]) continue;
+      bool done = false;
+      TRY(batch_run_piece(f->batches[i], runs[i], &done));
+      fin[i] = done;
+      all = all && done;
+    }
+    if (f->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
+    if (all) break;
+    if (round % 32 == 0)
+      for (size_t i = 0; i < nb; ++i) CU(cudaStreamSynchronize(f->batches[i]->base->st));
+  }
+  for (size_t i = 0; i < nb; ++i) TRY(batch_run_end(f->batches[i], runs[i]));
+  f->last_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  return MMC_OK;
+}
+
+int mmc_farm_last_run_ms(mmc_farm* f, double* ms) {
+  if (!f || !ms) return fail(MMC_ERR_INVALID, "null argument");
+  *ms = f->last_ms;
+  return MMC_OK;
+}
+
+void mmc_farm_request_stop(mmc_farm* f) {
+  if (f) f->stop.store(1);
 }
 
 void mmc_batch_request_stop(mmc_batch* b) {

@@ -174,6 +174,13 @@ def lib(path=None):
                                                     _dp]),
         "mmc_batch_launch_shape": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int)]),
         "mmc_batch_autotune": (ctypes.c_int, [H, ctypes.c_int, _dp, ctypes.POINTER(ctypes.c_int)]),
+        "mmc_batch_set_launch_shape": (ctypes.c_int, [H, ctypes.POINTER(ctypes.c_int)]),
+        "mmc_farm_create": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_void_p)]),
+        "mmc_farm_destroy": (None, [H]),
+        "mmc_farm_run_sweeps": (ctypes.c_int, [H, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong]),
+        "mmc_farm_last_run_ms": (ctypes.c_int, [H, _dp]),
+        "mmc_farm_request_stop": (None, [H]),
         "mmc_batch_request_stop": (None, [H]),
         "mmc_batch_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
         "mmc_batch_set_m": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
@@ -452,8 +459,12 @@ class Batch:
         check(lib().mmc_batch_autotune(self.h, int(sweeps), ctypes.byref(ms), ctypes.byref(n)))
         return ms.value, n.value
 
+    def set_launch_shape(self, shape):
+        arr = (ctypes.c_int * 7)(*[int(v) for v in shape])
+        check(lib().mmc_batch_set_launch_shape(self.h, arr))
+
     def launch_shape(self):
-        out = (ctypes.c_int * 6)()
+        out = (ctypes.c_int * 7)()
         check(lib().mmc_batch_launch_shape(self.h, out))
         return tuple(out)
 
@@ -470,3 +481,34 @@ class Batch:
         m = np.zeros((3, self.n))
         check(lib().mmc_batch_get_m(self.h, r, dptr(m[0]), dptr(m[1]), dptr(m[2])))
         return m
+
+
+class Farm:
+    """Batches of different lattice sizes advanced together (mmc_farm_*); the
+    batches stay owned by the caller."""
+
+    def __init__(self, batches):
+        self.batches = list(batches)
+        arr = (ctypes.c_void_p * len(self.batches))(*[b.h.value for b in self.batches])
+        h = ctypes.c_void_p()
+        check(lib().mmc_farm_create(arr, len(self.batches), ctypes.byref(h)))
+        self.h = h
+
+    def run_sweeps(self, stage, sweep0, nsweeps):
+        check(lib().mmc_farm_run_sweeps(self.h, stage, sweep0, nsweeps))
+
+    def last_run_ms(self):
+        v = ctypes.c_double()
+        check(lib().mmc_farm_last_run_ms(self.h, ctypes.byref(v)))
+        return v.value
+
+    def close(self):
+        if self.h:
+            lib().mmc_farm_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -77,6 +77,59 @@ def test_batch_autotune_keeps_state_and_results(M, geom):
         assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
 
 
+TILE_GEOMS = [dict(nx=64, ny=64, pbc_x=1, pbc_y=1), dict(nx=96, ny=41, pbc_x=1, pbc_y=0),
+              dict(nx=41, ny=23, pbc_x=0, pbc_y=0)]
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("geom", TILE_GEOMS)
+def test_mc_tile_bitwise_equals_colour_kernels(M, prec, geom):
+    """Both colours in one tile launch (ring of colour-0 cells recomputed)
+    against one launch per colour."""
+    cfgs = cfgs_for(M, 3, prec, sweep_engine=1, **geom)
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        sa, sb = list(a.launch_shape()), list(b.launch_shape())
+        sa[6], sb[6] = 0, 1
+        a.set_launch_shape(sa)
+        b.set_launch_shape(sb)
+        assert a.launch_shape()[6] == 0 and b.launch_shape()[6] == 1
+        for s0, n in ((0, 37), (37, 32)):
+            a.run_sweeps(3, s0, n)
+            b.run_sweeps(3, s0, n)
+        for r in range(3):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
+
+
+def test_mc_tile_fp64_decisions_match_oracle(M, O):
+    c = cfgs_for(M, 1, 64, sweep_engine=1, nx=64, ny=64, pbc_x=1, pbc_y=1)[0]
+    with M.Batch([c]) as b:
+        s = list(b.launch_shape())
+        s[6] = 1
+        b.set_launch_shape(s)
+        m0 = b.get_m(0)
+        b.run_sweeps(2, 0, 60)
+        got = b.get_m(0)
+        acc = b.energy()[0].accepted
+        k6 = None
+    with M.Lattice(c) as lat:
+        k6 = lat.tensor()
+    m = m0.copy()
+    want_acc = O.sweeps(c, k6, c.Temperature_start, 2, 0, 60, m, demag_mode=1)
+    assert acc == want_acc
+    assert np.array_equal(got, m)
+
+
+def test_mc_tile_rejected_where_ineligible(M):
+    # a 48-wide periodic axis is not a whole number of 32-cell tiles
+    with M.Batch(cfgs_for(M, 1, 32, nx=48, ny=64, pbc_x=1, pbc_y=1)) as b:
+        s = list(b.launch_shape())
+        assert s[6] == 0
+        s[6] = 1
+        with pytest.raises(M.MmcError):
+            b.set_launch_shape(s)
+
+
 def test_batch_temperatures_and_chunking(M):
     cfgs = cfgs_for(M, 4, 32)
     with M.Batch(cfgs) as a, M.Batch(cfgs) as b:

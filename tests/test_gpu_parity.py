@@ -31,6 +31,11 @@ GEOMS = {
     "odd_periodic": dict(nx=15, ny=7, nz=1, pbc_x=1, pbc_y=-1),
     "mixed_3d": dict(nx=9, ny=6, nz=3, pbc_x=1, pbc_y=0, pbc_z=1),
     "radix_7_5": dict(nx=7, ny=10, nz=2, pbc_x=2, pbc_y=1, pbc_z=0),
+    # pass kernels with the two-colour tile sweep: whole periodic tiles, and
+    # partial tiles on an open axis
+    "tile64_kernels": dict(nx=64, ny=64, pbc_x=1, pbc_y=1, sweep_engine=1),
+    "tile96x41_kernels": dict(nx=96, ny=41, pbc_x=1, pbc_y=0, sweep_engine=1),
+    "open12x10_kernels": dict(nx=12, ny=10, pbc_x=0, pbc_y=0, sweep_engine=1),
 }
 
 
@@ -133,7 +138,8 @@ def test_energy_and_observables(M, O, geom, prec):
 
 
 @pytest.mark.parametrize("demag", [0, 1])
-@pytest.mark.parametrize("geom", ["film16_pbc2", "odd_periodic", "mixed_3d"])
+@pytest.mark.parametrize("geom", ["film16_pbc2", "odd_periodic", "mixed_3d", "tile64_kernels", "tile96x41_kernels",
+                                  "open12x10_kernels"])
 def test_fp64_decisions_bitwise_100_sweeps(M, O, geom, demag):
     """FP64 accept/reject decisions identical to the oracle's for 100 sweeps:
     the final state (every spin is its initial vector or a Philox proposal) and
@@ -306,6 +312,8 @@ FILMS = {
     "ny3_open": dict(nx=20, ny=3, pbc_x=1, pbc_y=0),
     "ny1": dict(nx=12, ny=1, pbc_x=1, pbc_y=0),
     "rect_x96": dict(nx=96, ny=6, pbc_x=1, pbc_y=-1),
+    "tile64": dict(nx=64, ny=64, pbc_x=2, pbc_y=2),
+    "tile96x41": dict(nx=96, ny=41, pbc_x=1, pbc_y=0),
 }
 
 
