@@ -146,9 +146,15 @@ def dist_setup():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("gloo")
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
         return dist, rank, local, world
     return None, rank, local, world
+
+
+def replica_seeds(rank, R):
+    """Seeds of rank `rank`'s replicas: 256.. on rank 0, disjoint across ranks."""
+    return [256 + rank * R + r for r in range(R)]
 
 
 def reduce_max(dist, v):
@@ -229,7 +235,7 @@ def run_ours(args):
     os.makedirs(CACHE_DIR, exist_ok=True)
     R = args.batch
     S = args.sweeps
-    seeds = [256 + rank * R + r for r in range(R)]
+    seeds = replica_seeds(rank, R)
     cfgs = [M.Config.defaults(precision=32, **dict(WORKLOAD, randomseed=sd)) for sd in seeds]
     t0 = time.perf_counter()
     batch = M.Batch(cfgs, device=local)
@@ -392,7 +398,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--launch-shape", default="",
-                    help="six comma-separated values of a launch shape to use instead of autotuning")
+                    help="seven comma-separated values of a launch shape to use instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
