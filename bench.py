@@ -312,7 +312,7 @@ def run_ours(args):
         }
         fam = dict(zip(["k_rows", "k_col_pass"], prof[:2]))
     else:
-        mc = "k_mc_tile" if shape[6] else "k_mc_checker"  # one launch, or one per colour
+        mc = {1: "k_mc_tile", 2: "k_mc_quad"}.get(shape[6], "k_mc_checker")  # tile: one launch, else one per colour
         kbytes = {
             "k_x_forward": R * (3 * s_ * n + 3 * 2 * s_ * nh),
             "k_col_pass": R * 2 * (3 * 2 * s_ * nh) + 6 * 2 * s_ * nh,
@@ -321,7 +321,7 @@ def run_ours(args):
         }
         fam = dict(zip(["k_x_forward", "k_col_pass", "k_x_inverse", mc], prof[:4]))
     dom = max(fam, key=fam.get)
-    launches = 2 if dom == "k_mc_checker" else 1
+    launches = 2 if dom in ("k_mc_checker", "k_mc_quad") else 1
     per_launch_ms = fam[dom] / launches
     bytes_launch = kbytes[dom] / launches
     peak, peak_kind = measured_peaks()
@@ -365,7 +365,7 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": R * 3 * n * 8, "d2h_bytes_per_step": R * 3 * n * 8},
         "roofline": roofline,
         "clocks": clk.summary(),
-        "gpu_launches": args.steps * S * (3 if shape[5] > 0 else 5 if shape[6] else 6),
+        "gpu_launches": args.steps * S * (3 if shape[5] > 0 else 5 if shape[6] == 1 else 6),
         "single_lattice_fp32": {"value": single_v, "unit": UNIT, "engine": single_engine},
         "fp64_plain": fp64_line,
         "setup_s": setup_s,

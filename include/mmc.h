@@ -317,8 +317,9 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
 /* Launch shape of the batch's pass kernels: rows per CTA and threads of the x
  * passes, kx columns per tile of the y and z passes, threads of the column
  * passes, the band of the film row kernel (0 when sweeps use one kernel per
- * pass), and whether both Metropolis colours of a film sweep run as one tile
- * launch (1) or one launch per colour (0). */
+ * pass), and the Metropolis form: 0 one launch per colour, 1 both colours of
+ * a film in one tile launch, 2 one vectorised launch per colour (films with
+ * nx a multiple of 4). */
 int mmc_batch_launch_shape(mmc_batch* b, int out[7]);
 /* Autotuner: times each launch shape this batch can run with (the film row
  * kernel with each band that fits; the pass kernels with 1-16 rows per x-pass

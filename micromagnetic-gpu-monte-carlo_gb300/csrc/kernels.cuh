@@ -285,6 +285,21 @@ __device__ __forceinline__ long long nbr_idx(const Geom& g, int x, int y, int z,
   return c[0] + (long long)g.nx * (c[1] + (long long)g.ny * c[2]);
 }
 
+// nbr_idx from the cell's own index i: a step of +-stride, wrapped on a
+// periodic axis; the same result without rebuilding the index.
+__device__ __forceinline__ long long nbr_step(const Geom& g, long long i, int x, int y, int z, int axis, int dir) {
+  const int n = axis == 0 ? g.nx : axis == 1 ? g.ny : g.nz;
+  const int c = axis == 0 ? x : axis == 1 ? y : z;
+  const long long stride = axis == 0 ? 1 : axis == 1 ? (long long)g.nx : (long long)g.nx * g.ny;
+  const int v = c + dir;
+  long long j = i + dir * stride;
+  if (v < 0 || v >= n) {
+    if (!g.per[axis]) return -1;
+    j += v < 0 ? n * stride : -n * stride;
+  }
+  return n == 1 ? -1 : j;  // a periodic axis of length 1 wraps onto the cell itself
+}
+
 __device__ __forceinline__ int axis_color(int v, int n, int per) {
   if (per && (n & 1) && n > 1 && v == n - 1) return 2;
   return v & 1;
@@ -430,19 +445,27 @@ __device__ __forceinline__ bool mc_trial(const Geom& g, const McCoef<T>& c, T* _
   T* my = m + n;
   T* mz = m + 2 * n;
   const long long i = x + (long long)g.nx * (y + (long long)g.ny * z);
+  const T ox = mx[i], oy = my[i], oz = mz[i];
   Nbrs<T> nb;
+  const bool film = g.nz == 1;  // no z bonds: skip their index work and loads
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
     for (int s = 0; s < 2; ++s) {
-      const long long j = nbr_idx(g, x, y, z, a, s ? 1 : -1);
+      if (a == 2 && film) {
+        nb.has[a][s] = false;
+        nb.v[a][s][0] = ox;
+        nb.v[a][s][1] = oy;
+        nb.v[a][s][2] = oz;
+        continue;
+      }
+      const long long j = nbr_step(g, i, x, y, z, a, s ? 1 : -1);
       nb.has[a][s] = j >= 0;
       const long long jj = j >= 0 ? j : i;
       nb.v[a][s][0] = mx[jj];
       nb.v[a][s][1] = my[jj];
       nb.v[a][s][2] = mz[jj];
     }
-  const T ox = mx[i], oy = my[i], oz = mz[i];
   T hx = 0, hy = 0, hz = 0;
   if (c.cd != (T)0) {
     hx = h[i];
@@ -502,6 +525,146 @@ __global__ void __launch_bounds__(256, 4) k_mc_general(Geom g, const McCoef<T>* 
     if (cell_color(g, x, y, z) == color) accepted = mc_trial<T>(g, c, m, h, ctr->stage, ctr->sweep, x, y, z);
   }
   count_accepts(accepted, acc);
+}
+
+// One colour of a two-colour film sweep (nz = 1, nx a multiple of 4) with
+// 16-byte loads: a thread owns a segment of 4 consecutive cells of one row
+// and makes the decisions of its 2 cells of this colour.  The row segment, the
+// same segment of the rows above and below, and one cell on each side are
+// loaded as whole vectors; the segment is stored back whole (its cells of the
+// other colour are written with the values just read, which no thread of this
+// launch changes).  Decisions are those of k_mc_checker (same mc_accept, same
+// inputs).
+template <typename T>
+struct Vec4 {
+  T v[4];
+};
+template <typename T>
+__device__ __forceinline__ Vec4<T> ld4(const T* p) {
+  Vec4<T> r;
+  if constexpr (sizeof(T) == 4) {
+    const float4 a = *reinterpret_cast<const float4*>(p);
+    r.v[0] = a.x, r.v[1] = a.y, r.v[2] = a.z, r.v[3] = a.w;
+  } else {
+    const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+    r.v[0] = a.x, r.v[1] = a.y, r.v[2] = b.x, r.v[3] = b.y;
+  }
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ void st4(T* p, const Vec4<T>& r) {
+  if constexpr (sizeof(T) == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(r.v[0], r.v[1], r.v[2], r.v[3]);
+  } else {
+    reinterpret_cast<double2*>(p)[0] = make_double2(r.v[0], r.v[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(r.v[2], r.v[3]);
+  }
+}
+
+// The decisions of the two cells at offsets P0 and P0 + 2 of a segment.
+template <typename T, int P0>
+__device__ __forceinline__ bool quad_cells(const McCoef<T>& c, Vec4<T> (&own)[3], const Vec4<T> (&up)[3],
+                                           const Vec4<T> (&dn)[3], const T (&lft)[3], const T (&rgt)[3],
+                                           const Vec4<T> (&hh)[3], bool hl, bool hr, bool hd, bool hu,
+                                           uint32_t cell0, uint32_t stage, uint32_t sweep, unsigned int& mine) {
+  bool changed = false;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int o = P0 + 2 * q;  // compile-time after unrolling
+    Nbrs<T> nb;
+    const bool lin = o > 0, rin = o < 3;
+    nb.has[0][0] = lin || hl;
+    nb.has[0][1] = rin || hr;
+    nb.has[1][0] = hd;
+    nb.has[1][1] = hu;
+    nb.has[2][0] = nb.has[2][1] = false;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const T ov = own[k].v[o];
+      nb.v[0][0][k] = lin ? own[k].v[(o + 3) & 3] : (hl ? lft[k] : ov);
+      nb.v[0][1][k] = rin ? own[k].v[(o + 1) & 3] : (hr ? rgt[k] : ov);
+      nb.v[1][0][k] = hd ? dn[k].v[o] : ov;
+      nb.v[1][1][k] = hu ? up[k].v[o] : ov;
+      nb.v[2][0][k] = nb.v[2][1][k] = ov;
+    }
+    const Proposal<T> pr = mc_propose<T>(c, cell0 + (uint32_t)o, stage, sweep);
+    if (mc_accept<T>(c, nb, own[0].v[o], own[1].v[o], own[2].v[o], hh[0].v[o], hh[1].v[o], hh[2].v[o], pr)) {
+      own[0].v[o] = pr.x;
+      own[1].v[o] = pr.y;
+      own[2].v[o] = pr.z;
+      changed = true;
+      ++mine;
+    }
+  }
+  return changed;
+}
+
+__host__ __device__ inline bool mc_quad_ok(const Geom& g) { return g.nz == 1 && g.ncolors == 2 && g.nx % 4 == 0; }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m,
+                                                 const T* __restrict__ h, const SweepCounters* __restrict__ ctr,
+                                                 int color, unsigned long long* acc) {
+  const McCoef<T> c = cp[blockIdx.z];
+  const long long n = g.n;
+  m += blockIdx.z * 3 * n;
+  h += blockIdx.z * 3 * n;
+  acc += blockIdx.z;
+  const int nseg = g.nx >> 2;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned int mine = 0;
+  if (t < nseg * g.ny) {
+    const int y = t / nseg, s = t - y * nseg;  // nseg is a power of two for the usual sizes; cheap either way
+    const int x0 = 4 * s;
+    const long long rowb = (long long)y * g.nx;
+    // neighbour rows: wrapped on a periodic axis, missing at an open edge or
+    // when the axis has length 1
+    int yu = y + 1, yd = y - 1;
+    bool hu = true, hd = true;
+    if (yu >= g.ny) { if (g.per[1]) yu -= g.ny; else hu = false; }
+    if (yd < 0) { if (g.per[1]) yd += g.ny; else hd = false; }
+    if (g.ny == 1) hu = hd = false;
+    // side cells
+    int xl = x0 - 1, xr = x0 + 4;
+    bool hl = true, hr = true;
+    if (xl < 0) { if (g.per[0]) xl += g.nx; else hl = false; }
+    if (xr >= g.nx) { if (g.per[0]) xr -= g.nx; else hr = false; }
+    Vec4<T> own[3], up[3], dn[3];
+    T lft[3], rgt[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const T* base = m + k * n;
+      own[k] = ld4<T>(base + rowb + x0);
+      up[k] = hu ? ld4<T>(base + (long long)yu * g.nx + x0) : own[k];
+      dn[k] = hd ? ld4<T>(base + (long long)yd * g.nx + x0) : own[k];
+      lft[k] = hl ? base[rowb + xl] : (T)0;
+      rgt[k] = hr ? base[rowb + xr] : (T)0;
+    }
+    Vec4<T> hh[3];
+    const bool dm = c.cd != (T)0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (dm) hh[k] = ld4<T>(h + k * n + rowb + x0);
+      else hh[k].v[0] = hh[k].v[1] = hh[k].v[2] = hh[k].v[3] = (T)0;
+    }
+    // this colour's cells sit at offsets p0 and p0 + 2 (x0 is even); the
+    // offsets are compile-time inside quad_cells so the vectors stay in registers
+    bool changed;
+    if (((color + y) & 1) == 0)
+      changed = quad_cells<T, 0>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
+                                 ctr->sweep, mine);
+    else
+      changed = quad_cells<T, 1>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
+                                 ctr->sweep, mine);
+    if (changed) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) st4<T>(m + k * n + rowb + x0, own[k]);
+    }
+  }
+  unsigned int v = mine;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, (unsigned long long)v);
 }
 
 // Both colours of a two-colour film sweep (nz = 1) in one launch.  A CTA owns
@@ -973,16 +1136,24 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
 
 template <typename T>
 cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
-                    unsigned long long* acc, cudaStream_t st, int nrep, int tile) {
+                    unsigned long long* acc, cudaStream_t st, int nrep, int form) {
   const int threads = 256;
-  if (color < 0) {  // every colour: one tile launch for films (tile != 0), else one launch per colour
-    if (tile && mc_tile_ok(g)) {
+  // form: MC_FORM_TILE both colours in one tile launch, MC_FORM_QUAD one
+  // vectorised launch per colour, else one scalar launch per colour
+  if (color < 0) {  // every colour of the sweep
+    if (form == MC_FORM_TILE && mc_tile_ok(g)) {
       dim3 grid((unsigned)((g.nx + MCT - 1) / MCT), (unsigned)((g.ny + MCT - 1) / MCT), nrep);
       k_mc_tile<T><<<grid, threads, mc_tile_smem<T>(), st>>>(g, c, m, h, ctr, acc);
       return cudaGetLastError();
     }
-    for (int col = 0; col < g.ncolors; ++col) MMC_TRY(mc_impl<T>(g, c, m, h, ctr, col, acc, st, nrep, 0));
+    for (int col = 0; col < g.ncolors; ++col) MMC_TRY(mc_impl<T>(g, c, m, h, ctr, col, acc, st, nrep, form));
     return cudaSuccess;
+  }
+  if (form == MC_FORM_QUAD && mc_quad_ok(g)) {
+    const long long total = (long long)g.ny * (g.nx >> 2);
+    dim3 grid((unsigned)((total + threads - 1) / threads), 1, nrep);
+    k_mc_quad<T><<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);
+    return cudaGetLastError();
   }
   if (g.ncolors == 2) {
     const long long total = (long long)g.ny * g.nz * ((g.nx + 1) / 2);
@@ -1037,8 +1208,8 @@ cudaError_t launch_demag_sym(const Geom& g, const FftPlan& px, const FftPlan& py
 }
 template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr, int color,
-                      unsigned long long* acc, cudaStream_t st, int nrep, int tile) {
-  return mc_impl<T>(g, c, m, h, ctr, color, acc, st, nrep, tile);
+                      unsigned long long* acc, cudaStream_t st, int nrep, int form) {
+  return mc_impl<T>(g, c, m, h, ctr, color, acc, st, nrep, form);
 }
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials, int npartials,

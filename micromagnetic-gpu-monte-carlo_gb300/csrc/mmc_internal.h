@@ -118,7 +118,7 @@ struct DemagTuning {
   int col_tx;      // kx columns per tile in the y pass
   int col_tx_z;    // kx columns per tile in the z pass
   int col_threads;
-  int mc_tile;     // 1: both colours of a film sweep in one tile launch
+  int mc_form;     // MC_FORM_*
 };
 
 // Device counters read by the sweep kernels: [stage, sweep].
@@ -136,13 +136,18 @@ template <typename T>
 cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                          const DemagTuning& tun, const T* m, T* h, void* spec, const void* khat,
                          cudaStream_t st, int nrep = 1, cudaEvent_t* ev = nullptr);
-// color < 0: every colour of the sweep (films with tile != 0: one fused tile
-// launch, else one launch per colour).
+// Metropolis kernel forms (all make the same decisions): one scalar launch
+// per colour; both colours of a film in one tile launch; one vectorised launch
+// per colour for films with nx a multiple of 4.
+enum : int { MC_FORM_SCALAR = 0, MC_FORM_TILE = 1, MC_FORM_QUAD = 2 };
+// color < 0: every colour of the sweep in the given form (falls back to the
+// scalar form where the lattice does not qualify).
 template <typename T>
 cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const SweepCounters* ctr,
-                      int color, unsigned long long* acc, cudaStream_t st, int nrep = 1, int tile = 0);
-// Whether a lattice can use the fused two-colour tile sweep, and its tile side.
+                      int color, unsigned long long* acc, cudaStream_t st, int nrep = 1, int form = 0);
+// Whether a lattice can use the tile form (and its tile side) or the vector form.
 bool mc_tile_eligible(const Geom& g);
+bool mc_quad_eligible(const Geom& g);
 constexpr int MC_TILE_SIDE = 32;
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials,

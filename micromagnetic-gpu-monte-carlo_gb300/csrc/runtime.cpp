@@ -187,10 +187,8 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz);
   t.col_tx_z = pick(pz, g.nyp);
   t.col_threads = col_threads_for(g, py, pz, t.col_tx, t.col_tx_z);
-  // the fused two-colour sweep when there are enough tiles to fill the device
-  const long long tiles = (long long)((g.nx + MC_TILE_SIDE - 1) / MC_TILE_SIDE) *
-                          ((g.ny + MC_TILE_SIDE - 1) / MC_TILE_SIDE) * nrep;
-  t.mc_tile = mc_tile_eligible(g) && tiles >= 2LL * nsm ? 1 : 0;
+  // films: the vectorised per-colour sweep (the autotuner also tries the others)
+  t.mc_form = mc_quad_eligible(g) ? MC_FORM_QUAD : MC_FORM_SCALAR;
   return t;
 }
 
@@ -361,9 +359,9 @@ cudaError_t demag(mmc_handle* h) {
 cudaError_t mc_color(mmc_handle* h, int color) {
   if (h->prec == 32)
     return launch_mc<float>(h->g, (const McCoef<float>*)h->coef, (float*)h->m, (const float*)h->h, h->ctr, color,
-                            h->acc, h->st, 1, h->tun.mc_tile);
+                            h->acc, h->st, 1, h->tun.mc_form);
   return launch_mc<double>(h->g, (const McCoef<double>*)h->coef, (double*)h->m, (const double*)h->h, h->ctr, color,
-                           h->acc, h->st, 1, h->tun.mc_tile);
+                           h->acc, h->st, 1, h->tun.mc_form);
 }
 
 // Enqueues one full sweep: demag refresh, every colour, counter advance.
@@ -1232,9 +1230,9 @@ cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
   cudaError_t e;
   if (h->cfg.cal_demag_flag && (e = batch_demag(b, ev)) != cudaSuccess) return e;
   e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h, b->ctr,
-                                       -1, b->acc, h->st, b->R, b->tun.mc_tile)
+                                       -1, b->acc, h->st, b->R, b->tun.mc_form)
                     : launch_mc<double>(h->g, (const McCoef<double>*)b->coef, (double*)b->m, (const double*)b->h,
-                                        b->ctr, -1, b->acc, h->st, b->R, b->tun.mc_tile);
+                                        b->ctr, -1, b->acc, h->st, b->R, b->tun.mc_form);
   if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[4], h->st)) != cudaSuccess) return e;
   return launch_advance(b->ctr, 1, h->st);
@@ -1415,15 +1413,21 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
       }
     }
   }
-  // the other Metropolis form for every pass-kernel shape
-  if (mc_tile_eligible(g)) {
+  // the other Metropolis forms for every pass-kernel shape
+  {
+    std::vector<int> forms;
+    if (mc_quad_eligible(g)) forms.push_back(MC_FORM_QUAD);
+    if (mc_tile_eligible(g)) forms.push_back(MC_FORM_TILE);
+    forms.push_back(MC_FORM_SCALAR);
     const size_t nk = cands.size();
     for (size_t i = 0; i < nk; ++i)
-      if (cands[i].rows_band == 0) {
-        Cand c2 = cands[i];
-        c2.tun.mc_tile = 1 - c2.tun.mc_tile;
-        cands.push_back(c2);
-      }
+      if (cands[i].rows_band == 0)
+        for (int f : forms)
+          if (f != cands[i].tun.mc_form) {
+            Cand c2 = cands[i];
+            c2.tun.mc_form = f;
+            cands.push_back(c2);
+          }
   }
   const size_t mbytes = (size_t)b->R * 3 * g.n * h->tsize;
   void* saved = nullptr;
@@ -2030,7 +2034,8 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[7]) {
       !pow2(t.col_tx) || t.col_tx > 8 || col_pass_smem(h->py.p, t.col_tx, cs) > smem_limit() || !pow2(t.col_tx_z) ||
       t.col_tx_z > 8 || col_pass_smem(h->pz.p, t.col_tx_z, cs) > smem_limit() ||
       (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
-      t.col_threads % 32 != 0 || (t.mc_tile != 0 && t.mc_tile != 1) || (t.mc_tile && !mc_tile_eligible(g)))
+      t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_QUAD ||
+      (t.mc_form == MC_FORM_TILE && !mc_tile_eligible(g)) || (t.mc_form == MC_FORM_QUAD && !mc_quad_eligible(g)))
     return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
   if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())
     return fail(MMC_ERR_UNSUPPORTED, "row-kernel band not available for this batch");
@@ -2054,7 +2059,7 @@ int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int*
 int mmc_batch_launch_shape(mmc_batch* b, int out[7]) {
   if (!b || !out) return fail(MMC_ERR_INVALID, "null argument");
   out[5] = b->rows_band;
-  out[6] = b->tun.mc_tile;
+  out[6] = b->tun.mc_form;
   out[0] = b->tun.x_rows_per_cta;
   out[1] = b->tun.x_threads;
   out[2] = b->tun.col_tx;

@@ -78,21 +78,34 @@ def test_batch_autotune_keeps_state_and_results(M, geom):
 
 
 TILE_GEOMS = [dict(nx=64, ny=64, pbc_x=1, pbc_y=1), dict(nx=96, ny=41, pbc_x=1, pbc_y=0),
-              dict(nx=41, ny=23, pbc_x=0, pbc_y=0)]
+              dict(nx=41, ny=23, pbc_x=0, pbc_y=0), dict(nx=12, ny=2, pbc_x=1, pbc_y=1),
+              dict(nx=4, ny=1, pbc_x=1, pbc_y=1), dict(nx=20, ny=10, pbc_x=0, pbc_y=1)]
+
+
+def form_ok(geom, form):
+    """Eligibility of the tile (1) and vector (2) forms for a two-colour film."""
+    nx, ny = geom["nx"], geom["ny"]
+    if form == 2:
+        return nx % 4 == 0
+    per_ok = lambda n, p: p == 0 or (n % 32 == 0 and n >= 64)
+    return per_ok(nx, geom.get("pbc_x", 2)) and per_ok(ny, geom.get("pbc_y", 1))
 
 
 @pytest.mark.parametrize("prec", [32, 64])
 @pytest.mark.parametrize("geom", TILE_GEOMS)
-def test_mc_tile_bitwise_equals_colour_kernels(M, prec, geom):
-    """Both colours in one tile launch (ring of colour-0 cells recomputed)
-    against one launch per colour."""
+@pytest.mark.parametrize("form", [1, 2])
+def test_mc_forms_bitwise_equal_scalar_kernels(M, prec, geom, form):
+    """Both colours in one tile launch (ring of colour-0 cells recomputed), or
+    the vectorised per-colour form, against the scalar per-colour form."""
+    if not form_ok(geom, form):
+        pytest.skip("form not available for this lattice (checked in test_mc_forms_rejected_where_ineligible)")
     cfgs = cfgs_for(M, 3, prec, sweep_engine=1, **geom)
     with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
         sa, sb = list(a.launch_shape()), list(b.launch_shape())
-        sa[6], sb[6] = 0, 1
+        sa[6], sb[6] = 0, form
         a.set_launch_shape(sa)
         b.set_launch_shape(sb)
-        assert a.launch_shape()[6] == 0 and b.launch_shape()[6] == 1
+        assert a.launch_shape()[6] == 0 and b.launch_shape()[6] == form
         for s0, n in ((0, 37), (37, 32)):
             a.run_sweeps(3, s0, n)
             b.run_sweeps(3, s0, n)
@@ -101,11 +114,12 @@ def test_mc_tile_bitwise_equals_colour_kernels(M, prec, geom):
         assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
 
 
-def test_mc_tile_fp64_decisions_match_oracle(M, O):
+@pytest.mark.parametrize("form", [1, 2])
+def test_mc_forms_fp64_decisions_match_oracle(M, O, form):
     c = cfgs_for(M, 1, 64, sweep_engine=1, nx=64, ny=64, pbc_x=1, pbc_y=1)[0]
     with M.Batch([c]) as b:
         s = list(b.launch_shape())
-        s[6] = 1
+        s[6] = form
         b.set_launch_shape(s)
         m0 = b.get_m(0)
         b.run_sweeps(2, 0, 60)
@@ -120,12 +134,19 @@ def test_mc_tile_fp64_decisions_match_oracle(M, O):
     assert np.array_equal(got, m)
 
 
-def test_mc_tile_rejected_where_ineligible(M):
+def test_mc_forms_rejected_where_ineligible(M):
     # a 48-wide periodic axis is not a whole number of 32-cell tiles
     with M.Batch(cfgs_for(M, 1, 32, nx=48, ny=64, pbc_x=1, pbc_y=1)) as b:
         s = list(b.launch_shape())
-        assert s[6] == 0
+        assert s[6] == 2
         s[6] = 1
+        with pytest.raises(M.MmcError):
+            b.set_launch_shape(s)
+    # the vector form needs nx % 4 == 0
+    with M.Batch(cfgs_for(M, 1, 32, nx=18, ny=8, pbc_x=1, pbc_y=1)) as b:
+        s = list(b.launch_shape())
+        assert s[6] == 0
+        s[6] = 2
         with pytest.raises(M.MmcError):
             b.set_launch_shape(s)
 
