@@ -186,6 +186,73 @@ def cpu_sample(M, O, k6, seconds=12.0, threads=0):
     return ns * n / dt, ns
 
 
+def pt_farm(M, local, sweeps):
+    """The batched parallel-tempering workload: 64 FP32 replicas (seeds 1..64)
+    in 4 ladders of 16 temperatures geometric over 40-1400 K, swaps every 10
+    sweeps; each ladder draws its square side from {64, 96, 128, 192, 256}, its
+    B_z from U[0.1, 0.5] T and its DMI from U[3e-3, 6e-3] J/m^2 (a ladder
+    shares one Hamiltonian so its swaps are valid); ladders of one side form
+    one batch, all batches advance together as a farm, each with its autotuned
+    launch shape."""
+    rng = np.random.default_rng(64)
+    sides = rng.choice([64, 96, 128, 192, 256], size=4)
+    bz = rng.uniform(0.1, 0.5, size=4)
+    dind = rng.uniform(3e-3, 6e-3, size=4)
+    T = np.geomspace(40.0, 1400.0, 16)
+    base = {k: v for k, v in WORKLOAD.items() if k not in ("nx", "ny", "Bextz", "Dind", "randomseed")}
+    batches, seed, t0 = [], 1, time.perf_counter()
+    for side in sorted(set(int(v) for v in sides)):
+        ls = [i for i in range(4) if int(sides[i]) == side]
+        cfgs = [M.Config.defaults(precision=32, nx=side, ny=side, randomseed=seed + k, Bextz=float(bz[ls[k // 16]]),
+                                  Dind=float(dind[ls[k // 16]]), **base) for k in range(16 * len(ls))]
+        b = M.Batch(cfgs, device=local)
+        b.build_demag(CACHE_DIR)
+        b.set_ladders(np.arange(16 * len(ls), dtype=np.int32).reshape(len(ls), 16), np.tile(T, (len(ls), 1)), 10,
+                      1000 + seed)
+        b.autotune(4)
+        batches.append(b)
+        seed += 16 * len(ls)
+    setup = time.perf_counter() - t0
+    with M.Farm(batches) as farm:
+        farm.run_sweeps(0, 0, 200)
+        farm.run_sweeps(1, 0, sweeps)
+        ms = farm.last_run_ms()
+    cells = sum(b.R * b.n for b in batches)
+    att = acc = 0
+    for b in batches:
+        _, cnt = b.ladder_state()
+        att += int(cnt[0])
+        acc += int(cnt[1])
+        b.close()
+    return {"value": cells * sweeps / (ms / 1e3), "unit": UNIT, "replicas": 64, "ladders": 4,
+            "sides": [int(v) for v in sides], "batches": len(batches), "swap_interval": 10, "sweeps": sweeps,
+            "wall_ms": ms, "swap_acceptance": acc / max(att, 1), "setup_s": setup,
+            "timing": "host wall clock of one farm call (all batches, their graphs and swap passes)"}
+
+
+def relax_line(M, local):
+    """Gradient and relaxation on the 256x256x1 film in FP64: a short anneal
+    (34 stages of 100 sweeps, seed 11), then projected steepest descent to a
+    max torque |m x H|/Ms < 1e-6."""
+    lat = M.Lattice(M.Config.defaults(precision=64, **dict(WORKLOAD, randomseed=11)), device=local)
+    lat.build_demag(CACHE_DIR)
+    for k in range(34):
+        lat.run_sweeps(stage_temperature(k), k, 0, 100)
+    e0 = lat.energy().e_total
+    lat.grad()
+    t0 = time.perf_counter()
+    for _ in range(10):
+        lat.grad()
+    grad_ms = (time.perf_counter() - t0) / 10 * 1e3
+    t0 = time.perf_counter()
+    it, tq = lat.relax(1e-6, 200000)
+    dt = time.perf_counter() - t0
+    e1 = lat.energy().e_total
+    lat.close()
+    return {"precision": "fp64", "iterations": it, "max_torque": tq, "seconds": dt, "ms_per_iteration":
+            1e3 * dt / max(it, 1), "energy_before_J": e0, "energy_after_J": e1, "grad_ms_with_copy_to_host": grad_ms}
+
+
 def run_reference(args):
     """The reference's CPU path on the host cores.  The reference cannot be
     built (its Metropolis, energy and tensor-image kernel bodies are not
@@ -342,6 +409,15 @@ def run_ours(args):
     single.run_sweeps(stage_temperature(1), 1, 0, 4000)
     single_v = 4000 * n / (single.last_run_ms() / 1e3)
     single_engine = single.engine()
+    phases = None
+    if single_engine[0] == M.ENGINE_FUSED:
+        # device timestamps of the film engine's phases (CTA 0), sweeps 2..14 of a 16-sweep launch
+        st = single.profile_fused(stage_temperature(1), 1, 4000, 16).astype(np.float64)[2:15, :, 0]
+        d = np.diff(st, axis=1).mean(axis=0) / 1e3
+        names = ["copies", "demag_field_rows", "metropolis", "spectrum_rows", "barrier_1", "column_copies",
+                 "column_phase", "barrier_2"]
+        phases = {k: round(float(v), 3) for k, v in zip(names, d)}
+        phases["sweep"] = round(float((st[1:, 0] - st[:-1, 0]).mean() / 1e3), 3)
     fp64_line = None
     if not args.no_fp64:
         lat64 = M.Lattice(M.Config.defaults(precision=64, sweep_engine=M.ENGINE_KERNELS, **WORKLOAD), device=local)
@@ -352,6 +428,9 @@ def run_ours(args):
         lat64.close()
         fp64_line = {"value": fp64, "unit": UNIT, "engine": "kernels", "lattices": 1,
                      "batched_fp32_over_fp64": value / world / fp64, "single_fp32_over_fp64": single_v / fp64}
+
+    farm_line = None if args.no_farm else pt_farm(M, local, 2000)
+    relax = None if args.no_relax else relax_line(M, local)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -366,8 +445,11 @@ def run_ours(args):
         "roofline": roofline,
         "clocks": clk.summary(),
         "gpu_launches": args.steps * S * (3 if shape[5] > 0 else 5 if shape[6] == 1 else 6),
-        "single_lattice_fp32": {"value": single_v, "unit": UNIT, "engine": single_engine},
+        "single_lattice_fp32": {"value": single_v, "unit": UNIT, "engine": single_engine,
+                                "film_engine_phase_us": phases},
         "fp64_plain": fp64_line,
+        "pt_farm_fp32": farm_line,
+        "relax": relax,
         "setup_s": setup_s,
         "autotune": {"candidates": tune_n, "best_ms_per_batch_sweep": tune_ms, "seconds": tune_s,
                      "launch_shape": list(shape)},
@@ -397,8 +479,10 @@ def main():
     ap.add_argument("--ref-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-farm", action="store_true", help="skip the parallel-tempering farm line")
+    ap.add_argument("--no-relax", action="store_true", help="skip the gradient / relaxation line")
     ap.add_argument("--launch-shape", default="",
-                    help="seven comma-separated values of a launch shape to use instead of autotuning")
+                    help="eight comma-separated values of a launch shape to use instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

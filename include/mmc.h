@@ -232,7 +232,7 @@ int mmc_energy(mmc_handle* h, mmc_observables* out);
 int mmc_grad(mmc_handle* h, double* dE_dm, double dE_dparams[7]);
 /* Energy minimisation from the current m: projected steepest descent on the
  * unit sphere (direction P = t - (t.m) m with t = H / Ms, m renormalised every
- * step) with alternating Barzilai-Borwein step lengths, until
+ * step) with Barzilai-Borwein step lengths s.s / s.y, until
  * max_i |m_i x H_i| / Ms < torque_tol or max_iter updates.  H uses the
  * symmetrised demag field, so P is the projected negative gradient of the
  * energy.  iters receives the updates made, max_torque the last torque (either
@@ -319,23 +319,24 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
  * passes, the band of the film row kernel (0 when sweeps use one kernel per
  * pass), and the Metropolis form: 0 one launch per colour, 1 both colours of
  * a film in one tile launch, 2 one vectorised launch per colour (films with
- * nx a multiple of 4). */
-int mmc_batch_launch_shape(mmc_batch* b, int out[7]);
+ * nx a multiple of 4), and whether the pass kernels expand their transforms in
+ * line (1) or call them out of line (0). */
+int mmc_batch_launch_shape(mmc_batch* b, int out[8]);
 /* Autotuner: times each launch shape this batch can run with (the film row
  * kernel with each band that fits; the pass kernels with 1-16 rows per x-pass
- * CTA and 1-8 kx columns per column-pass tile, each with both Metropolis
- * forms) for `sweeps` sweeps from the
+ * CTA and 1-8 kx columns per column-pass tile, each with the transforms in
+ * and out of line and every Metropolis form) for `sweeps` sweeps from the
  * current state, keeps the fastest and restores m and the acceptance
  * counters.  Every shape gives bit-identical results, so the choice changes
  * only the speed.  best_ms_per_sweep and candidates may be NULL.  No
  * counterpart in the reference, whose block shape is fixed in the source
  * (src/main.cu:275-286). */
 int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int* candidates);
-/* Sets the launch shape (the seven values of mmc_batch_launch_shape), e.g. one
+/* Sets the launch shape (the eight values of mmc_batch_launch_shape), e.g. one
  * an earlier autotune chose.  Values outside the ranges the autotuner tries,
  * or a row-kernel band that does not fit this batch, are rejected.  Results do
  * not depend on the shape.  No counterpart in the reference. */
-int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[7]);
+int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[8]);
 
 /* Replica farms: batches of different lattice sizes advanced together.  One
  * call runs nsweeps sweeps of every batch (each with its own temperatures,

@@ -218,7 +218,7 @@ struct RegDft<T, INV, 1> {
 //   transpose in the line (swizzled) --(B-point DFT over b)--> X[ka + A kb].
 // `roots` holds exp(-2 pi i j / N), j < N.
 template <typename T, bool INV, int A, int B>
-__device__ __noinline__ void fft_lines_warp(C<T>* buf, int nlines, int stride, const C<T>* roots) {
+__device__ __forceinline__ void fft_lines_warp_body(C<T>* buf, int nlines, int stride, const C<T>* roots) {
   using V = C<T>;
   constexpr int Q = A / B;
   constexpr int GPW = 32 / B;  // lines per warp
@@ -267,22 +267,38 @@ __device__ __noinline__ void fft_lines_warp(C<T>* buf, int nlines, int stride, c
   }
 }
 
+// Out-of-line copy (kernels that hold much state around the transform call it
+// so that the transform's registers are not added to theirs).
+template <typename T, bool INV, int A, int B>
+__device__ __noinline__ void fft_lines_warp(C<T>* buf, int nlines, int stride, const C<T>* roots) {
+  fft_lines_warp_body<T, INV, A, B>(buf, nlines, stride, roots);
+}
+
 // Transform dispatcher: the warp-level path for the lengths the plan marks,
 // the Stockham stages otherwise.  Returns the buffer holding the result; all
 // threads of the block must call it after the input is complete
 // (__syncthreads()), and the result is complete for all threads on return.
-template <typename T, bool INV>
+template <typename T, bool INV, int A, int B, bool INL>
+__device__ __forceinline__ void fft_warp_call(C<T>* buf, int nlines, int stride, const C<T>* roots) {
+  if constexpr (INL)
+    fft_lines_warp_body<T, INV, A, B>(buf, nlines, stride, roots);
+  else
+    fft_lines_warp<T, INV, A, B>(buf, nlines, stride, roots);
+}
+
+// INL: expand the warp-level transforms into the calling kernel.
+template <typename T, bool INV, bool INL = false>
 __device__ C<T>* fft_run(C<T>* a, C<T>* b, int nlines, int stride, const FftPlan& p, const C<T>* tw) {
   if (p.warp_a == 16 && p.warp_b == 16) {
-    fft_lines_warp<T, INV, 16, 16>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 16, 16, INL>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 16 && p.warp_b == 8) {
-    fft_lines_warp<T, INV, 16, 8>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 16, 8, INL>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 8 && p.warp_b == 8) {
-    fft_lines_warp<T, INV, 8, 8>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 8, 8, INL>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 16 && p.warp_b == 2) {
-    fft_lines_warp<T, INV, 16, 2>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 16, 2, INL>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 8 && p.warp_b == 4) {
-    fft_lines_warp<T, INV, 8, 4>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 8, 4, INL>(a, nlines, stride, tw + p.full_off);
   } else {
     return fft_lines<T, INV>(a, b, nlines, stride, p, tw);
   }

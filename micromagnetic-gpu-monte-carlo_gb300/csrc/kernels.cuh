@@ -25,7 +25,7 @@ namespace mmc {
 // Rows that are pure zero padding are never loaded (pruned transform).
 
 // Real rows in[c][row][x] (x < xdata, zero up to p.n) -> S[c][z][y][kx], kx < hx.
-template <typename T>
+template <typename T, bool INL>
 __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
                             long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, FastDiv dhx,
                             int pitch, int rows_per_cta, long long in_rstride, long long s_rstride) {
@@ -68,7 +68,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nr
     }
   }
   __syncthreads();
-  V* res = fft_run<T, false>(bufA, bufB, nr * npairs, L, p, tw);
+  V* res = fft_run<T, false, INL>(bufA, bufB, nr * npairs, L, p, tw);
   for (int idx = threadIdx.x; idx < nr * npairs * hx; idx += blockDim.x) {
     const int rest = dhx.div(idx);
     const int k = idx - rest * hx;
@@ -86,7 +86,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nr
 }
 
 // Half spectra S[0..2][z][y][kx] -> real rows out[c][row][x], x < xout.
-template <typename T>
+template <typename T, bool INL>
 __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
                             FastDiv dxo, FastDiv dyo, int nrows, T* __restrict__ out, long long out_cstride,
                             int rows_per_cta, long long s_rstride, long long out_rstride) {
@@ -132,7 +132,7 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
     }
   }
   __syncthreads();
-  V* res = fft_run<T, true>(bufA, bufB, nr * 2, L, p, tw);
+  V* res = fft_run<T, true, INL>(bufA, bufB, nr * 2, L, p, tw);
   for (int idx = threadIdx.x; idx < nr * xout; idx += blockDim.x) {
     const int rr = dxo.div(idx), x = idx - rr * xout;
     const long long o = (long long)(row0 + rr) * xout + x;
@@ -154,7 +154,7 @@ enum : int { PASS_FWD = 1, PASS_MUL = 2, PASS_INV = 4, PASS_SYM = 8 };
 // pos*pos_stride + kx0 + col].  Loads pos < load_lim (zero above), stores
 // pos < store_lim.  With PASS_MUL the tile is multiplied by the symmetric
 // tensor spectrum (K^ . M^ / N, calHexchangeKernel) between the transforms.
-template <typename T>
+template <typename T, bool INL>
 __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long nspec, const C<T>* __restrict__ khat,
                            int hx, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
                            int flags, T inv_n, int tx, long long s_rstride) {
@@ -221,7 +221,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
   V* cur = bufA;
   V* oth = bufB;
   if (flags & PASS_FWD) {
-    V* r = fft_run<T, false>(cur, oth, nlines, stride, p, tw);
+    V* r = fft_run<T, false, INL>(cur, oth, nlines, stride, p, tw);
     if (r != cur) {
       oth = cur;
       cur = r;
@@ -255,7 +255,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
     __syncthreads();
   }
   if (flags & PASS_INV) {
-    V* r = fft_run<T, true>(cur, oth, nlines, stride, p, tw);
+    V* r = fft_run<T, true, INL>(cur, oth, nlines, stride, p, tw);
     if (r != cur) {
       oth = cur;
       cur = r;
@@ -1053,12 +1053,10 @@ inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize, b
 // inside a stream capture.
 template <typename T>
 cudaError_t prepare_impl(int max_dyn_smem) {
-  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_x_forward<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    max_dyn_smem));
-  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_x_inverse<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    max_dyn_smem));
-  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_col_pass<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    max_dyn_smem));
+  const void* fns[] = {(const void*)k_x_forward<T, false>, (const void*)k_x_forward<T, true>,
+                       (const void*)k_x_inverse<T, false>, (const void*)k_x_inverse<T, true>,
+                       (const void*)k_col_pass<T, false>,  (const void*)k_col_pass<T, true>};
+  for (const void* f : fns) MMC_TRY_ATTR(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)mc_tile_smem<T>()));
   return cudaSuccess;
@@ -1068,12 +1066,13 @@ template <typename T>
 cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int nrows, const T* in,
                           long long in_cstride, C<T>* S, long long nspec, int nyp, int hx, int pitch, int rpc,
                           int threads, cudaStream_t st, int nrep = 1, long long in_rstride = 0,
-                          long long s_rstride = 0) {
+                          long long s_rstride = 0, bool inl = false) {
   const int lines = (ncomp + 1) / 2;
   size_t sm = x_pass_smem(p, lines, rpc, sizeof(C<T>));
   dim3 grid((nrows + rpc - 1) / rpc, 1, nrep);
-  k_x_forward<T><<<grid, threads, sm, st>>>(p, ncomp, xdata, FastDiv((uint32_t)ydata), nrows, in, in_cstride, S, nspec,
-                                            nyp, FastDiv((uint32_t)hx), pitch, rpc, in_rstride, s_rstride);
+  auto kern = inl ? k_x_forward<T, true> : k_x_forward<T, false>;
+  kern<<<grid, threads, sm, st>>>(p, ncomp, xdata, FastDiv((uint32_t)ydata), nrows, in, in_cstride, S, nspec, nyp,
+                                  FastDiv((uint32_t)hx), pitch, rpc, in_rstride, s_rstride);
   return cudaGetLastError();
 }
 
@@ -1081,10 +1080,11 @@ template <typename T>
 cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, const C<T>* khat, int hx,
                          int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
                          int flags, T inv_n, int tx, int threads, cudaStream_t st, int nrep = 1,
-                         long long s_rstride = 0) {
+                         long long s_rstride = 0, bool inl = false) {
   size_t sm = col_pass_smem(p, ncomp, tx, sizeof(C<T>), (flags & PASS_MUL) != 0);
   dim3 grid((hx + tx - 1) / tx, planes, nrep);
-  k_col_pass<T><<<grid, threads, sm, st>>>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
+  auto kern = inl ? k_col_pass<T, true> : k_col_pass<T, false>;
+  kern<<<grid, threads, sm, st>>>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
                                            store_lim, flags, inv_n, tx, s_rstride);
   return cudaGetLastError();
 }
@@ -1107,27 +1107,28 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
   const int rows = g.ny * g.nz;
   if (ev) MMC_TRY(cudaEventRecord(ev[0], st));
   MMC_TRY(run_x_forward<T>(px, 3, g.nx, g.ny, rows, m, g.n, S, ns, g.nyp, g.hx, g.hxp, tun.x_rows_per_cta,
-                           tun.x_threads, st, nrep, mr, sr));
+                           tun.x_threads, st, nrep, mr, sr, tun.fft_inline != 0));
   if (ev) MMC_TRY(cudaEventRecord(ev[1], st));
   const long long ystride = g.hxp, yplane = (long long)g.nyp * g.hxp;
   if (g.nzp == 1) {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny,
                             PASS_FWD | PASS_MUL | PASS_INV | mul_flags, inv_n, tun.col_tx, tun.col_threads, st, nrep,
-                            sr));
+                            sr, tun.fft_inline != 0));
   } else {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.ny, g.nyp, PASS_FWD, inv_n, tun.col_tx,
-                            tun.col_threads, st, nrep, sr));
+                            tun.col_threads, st, nrep, sr, tun.fft_inline != 0));
     MMC_TRY(run_col_pass<T>(pz, 3, S, ns, K, g.hx, g.nyp, ystride, yplane, g.nz, g.nz,
                             PASS_FWD | PASS_MUL | PASS_INV | mul_flags, inv_n, tun.col_tx_z, tun.col_threads, st, nrep,
-                            sr));
+                            sr, tun.fft_inline != 0));
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.nyp, g.ny, PASS_INV, inv_n, tun.col_tx,
-                            tun.col_threads, st, nrep, sr));
+                            tun.col_threads, st, nrep, sr, tun.fft_inline != 0));
   }
   if (ev) MMC_TRY(cudaEventRecord(ev[2], st));
   const int rpc = tun.x_rows_per_cta;
   size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
   dim3 grid((rows + rpc - 1) / rpc, 1, nrep);
-  k_x_inverse<T><<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx, g.dny, rows, h, g.n, rpc,
+  auto kinv = tun.fft_inline ? k_x_inverse<T, true> : k_x_inverse<T, false>;
+  kinv<<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx, g.dny, rows, h, g.n, rpc,
                                                   sr, mr);
   MMC_TRY(cudaGetLastError());
   if (ev) MMC_TRY(cudaEventRecord(ev[3], st));
@@ -1231,7 +1232,7 @@ cudaError_t launch_col_pass_2d(const Geom& g, const FftPlan& py, const DemagTuni
   const T inv_n = (T)(1.0 / (double)g.np);
   return run_col_pass<T>(py, 3, reinterpret_cast<C<T>*>(spec), g.nspec, reinterpret_cast<const C<T>*>(khat), g.hx, 1,
                          (long long)g.nyp * g.hxp, g.hxp, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV, inv_n,
-                         tun.col_tx, tun.col_threads, st, nrep, 3 * g.nspec);
+                         tun.col_tx, tun.col_threads, st, nrep, 3 * g.nspec, tun.fft_inline != 0);
 }
 template <typename T>
 cudaError_t launch_prepare(int max_dyn_smem) {

@@ -119,6 +119,7 @@ struct DemagTuning {
   int col_tx_z;    // kx columns per tile in the z pass
   int col_threads;
   int mc_form;     // MC_FORM_*
+  int fft_inline;  // 1: the pass kernels expand the warp-level transforms in line
 };
 
 // Device counters read by the sweep kernels: [stage, sweep].

@@ -187,8 +187,11 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz);
   t.col_tx_z = pick(pz, g.nyp);
   t.col_threads = col_threads_for(g, py, pz, t.col_tx, t.col_tx_z);
-  // films: the vectorised per-colour sweep (the autotuner also tries the others)
-  t.mc_form = mc_quad_eligible(g) ? MC_FORM_QUAD : MC_FORM_SCALAR;
+  // FP32 film batches: the vectorised per-colour sweep, measured faster from
+  // about 8 replicas; single lattices and FP64 keep the scalar form (the
+  // autotuner tries every form)
+  t.mc_form = csize == 8 && nrep >= 8 && mc_quad_eligible(g) ? MC_FORM_QUAD : MC_FORM_SCALAR;
+  t.fft_inline = 0;
   return t;
 }
 
@@ -807,9 +810,11 @@ int relax_impl(mmc_handle* h, double tol, long long max_iter, long long* iters, 
       return fail(MMC_ERR_INVALID, "relaxation produced a non-finite torque");
     if (tq < tol || it >= max_iter) break;
     if (it > 0) {
-      // alternate the two Barzilai-Borwein step lengths; keep the last one
-      // when the curvature estimate is not positive
-      const double t = (it & 1) ? ss / sy : sy / yy;
+      // the long Barzilai-Borwein step s.s / s.y (the short one, s.y / y.y,
+      // stalled on annealed films in tests); keep the last step when the
+      // curvature estimate is not positive
+      const double t = ss / sy;
+      (void)yy;
       if (std::isfinite(t) && t > 0) tau = t;
     }
     CU(h->prec == 32 ? launch_relax_update<float>(h->g, (float*)h->m, h->relax_p, tau, h->relax_s, h->st)
@@ -1412,6 +1417,16 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
         cands.push_back({0, t});
       }
     }
+  }
+  // the in-line transforms for every pass-kernel shape
+  {
+    const size_t nk = cands.size();
+    for (size_t i = 0; i < nk; ++i)
+      if (cands[i].rows_band == 0) {
+        Cand c2 = cands[i];
+        c2.tun.fft_inline = 1 - c2.tun.fft_inline;
+        cands.push_back(c2);
+      }
   }
   // the other Metropolis forms for every pass-kernel shape
   {
@@ -2022,12 +2037,12 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
   return MMC_OK;
 }
 
-int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[7]) {
+int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[8]) {
   if (!b || !shape) return fail(MMC_ERR_INVALID, "null argument");
   mmc_handle* h = b->base;
   const Geom& g = h->g;
   const size_t cs = 2 * h->tsize;
-  DemagTuning t{shape[0], shape[1], shape[2], shape[3], shape[4], shape[6]};
+  DemagTuning t{shape[0], shape[1], shape[2], shape[3], shape[4], shape[6], shape[7]};
   const int band = shape[5];
   auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
   if (!pow2(t.x_rows_per_cta) || t.x_rows_per_cta > 16 || x_pass_smem(h->px.p, t.x_rows_per_cta, cs) > smem_limit() ||
@@ -2035,7 +2050,8 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[7]) {
       t.col_tx_z > 8 || col_pass_smem(h->pz.p, t.col_tx_z, cs) > smem_limit() ||
       (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
       t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_QUAD ||
-      (t.mc_form == MC_FORM_TILE && !mc_tile_eligible(g)) || (t.mc_form == MC_FORM_QUAD && !mc_quad_eligible(g)))
+      (t.mc_form == MC_FORM_TILE && !mc_tile_eligible(g)) || (t.mc_form == MC_FORM_QUAD && !mc_quad_eligible(g)) ||
+      (t.fft_inline != 0 && t.fft_inline != 1))
     return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
   if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())
     return fail(MMC_ERR_UNSUPPORTED, "row-kernel band not available for this batch");
@@ -2056,10 +2072,11 @@ int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int*
   return batch_autotune(b, sweeps, best_ms_per_sweep, candidates);
 }
 
-int mmc_batch_launch_shape(mmc_batch* b, int out[7]) {
+int mmc_batch_launch_shape(mmc_batch* b, int out[8]) {
   if (!b || !out) return fail(MMC_ERR_INVALID, "null argument");
   out[5] = b->rows_band;
   out[6] = b->tun.mc_form;
+  out[7] = b->tun.fft_inline;
   out[0] = b->tun.x_rows_per_cta;
   out[1] = b->tun.x_threads;
   out[2] = b->tun.col_tx;

@@ -460,11 +460,11 @@ class Batch:
         return ms.value, n.value
 
     def set_launch_shape(self, shape):
-        arr = (ctypes.c_int * 7)(*[int(v) for v in shape])
+        arr = (ctypes.c_int * 8)(*[int(v) for v in shape])
         check(lib().mmc_batch_set_launch_shape(self.h, arr))
 
     def launch_shape(self):
-        out = (ctypes.c_int * 7)()
+        out = (ctypes.c_int * 8)()
         check(lib().mmc_batch_launch_shape(self.h, out))
         return tuple(out)
 

@@ -134,11 +134,29 @@ def test_mc_forms_fp64_decisions_match_oracle(M, O, form):
     assert np.array_equal(got, m)
 
 
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("geom", [dict(nx=64, ny=48, pbc_x=2, pbc_y=2), dict(nx=12, ny=10, nz=3, pbc_x=0, pbc_y=0),
+                                  dict(nx=15, ny=8, pbc_x=1, pbc_y=1)])
+def test_inline_transforms_bitwise_equal(M, prec, geom):
+    """The pass kernels with the warp-level transforms in line and out of line
+    round identically."""
+    cfgs = cfgs_for(M, 2, prec, sweep_engine=1, **geom)
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        sa, sb = list(a.launch_shape()), list(b.launch_shape())
+        sa[7], sb[7] = 0, 1
+        a.set_launch_shape(sa)
+        b.set_launch_shape(sb)
+        a.run_sweeps(1, 0, 29)
+        b.run_sweeps(1, 0, 29)
+        for r in range(2):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+
+
 def test_mc_forms_rejected_where_ineligible(M):
     # a 48-wide periodic axis is not a whole number of 32-cell tiles
     with M.Batch(cfgs_for(M, 1, 32, nx=48, ny=64, pbc_x=1, pbc_y=1)) as b:
         s = list(b.launch_shape())
-        assert s[6] == 2
+        assert s[6] == 0  # one replica: the scalar form by default
         s[6] = 1
         with pytest.raises(M.MmcError):
             b.set_launch_shape(s)

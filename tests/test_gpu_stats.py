@@ -55,3 +55,41 @@ def test_full_anneal_statistics_fp32_vs_fp64(M, tmp_path_factory):
         assert diff <= 4 * se + 1e-12 * abs(b.mean()), name
     # the annealed states are ordered: low energy, skyrmion / stripe mixture
     assert e64.mean() < 0
+
+
+def test_fp32_error_report_256(M, tmp_path):
+    """FP32 against FP64 on the 256x256x1 film (PBC 20 images, config-1
+    material) for one random state: every field term, the energy terms, <m>
+    and Q.  Printed as a table (pytest -s) and bounded."""
+    W = dict(MATERIAL, nx=256, ny=256, randomseed=11)
+    out = {}
+    with M.Lattice(M.Config.defaults(precision=64, **W)) as a, M.Lattice(M.Config.defaults(precision=32, **W)) as b:
+        a.build_demag(str(tmp_path))
+        b.build_demag(str(tmp_path))
+        m = a.get_m()
+        b.set_m(m)
+        m32 = b.get_m()
+        a.set_m(m32)  # both start from the FP32-representable state
+        a.compute_demag()
+        b.compute_demag()
+        names = ["exchange", "dmi", "anisotropy", "zeeman", "demag", "total"]
+        for term, name in enumerate(names):
+            fa, fb = a.field(term), b.field(term)
+            out["H_" + name] = np.abs(fb - fa).max() / max(np.abs(fa).max(), 1e-300)
+        oa, ob = a.energy(), b.energy()
+        # energies relative to the sum of the terms' magnitudes (terms of a
+        # random state cancel)
+        scale = sum(abs(getattr(oa, k)) for k in ("e_exchange", "e_dmi", "e_anisotropy", "e_zeeman", "e_demag"))
+        for k in ("e_exchange", "e_dmi", "e_anisotropy", "e_zeeman", "e_demag", "e_total"):
+            out[k] = abs(getattr(ob, k) - getattr(oa, k)) / scale
+        out["<m_z>"] = abs(ob.m[2] - oa.m[2])
+        out["Q"] = abs(ob.q - oa.q)
+        ga, pa = a.grad()
+        gb, pb = b.grad()
+        out["dE/dm"] = np.abs(gb - ga).max() / np.abs(ga).max()
+        out["dE/dparams"] = float(np.max(np.abs(pb - pa) / np.abs(pa)))
+    for k, v in out.items():
+        print(f"fp32 vs fp64  {k:14s} {v:.3e}")
+    for k, v in out.items():
+        bound = 2e-5 if k.startswith("H_") or k == "dE/dm" else 1e-5 if k.startswith("e_") or k == "<m_z>" else 1e-4
+        assert v <= bound, (k, v)
