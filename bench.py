@@ -54,18 +54,28 @@ def stage_temperature(k):
 
 
 def ncu_traffic(kernel, shape):
-    """DRAM bytes per launch of `kernel` at launch shape `shape` from the
-    committed ncu summary (a line "dram_bytes_per_launch <kernel> <shape>: N"),
-    or None."""
+    """(DRAM bytes per launch, launch shape of the capture) of `kernel` from
+    the committed ncu summary (lines "dram_bytes_per_launch <kernel> <shape>:
+    N"): the capture at `shape` if there is one, else the kernel's capture at
+    another shape (the autotuner's pick varies between runs), else (None, None)."""
     p = os.path.join(ROOT, "profiles", "batch32_256x256_kernels.md")
     if not os.path.exists(p):
-        return None
-    key = f"dram_bytes_per_launch {kernel} {','.join(str(v) for v in shape)}:"
+        return None, None
+    want = ",".join(str(v) for v in shape)
+    found = (None, None)
     with open(p) as f:
         for line in f:
-            if line.strip().startswith(key):
-                return float(line.split(":", 1)[1])
-    return None
+            parts = line.strip().split()
+            if len(parts) == 4 and parts[0] == "dram_bytes_per_launch" and parts[1] == kernel:
+                sh = parts[2].rstrip(":")
+                try:
+                    val = float(parts[3])
+                except ValueError:
+                    continue
+                if sh == want:
+                    return val, sh
+                found = (val, sh)
+    return found
 
 
 def measured_peaks():
@@ -230,6 +240,34 @@ def pt_farm(M, local, sweeps):
             "timing": "host wall clock of one farm call (all batches, their graphs and swap passes)"}
 
 
+SLAB = dict(nx=512, ny=512, nz=8, dx=2e-9, dy=2e-9, dz=1e-9, ms=1.1e6, Aex=15e-12, Dind=3e-3, Ku1=0.8e6,
+            anisUx=0.0, anisUy=0.0, anisUz=1.0, Bextx=0.0, Bexty=0.0, Bextz=0.2, pbc_x=10, pbc_y=10, pbc_z=0,
+            cal_demag_flag=1, randomseed=7, use_random_init=1)
+
+
+def slab_line(M, local, sweeps):
+    """The 3-D slab in FP32: 512x512x8 cells, PBC 10 images in x and y, open
+    in z (padded to 15 layers), seed 7, one lattice on the pass kernels.  The
+    tensor uses the far-field form beyond 32 cells (tensor_far_radius = 32),
+    which is exact to about 1e-12 per term there and makes the setup seconds
+    instead of the ~10 minutes of exact 64-term sums over 441 images."""
+    t0 = time.perf_counter()
+    lat = M.Lattice(M.Config.defaults(precision=32, tensor_far_radius=32, **SLAB), device=local)
+    lat.build_demag(CACHE_DIR)
+    setup = time.perf_counter() - t0
+    T = [800.0 * 0.9 ** k for k in range(3)]
+    lat.run_sweeps(T[0], 0, 0, 20)
+    lat.run_sweeps(T[1], 1, 0, sweeps)
+    ms = lat.last_run_ms()
+    prof = lat.profile_sweeps(T[2], 2, 0, 20)
+    n = SLAB["nx"] * SLAB["ny"] * SLAB["nz"]
+    lat.close()
+    return {"value": n * sweeps / (ms / 1e3), "unit": UNIT, "cells": n, "sweeps": sweeps,
+            "us_per_sweep": 1e3 * ms / sweeps, "demag_us_per_sweep": 1e3 * prof[0] / 20,
+            "metropolis_us_per_sweep": 1e3 * prof[1] / 20, "tensor_setup_s": setup,
+            "tensor": "exact 64-term sums within 32 cells, far-field expansion beyond"}
+
+
 def relax_line(M, local):
     """Gradient and relaxation on the 256x256x1 film in FP64: a short anneal
     (34 stages of 100 sweeps, seed 11), then projected steepest descent to a
@@ -392,9 +430,10 @@ def run_ours(args):
     per_launch_ms = fam[dom] / launches
     bytes_launch = kbytes[dom] / launches
     peak, peak_kind = measured_peaks()
+    traffic, tshape = ncu_traffic(dom, shape)
     achieved = bytes_launch / (per_launch_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": ncu_traffic(dom, shape),
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic, "traffic_shape": tshape,
                 "algorithmic_bytes_per_launch": bytes_launch, "avg_ms_per_launch": per_launch_ms,
                 "kernel_ms_per_batch_sweep": fam, "launch_shape": shape,
                 "bytes_model": "per replica: x passes 3*4*N real + 3*8*N_h complex; column pass 2*3*8*N_h "
@@ -430,6 +469,7 @@ def run_ours(args):
                      "batched_fp32_over_fp64": value / world / fp64, "single_fp32_over_fp64": single_v / fp64}
 
     farm_line = None if args.no_farm else pt_farm(M, local, 2000)
+    slab = None if args.no_slab else slab_line(M, local, 200)
     relax = None if args.no_relax else relax_line(M, local)
 
     line = {
@@ -449,6 +489,7 @@ def run_ours(args):
                                 "film_engine_phase_us": phases},
         "fp64_plain": fp64_line,
         "pt_farm_fp32": farm_line,
+        "slab_512x512x8_fp32": slab,
         "relax": relax,
         "setup_s": setup_s,
         "autotune": {"candidates": tune_n, "best_ms_per_batch_sweep": tune_ms, "seconds": tune_s,
@@ -481,8 +522,9 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-farm", action="store_true", help="skip the parallel-tempering farm line")
     ap.add_argument("--no-relax", action="store_true", help="skip the gradient / relaxation line")
+    ap.add_argument("--no-slab", action="store_true", help="skip the 3-D slab line")
     ap.add_argument("--launch-shape", default="",
-                    help="eight comma-separated values of a launch shape to use instead of autotuning")
+                    help="nine comma-separated values of a launch shape to use instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

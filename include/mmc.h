@@ -97,6 +97,10 @@ typedef struct mmc_config {
   char tensor_cache[1024];                 /* directory for the demag tensor cache ("" = off) */
   int sweep_engine;                        /* enum mmc_engine, default MMC_ENGINE_AUTO */
   int fused_band;                          /* rows per CTA of the fused film engine, 0 = auto */
+  int tensor_far_radius;                   /* 0 (default): every tensor term by the exact 64-term
+                                              sum, as the reference; R >= 12: image offsets at least
+                                              R cells away by the far-field expansion (more accurate
+                                              there, and far cheaper; see mmc_build_demag) */
 } mmc_config;
 
 typedef struct mmc_observables {
@@ -150,7 +154,14 @@ int mmc_get_m(mmc_handle* h, double* mx, double* my, double* mz);
  * With a non-empty cache_dir (the -tensorcache= flag) the tensor is read from /
  * written to cache_<nxp>_<nyp>_<nzp>-<dx>_<dy>_<dz>-<pbcx>_<pbcy>_<pbcz>.ovf
  * in the reference's raw layout.  Called implicitly by the first call that
- * needs it when cal_demag_flag is set. */
+ * needs it when cal_demag_flag is set.
+ * With tensor_far_radius = R > 0, every image offset whose cell-centre
+ * distance is at least R times the largest cell side is summed with the
+ * far-field expansion of the 64-term sum (derivatives of 1/r up to order 8,
+ * truncation error O((d/r)^8): 4e-13 of the term at 32 cells against
+ * 60-digit evaluations), where the exact FP64 sum loses (r/d)^6 x 1e-16 to
+ * cancellation (1e-6 at 32 cells, 0.2 at 300 cells).  Such a tensor is cached
+ * under the reference's name with a "_far<R>" suffix. */
 int mmc_build_demag(mmc_handle* h, const char* cache_dir);
 
 /* The real-space tensor: 6 blocks (xx,xy,xz,yy,yz,zz) of nxp*nyp*nzp doubles,
@@ -319,24 +330,26 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
  * passes, the band of the film row kernel (0 when sweeps use one kernel per
  * pass), and the Metropolis form: 0 one launch per colour, 1 both colours of
  * a film in one tile launch, 2 one vectorised launch per colour (films with
- * nx a multiple of 4), and whether the pass kernels expand their transforms in
- * line (1) or call them out of line (0). */
-int mmc_batch_launch_shape(mmc_batch* b, int out[8]);
+ * nx a multiple of 4), whether the pass kernels expand their transforms in
+ * line (1) or call them out of line (0), and whether the column passes
+ * transform in place reading the tensor from global memory (1). */
+int mmc_batch_launch_shape(mmc_batch* b, int out[9]);
 /* Autotuner: times each launch shape this batch can run with (the film row
  * kernel with each band that fits; the pass kernels with 1-16 rows per x-pass
- * CTA and 1-8 kx columns per column-pass tile, each with the transforms in
- * and out of line and every Metropolis form) for `sweeps` sweeps from the
+ * CTA and 1-8 kx columns per column-pass tile, then -- one dimension at a
+ * time from the fastest so far -- the transforms in and out of line, the
+ * in-place column passes, every Metropolis form) for `sweeps` sweeps from the
  * current state, keeps the fastest and restores m and the acceptance
  * counters.  Every shape gives bit-identical results, so the choice changes
  * only the speed.  best_ms_per_sweep and candidates may be NULL.  No
  * counterpart in the reference, whose block shape is fixed in the source
  * (src/main.cu:275-286). */
 int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int* candidates);
-/* Sets the launch shape (the eight values of mmc_batch_launch_shape), e.g. one
+/* Sets the launch shape (the nine values of mmc_batch_launch_shape), e.g. one
  * an earlier autotune chose.  Values outside the ranges the autotuner tries,
  * or a row-kernel band that does not fit this batch, are rejected.  Results do
  * not depend on the shape.  No counterpart in the reference. */
-int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[8]);
+int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[9]);
 
 /* Replica farms: batches of different lattice sizes advanced together.  One
  * call runs nsweeps sweeps of every batch (each with its own temperatures,
@@ -368,6 +381,14 @@ int mmc_ovf_read(const char* path, int nx, int ny, int nz, double dx, double dy,
 int mmc_ovf_write(const char* path, int nx, int ny, int nz, double dx, double dy, double dz,
                   const double* mx, const double* my, const double* mz, int format,
                   const char* title);
+
+/* Test hook of failure detection (no counterpart in the reference): runs one
+ * CTA that waits at a device barrier for an arrival that never comes, with a
+ * budget of spin_limit polls (1 .. 2^24); the wait runs out, the kernel
+ * records the timeout and returns, and *status receives MMC_ERR_TIMEOUT (or
+ * MMC_OK if the wait had completed).  The device stays usable afterwards --
+ * this is how the film engine's barriers report MMC_ERR_TIMEOUT. */
+int mmc_selftest_barrier_timeout(int device, long long spin_limit, int* status);
 
 /* Test hook (no counterpart in the reference, whose random pools came from
  * cuRAND's host API, src/main.cu:351-385): evaluates Philox4x32-10 on device

@@ -42,10 +42,13 @@ __device__ __forceinline__ unsigned long long global_ns() {
 
 // Bounded grid barrier.  Thread 0 publishes the CTA's arrival with a release
 // reduction (no round trip) and polls the counter with acquire loads.
-__device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned int& target, int* flag_smem) {
+// spin_limit: polls before the wait gives up (the default is seconds, far
+// beyond any legitimate wait); expect: arrivals this barrier waits for.
+__device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned int& target, int* flag_smem,
+                                          unsigned long long spin_limit = 1ull << 24, unsigned int expect = 0) {
   __syncthreads();
   if (threadIdx.x == 0) {
-    target += gridDim.x;
+    target += expect ? expect : gridDim.x;
     __threadfence();
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&bar->count), "r"(1u) : "memory");
     unsigned long long spins = 0;
@@ -54,7 +57,7 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned int& target
       unsigned int v;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(&bar->count) : "memory");
       if ((int)(v - target) >= 0) break;
-      if (++spins > (1ull << 24)) {  // seconds, far beyond any legitimate wait
+      if (++spins > spin_limit) {
         atomicExch(&bar->err, 1);
         ok = 0;
         break;

@@ -103,6 +103,7 @@ const KeyDef kKeys[] = {
     KD(rand_block_size, K_INT, true), KD(cal_demag_flag, K_BOOL, true),
     // optional keys of this library
     KD(use_reference_pi, K_BOOL, false), KD(tensor_cache, K_STR, false), KD(fused_band, K_INT, false),
+    KD(tensor_far_radius, K_INT, false),
 };
 #undef KD
 
@@ -151,6 +152,8 @@ int config_validate(const mmc_config* c) {
   if (c->ovf_format < 0 || c->ovf_format > 2) return fail(MMC_ERR_CONFIG, "bad ovf_format");
   if (c->sweep_engine < 0 || c->sweep_engine > 2) return fail(MMC_ERR_CONFIG, "bad sweep_engine");
   if (c->fused_band < 0 || c->fused_band > 60) return fail(MMC_ERR_CONFIG, "fused_band must be in [0, 60]");
+  if (c->tensor_far_radius != 0 && (c->tensor_far_radius < 12 || c->tensor_far_radius > 1000000))
+    return fail(MMC_ERR_CONFIG, "tensor_far_radius must be 0 (off) or in [12, 1e6] cells");
   if (c->circle_per_stage < 0) return fail(MMC_ERR_CONFIG, "circle_per_stage must be >= 0");
   if (c->terminal_output_period < 1 || c->energy_output_period < 1 || c->ms_output_period < 1)
     return fail(MMC_ERR_CONFIG, "output periods must be >= 1");

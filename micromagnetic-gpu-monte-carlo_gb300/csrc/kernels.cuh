@@ -157,7 +157,7 @@ enum : int { PASS_FWD = 1, PASS_MUL = 2, PASS_INV = 4, PASS_SYM = 8 };
 template <typename T, bool INL>
 __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long nspec, const C<T>* __restrict__ khat,
                            int hx, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
-                           int flags, T inv_n, int tx, long long s_rstride) {
+                           int flags, T inv_n, int tx, long long s_rstride, int lean) {
   using V = C<T>;
   S += blockIdx.z * s_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -168,16 +168,19 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
   const int ntx = min(tx, hx - kx0);
   const long long pbase = (long long)blockIdx.y * plane_stride + kx0;
   const int nlines = ncomp * ntx;
+  // lean (warp-level transforms only): one buffer, transformed in place, and
+  // the tensor read from global memory in the product -- a third of the
+  // shared memory, so more CTAs fit on an SM
   V* bufA = tw + ((p.tw_total + 1) & ~1);
-  V* bufB = bufA + (long long)ncomp * tx * stride;
-  V* ktile = bufB + (long long)ncomp * tx * stride;  // [comp][pos][t] when PASS_MUL
+  V* bufB = lean ? bufA : bufA + (long long)ncomp * tx * stride;
+  V* ktile = bufB + (long long)ncomp * tx * stride;  // [comp][pos][t] when PASS_MUL and not lean
   load_twiddles<T>(p, tw);
   // the tensor tile goes to shared memory asynchronously while the forward
   // transform runs (16-byte copies when the tile rows are 16-byte aligned)
-  const bool kasync = (flags & PASS_MUL) && (((long long)ntx * sizeof(V)) % 16 == 0) && ((kx0 * sizeof(V)) % 16 == 0) &&
+  const bool kasync = !lean && (flags & PASS_MUL) && (((long long)ntx * sizeof(V)) % 16 == 0) && ((kx0 * sizeof(V)) % 16 == 0) &&
                       ((plane_stride * sizeof(V)) % 16 == 0) && ((pos_stride * sizeof(V)) % 16 == 0);
   const FastDiv dt((uint32_t)ntx);  // index arithmetic without run-time division
-  if (flags & PASS_MUL) {
+  if ((flags & PASS_MUL) && !lean) {
     const int per = (int)(ntx * sizeof(V) / 16);
     if (kasync) {
       const FastDiv dper((uint32_t)per);
@@ -198,17 +201,18 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
     }
   }
   const int total = ncomp * L * ntx;
-  for (int base = threadIdx.x; base < total; base += 4 * blockDim.x) {
-    V v[4];
+  constexpr int LB = 8;  // loads in flight per thread
+  for (int base = threadIdx.x; base < total; base += LB * blockDim.x) {
+    V v[LB];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < LB; ++u) {
       const int idx = base + u * blockDim.x;
       const int rest = dt.div(idx), t = idx - rest * ntx;
       const int c = p.dn.div(rest), pos = rest - c * L;
       v[u] = (idx < total && pos < load_lim) ? S[c * nspec + pbase + pos * pos_stride + t] : cmk<V>(0, 0);
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < LB; ++u) {
       const int idx = base + u * blockDim.x;
       if (idx < total) {
         const int rest = dt.div(idx), t = idx - rest * ntx;
@@ -232,8 +236,8 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
     __syncthreads();
     for (int idx = threadIdx.x; idx < L * ntx; idx += blockDim.x) {
       const int pos = dt.div(idx), t = idx - pos * ntx;
-      const V* kk = ktile + (long long)pos * ntx + t;
-      const long long ks = (long long)L * ntx;
+      const V* kk = lean ? khat + pbase + pos * pos_stride + t : ktile + (long long)pos * ntx + t;
+      const long long ks = lean ? nspec : (long long)L * ntx;
       V kxx = kk[0], kxy = kk[ks], kxz = kk[2 * ks];
       V kyy = kk[3 * ks], kyz = kk[4 * ks], kzz = kk[5 * ks];
       if (flags & PASS_SYM) kxx.y = kxy.y = kxz.y = kyy.y = kyz.y = kzz.y = (T)0;
@@ -1043,6 +1047,9 @@ __global__ void k_khat_store(long long count, const double2* __restrict__ src, C
 inline size_t x_pass_smem(const FftPlan& p, int lines_per_row, int rows, size_t csize) {
   return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)rows * lines_per_row * p.n) * csize;
 }
+inline size_t col_pass_smem_lean(const FftPlan& p, int ncomp, int tx, size_t csize) {
+  return ((size_t)((p.tw_total + 1) & ~1) + (size_t)ncomp * tx * (p.n + 1)) * csize;
+}
 inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize, bool mul) {
   return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)ncomp * tx * (p.n + 1) + (mul ? 6 * (size_t)p.n * tx : 0)) *
          csize;
@@ -1080,12 +1087,14 @@ template <typename T>
 cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, const C<T>* khat, int hx,
                          int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
                          int flags, T inv_n, int tx, int threads, cudaStream_t st, int nrep = 1,
-                         long long s_rstride = 0, bool inl = false) {
-  size_t sm = col_pass_smem(p, ncomp, tx, sizeof(C<T>), (flags & PASS_MUL) != 0);
+                         long long s_rstride = 0, bool inl = false, bool lean = false) {
+  lean = lean && p.warp_a != 0;  // in-place transforms exist for the warp path only
+  size_t sm = lean ? col_pass_smem_lean(p, ncomp, tx, sizeof(C<T>))
+                   : col_pass_smem(p, ncomp, tx, sizeof(C<T>), (flags & PASS_MUL) != 0);
   dim3 grid((hx + tx - 1) / tx, planes, nrep);
   auto kern = inl ? k_col_pass<T, true> : k_col_pass<T, false>;
   kern<<<grid, threads, sm, st>>>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
-                                           store_lim, flags, inv_n, tx, s_rstride);
+                                           store_lim, flags, inv_n, tx, s_rstride, lean ? 1 : 0);
   return cudaGetLastError();
 }
 
@@ -1113,15 +1122,15 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
   if (g.nzp == 1) {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny,
                             PASS_FWD | PASS_MUL | PASS_INV | mul_flags, inv_n, tun.col_tx, tun.col_threads, st, nrep,
-                            sr, tun.fft_inline != 0));
+                            sr, tun.fft_inline != 0, tun.col_lean != 0));
   } else {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.ny, g.nyp, PASS_FWD, inv_n, tun.col_tx,
-                            tun.col_threads, st, nrep, sr, tun.fft_inline != 0));
+                            tun.col_threads, st, nrep, sr, tun.fft_inline != 0, tun.col_lean != 0));
     MMC_TRY(run_col_pass<T>(pz, 3, S, ns, K, g.hx, g.nyp, ystride, yplane, g.nz, g.nz,
                             PASS_FWD | PASS_MUL | PASS_INV | mul_flags, inv_n, tun.col_tx_z, tun.col_threads, st, nrep,
-                            sr, tun.fft_inline != 0));
+                            sr, tun.fft_inline != 0, tun.col_lean != 0));
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.nyp, g.ny, PASS_INV, inv_n, tun.col_tx,
-                            tun.col_threads, st, nrep, sr, tun.fft_inline != 0));
+                            tun.col_threads, st, nrep, sr, tun.fft_inline != 0, tun.col_lean != 0));
   }
   if (ev) MMC_TRY(cudaEventRecord(ev[2], st));
   const int rpc = tun.x_rows_per_cta;
@@ -1232,7 +1241,8 @@ cudaError_t launch_col_pass_2d(const Geom& g, const FftPlan& py, const DemagTuni
   const T inv_n = (T)(1.0 / (double)g.np);
   return run_col_pass<T>(py, 3, reinterpret_cast<C<T>*>(spec), g.nspec, reinterpret_cast<const C<T>*>(khat), g.hx, 1,
                          (long long)g.nyp * g.hxp, g.hxp, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV, inv_n,
-                         tun.col_tx, tun.col_threads, st, nrep, 3 * g.nspec, tun.fft_inline != 0);
+                         tun.col_tx, tun.col_threads, st, nrep, 3 * g.nspec, tun.fft_inline != 0,
+                         tun.col_lean != 0);
 }
 template <typename T>
 cudaError_t launch_prepare(int max_dyn_smem) {

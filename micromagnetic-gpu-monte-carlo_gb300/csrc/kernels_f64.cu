@@ -22,6 +22,21 @@ int energy_partials_count(const Geom& g) { return energy_blocks(g); }
 size_t grid_barrier_bytes() { return sizeof(GridBarrier); }
 int grid_barrier_error(const GridBarrier* b) { return b->err; }
 
+// Failure-detection self-test: one CTA waits at a grid barrier for one more
+// arrival than the grid has, so the wait can only end by its poll budget; the
+// kernel records the timeout in the barrier's error word and returns.
+static __global__ void k_barrier_timeout_selftest(GridBarrier* bar, unsigned long long spin_limit, int* ok_out) {
+  __shared__ int flag;
+  unsigned int target = 0;
+  const bool ok = grid_sync(bar, target, &flag, spin_limit, gridDim.x + 1);
+  if (threadIdx.x == 0) *ok_out = ok ? 1 : 0;
+}
+
+cudaError_t launch_barrier_timeout_selftest(void* bar, unsigned long long spin_limit, int* ok_out) {
+  k_barrier_timeout_selftest<<<1, 32>>>(reinterpret_cast<GridBarrier*>(bar), spin_limit, ok_out);
+  return cudaGetLastError();
+}
+
 // Forward transform of the six real tensor blocks k6[c][z][y][x] (padded
 // grid) into spec64[c][kz][ky][kx] (src/main.cu:593-642 ran cuFFT D2Z here).
 cudaError_t launch_tensor_fft(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,

@@ -120,6 +120,7 @@ struct DemagTuning {
   int col_threads;
   int mc_form;     // MC_FORM_*
   int fft_inline;  // 1: the pass kernels expand the warp-level transforms in line
+  int col_lean;    // 1: column passes transform in place and read K^ from global memory
 };
 
 // Device counters read by the sweep kernels: [stage, sweep].
@@ -185,8 +186,11 @@ template <typename T>
 cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat, cudaStream_t st);
 
 // FP64 setup: the Newell tensor (newell.cu) and its forward transform.
+// far_r2 > 0: image offsets with squared distance >= far_r2 (m^2) use the
+// far-field expansion (newell_far.h).
 cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz,
-                          double pi, double* k6, int px0, int px1, int finalize, cudaStream_t st);
+                          double pi, double* k6, int px0, int px1, int finalize, cudaStream_t st,
+                          double far_r2 = 0.0);
 cudaError_t launch_tensor_fft(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                               const DemagTuning& tun, const double* k6, double2* spec64, cudaStream_t st);
 cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st);
@@ -257,5 +261,7 @@ template <typename T>
 cudaError_t launch_pt_swap(const PtDevice& pt, const McParams* params, McCoef<T>* coef, const double* red,
                            cudaStream_t st);
 int grid_barrier_error(const GridBarrier* host_copy);
+// Test hook: a barrier wait that can only run out (see mmc_selftest_barrier_timeout).
+cudaError_t launch_barrier_timeout_selftest(void* bar, unsigned long long spin_limit, int* ok_out);
 
 }  // namespace mmc

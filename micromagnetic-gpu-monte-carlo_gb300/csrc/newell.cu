@@ -16,6 +16,7 @@
 
 #include "mmc_internal.h"
 #include "mmc_math.h"
+#include "newell_far.h"
 
 namespace mmc {
 
@@ -56,9 +57,11 @@ __device__ __forceinline__ int wrap_offset(int x, int n) { return (x + (n + 1) /
 // point.  The sums live in k6 between launches, so splitting the image range
 // over several launches keeps the reference's summation order exactly; the
 // launch with `finalize` divides by -4 pi dx dy dz.
+// far_r2 > 0: image offsets with |r|^2 >= far_r2 use the far-field expansion
+// (newell_far.h) in place of the 64 terms.
 __global__ void __launch_bounds__(128) k_newell(int nxp, int nyp, int nzp, double dx, double dy, double dz, int Px,
                                                 int Py, int Pz, int px0, int px1, int finalize, double pi,
-                                                double* __restrict__ k6, long long np) {
+                                                double far_r2, double* __restrict__ k6, long long np) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= np) return;
   const int x = (int)(i % nxp), y = (int)((i / nxp) % nyp), z = (int)(i / ((long long)nxp * nyp));
@@ -76,6 +79,20 @@ __global__ void __launch_bounds__(128) k_newell(int nxp, int nyp, int nzp, doubl
     for (int py = -Py; py <= Py; py++)
       for (int pz = -Pz; pz <= Pz; pz++) {
         const int ix = idx_x + px * nxp, iy = idx_y + py * nyp, iz = idx_z + pz * nzp;
+        if (far_r2 > 0.0) {
+          const double X = ix * dx, Y = iy * dy, Z = iz * dz;
+          if (X * X + Y * Y + Z * Z >= far_r2) {
+            double r[6];
+            mmcm::newell_far_raw(X, Y, Z, dx, dy, dz, r);
+            kxx += r[0];
+            kxy += r[1];
+            kxz += r[2];
+            kyy += r[3];
+            kyz += r[4];
+            kzz += r[5];
+            continue;
+          }
+        }
 #pragma unroll 1
         for (int bits = 0; bits < 64; ++bits) {
           // bit order matches the nested FOR01 loops ikx, iky, ikz, ilx, ily, ilz
@@ -119,10 +136,10 @@ __global__ void __launch_bounds__(128) k_newell(int nxp, int nyp, int nzp, doubl
 }  // namespace
 
 cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz, double pi,
-                          double* k6, int px0, int px1, int finalize, cudaStream_t st) {
+                          double* k6, int px0, int px1, int finalize, cudaStream_t st, double far_r2) {
   const int threads = 128;
-  k_newell<<<(unsigned)((g.np + threads - 1) / threads), threads, 0, st>>>(g.nxp, g.nyp, g.nzp, dx, dy, dz, Px, Py,
-                                                                          Pz, px0, px1, finalize, pi, k6, g.np);
+  k_newell<<<(unsigned)((g.np + threads - 1) / threads), threads, 0, st>>>(
+      g.nxp, g.nyp, g.nzp, dx, dy, dz, Px, Py, Pz, px0, px1, finalize, pi, far_r2, k6, g.np);
   return cudaGetLastError();
 }
 

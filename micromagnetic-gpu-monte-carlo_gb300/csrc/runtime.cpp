@@ -192,6 +192,7 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   // autotuner tries every form)
   t.mc_form = csize == 8 && nrep >= 8 && mc_quad_eligible(g) ? MC_FORM_QUAD : MC_FORM_SCALAR;
   t.fft_inline = 0;
+  t.col_lean = 0;
   return t;
 }
 
@@ -577,11 +578,21 @@ int profile_sweeps_impl(mmc_handle* h, double T_K, long long stage, long long sw
   return MMC_OK;
 }
 
+// Squared switch distance of the far-field tensor terms (0 = off).
+double far_r2(const mmc_config& c) {
+  if (c.tensor_far_radius <= 0) return 0.0;
+  const double d = std::max(c.dx, std::max(c.dy, c.dz)) * (double)c.tensor_far_radius;
+  return d * d;
+}
+
 std::string cache_name(const mmc_handle* h) {
   char b[256];
-  std::snprintf(b, sizeof b, "cache_%d_%d_%d-%g_%g_%g-%d_%d_%d.ovf", h->g.nxp, h->g.nyp, h->g.nzp, h->cfg.dx,
+  std::snprintf(b, sizeof b, "cache_%d_%d_%d-%g_%g_%g-%d_%d_%d", h->g.nxp, h->g.nyp, h->g.nzp, h->cfg.dx,
                 h->cfg.dy, h->cfg.dz, h->cfg.pbc_x, h->cfg.pbc_y, h->cfg.pbc_z);
-  return b;
+  std::string name = b;
+  // a tensor with far-field terms is not the reference's: keep it apart
+  if (h->cfg.tensor_far_radius > 0) name += "_far" + std::to_string(h->cfg.tensor_far_radius);
+  return name + ".ovf";
 }
 
 bool dir_exists(const std::string& d) {
@@ -658,7 +669,8 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
           break;
         }
         const int px1 = std::min(Px, px0 + slab - 1);
-        cudaError_t e = launch_newell(g, c.dx, c.dy, c.dz, Px, Py, Pz, pi_of(&c), k6, px0, px1, px1 == Px, h->st);
+        cudaError_t e = launch_newell(g, c.dx, c.dy, c.dz, Px, Py, Pz, pi_of(&c), k6, px0, px1, px1 == Px, h->st,
+                                      far_r2(c));
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
         if (e != cudaSuccess) {
           status = fail(MMC_ERR_CUDA, std::string("tensor build: ") + cudaGetErrorString(e));
@@ -1396,54 +1408,9 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     int rows_band;
     DemagTuning tun;
   };
-  std::vector<Cand> cands;
   const Geom& g = h->g;
   const size_t cs = 2 * h->tsize;
   const DemagTuning base = choose_tuning(g, h->px.p, h->py.p, h->pz.p, cs, h->nsm, b->R);
-  if (h->cfg.cal_demag_flag)
-    for (int bd : b->row_bands) cands.push_back({bd, base});
-  cands.push_back({0, base});
-  if (h->cfg.cal_demag_flag) {
-    const long long rows = (long long)g.ny * g.nz;
-    for (int r : {1, 2, 4, 8, 16}) {
-      if (r > rows || x_pass_smem(h->px.p, r, cs) > smem_limit()) continue;
-      for (int tx : {1, 2, 4, 8}) {
-        if (tx > g.hx || col_pass_smem(h->py.p, tx, cs) > smem_limit()) continue;
-        if (r == base.x_rows_per_cta && tx == base.col_tx) continue;
-        DemagTuning t = base;
-        t.x_rows_per_cta = r;
-        t.col_tx = tx;
-        t.col_threads = col_threads_for(g, h->py.p, h->pz.p, tx, t.col_tx_z);
-        cands.push_back({0, t});
-      }
-    }
-  }
-  // the in-line transforms for every pass-kernel shape
-  {
-    const size_t nk = cands.size();
-    for (size_t i = 0; i < nk; ++i)
-      if (cands[i].rows_band == 0) {
-        Cand c2 = cands[i];
-        c2.tun.fft_inline = 1 - c2.tun.fft_inline;
-        cands.push_back(c2);
-      }
-  }
-  // the other Metropolis forms for every pass-kernel shape
-  {
-    std::vector<int> forms;
-    if (mc_quad_eligible(g)) forms.push_back(MC_FORM_QUAD);
-    if (mc_tile_eligible(g)) forms.push_back(MC_FORM_TILE);
-    forms.push_back(MC_FORM_SCALAR);
-    const size_t nk = cands.size();
-    for (size_t i = 0; i < nk; ++i)
-      if (cands[i].rows_band == 0)
-        for (int f : forms)
-          if (f != cands[i].tun.mc_form) {
-            Cand c2 = cands[i];
-            c2.tun.mc_form = f;
-            cands.push_back(c2);
-          }
-  }
   const size_t mbytes = (size_t)b->R * 3 * g.n * h->tsize;
   void* saved = nullptr;
   CU(cudaMalloc(&saved, mbytes));
@@ -1452,13 +1419,17 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(acc0.data(), b->acc, b->R * sizeof(unsigned long long), cudaMemcpyDeviceToHost, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
-  int best = -1;
-  float best_t = 0;
   int status = MMC_OK;
-  for (size_t i = 0; i < cands.size() && e == cudaSuccess && status == MMC_OK; ++i) {
-    if (cands[i].rows_band > 0 && (status = batch_alloc_rows(b)) != MMC_OK) break;
-    b->rows_band = cands[i].rows_band;
-    b->tun = cands[i].tun;
+  int tried = 0;
+  Cand best{0, base};
+  float best_t = -1;
+  // times one candidate from the saved state; keeps it when it is the fastest
+  auto trial = [&](const Cand& cd) {
+    if (e != cudaSuccess || status != MMC_OK) return;
+    if (cd.rows_band > 0 && (status = batch_alloc_rows(b)) != MMC_OK) return;
+    ++tried;
+    b->rows_band = cd.rows_band;
+    b->tun = cd.tun;
     SweepCounters c0{0, 0};
     e = cudaMemcpyAsync(b->m, saved, mbytes, cudaMemcpyDeviceToDevice, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st);
@@ -1470,14 +1441,64 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[1]);
     float ms = 0;
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
-    if (e == cudaSuccess && (best < 0 || ms < best_t)) {
-      best = (int)i;
+    if (e == cudaSuccess && (best_t < 0 || ms < best_t)) {
+      best = cd;
       best_t = ms;
     }
+  };
+  // coordinate search: the pass-kernel tiling first, then one dimension at a
+  // time from the best so far; the row kernel bands are whole alternatives
+  trial({0, base});
+  if (h->cfg.cal_demag_flag) {
+    const long long rows = (long long)g.ny * g.nz;
+    for (int r : {1, 2, 4, 8, 16}) {
+      if (r > rows || x_pass_smem(h->px.p, r, cs) > smem_limit()) continue;
+      for (int tx : {1, 2, 4, 8}) {
+        if (tx > g.hx || col_pass_smem(h->py.p, tx, cs) > smem_limit()) continue;
+        if (r == base.x_rows_per_cta && tx == base.col_tx) continue;
+        DemagTuning t = base;
+        t.x_rows_per_cta = r;
+        t.col_tx = tx;
+        t.col_threads = col_threads_for(g, h->py.p, h->pz.p, tx, t.col_tx_z);
+        trial({0, t});
+      }
+    }
+    Cand c = best;
+    c.tun.fft_inline = 1 - c.tun.fft_inline;
+    trial(c);
+    // in-place column passes with the full and half thread count
+    if (h->py.p.warp_a) {
+      for (int half = 0; half < 2; ++half) {
+        Cand d = best;
+        d.tun.col_lean = 1;
+        if (half) d.tun.col_threads = std::max(64, best.tun.col_threads / 2);
+        if (half && d.tun.col_threads == best.tun.col_threads) continue;
+        trial(d);
+      }
+    }
   }
-  if (e == cudaSuccess && best >= 0) {
-    b->rows_band = cands[best].rows_band;
-    b->tun = cands[best].tun;
+  {
+    std::vector<int> forms;
+    if (mc_quad_eligible(g)) forms.push_back(MC_FORM_QUAD);
+    if (mc_tile_eligible(g)) forms.push_back(MC_FORM_TILE);
+    forms.push_back(MC_FORM_SCALAR);
+    const Cand pass_best = best;
+    for (int f : forms)
+      if (f != pass_best.tun.mc_form) {
+        Cand c = pass_best;
+        c.tun.mc_form = f;
+        trial(c);
+      }
+  }
+  if (h->cfg.cal_demag_flag)
+    for (int bd : b->row_bands) {
+      Cand c = best;
+      c.rows_band = bd;
+      trial(c);
+    }
+  if (e == cudaSuccess && status == MMC_OK && best_t >= 0) {
+    b->rows_band = best.rows_band;
+    b->tun = best.tun;
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->m, saved, mbytes, cudaMemcpyDeviceToDevice, h->st);
   if (e == cudaSuccess)
@@ -1490,7 +1511,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   if (status != MMC_OK) return status;
   CU(e);
   if (best_ms) *best_ms = best_t / sweeps;
-  if (ncand) *ncand = (int)cands.size();
+  if (ncand) *ncand = tried;
   return MMC_OK;
 }
 
@@ -1777,6 +1798,29 @@ int mmc_demag_apply_static(mmc_handle* h, const void* mdev, void* hdev, void* st
   return MMC_OK;
 }
 
+int mmc_selftest_barrier_timeout(int device, long long spin_limit, int* status) {
+  if (!status || spin_limit < 1 || spin_limit > (1ll << 24)) return fail(MMC_ERR_INVALID, "bad argument");
+  CU(cudaSetDevice(device));
+  void* bar = nullptr;
+  int* ok = nullptr;
+  CU(cudaMalloc(&bar, grid_barrier_bytes()));
+  cudaError_t e = cudaMalloc(&ok, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(bar, 0, grid_barrier_bytes());
+  if (e == cudaSuccess) e = cudaMemset(ok, 0xff, sizeof(int));
+  if (e == cudaSuccess) e = launch_barrier_timeout_selftest(bar, (unsigned long long)spin_limit, ok);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  std::vector<unsigned char> hb(grid_barrier_bytes());
+  int ok_host = -1;
+  if (e == cudaSuccess) e = cudaMemcpy(hb.data(), bar, hb.size(), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&ok_host, ok, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(bar);
+  if (ok) cudaFree(ok);
+  CU(e);
+  const bool timed_out = grid_barrier_error(reinterpret_cast<const GridBarrier*>(hb.data())) != 0 && ok_host == 0;
+  *status = timed_out ? MMC_ERR_TIMEOUT : MMC_OK;
+  return MMC_OK;
+}
+
 int mmc_selftest_philox(int device, long long n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out,
                         uint32_t* out_curand) {
   if (n < 0 || (n > 0 && !ctr)) return fail(MMC_ERR_INVALID, "bad argument");
@@ -2037,12 +2081,12 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
   return MMC_OK;
 }
 
-int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[8]) {
+int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[9]) {
   if (!b || !shape) return fail(MMC_ERR_INVALID, "null argument");
   mmc_handle* h = b->base;
   const Geom& g = h->g;
   const size_t cs = 2 * h->tsize;
-  DemagTuning t{shape[0], shape[1], shape[2], shape[3], shape[4], shape[6], shape[7]};
+  DemagTuning t{shape[0], shape[1], shape[2], shape[3], shape[4], shape[6], shape[7], shape[8]};
   const int band = shape[5];
   auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
   if (!pow2(t.x_rows_per_cta) || t.x_rows_per_cta > 16 || x_pass_smem(h->px.p, t.x_rows_per_cta, cs) > smem_limit() ||
@@ -2051,7 +2095,7 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[8]) {
       (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
       t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_QUAD ||
       (t.mc_form == MC_FORM_TILE && !mc_tile_eligible(g)) || (t.mc_form == MC_FORM_QUAD && !mc_quad_eligible(g)) ||
-      (t.fft_inline != 0 && t.fft_inline != 1))
+      (t.fft_inline != 0 && t.fft_inline != 1) || (t.col_lean != 0 && t.col_lean != 1))
     return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
   if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())
     return fail(MMC_ERR_UNSUPPORTED, "row-kernel band not available for this batch");
@@ -2072,11 +2116,12 @@ int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int*
   return batch_autotune(b, sweeps, best_ms_per_sweep, candidates);
 }
 
-int mmc_batch_launch_shape(mmc_batch* b, int out[8]) {
+int mmc_batch_launch_shape(mmc_batch* b, int out[9]) {
   if (!b || !out) return fail(MMC_ERR_INVALID, "null argument");
   out[5] = b->rows_band;
   out[6] = b->tun.mc_form;
   out[7] = b->tun.fft_inline;
+  out[8] = b->tun.col_lean;
   out[0] = b->tun.x_rows_per_cta;
   out[1] = b->tun.x_threads;
   out[2] = b->tun.col_tx;

@@ -53,6 +53,7 @@ class Config(ctypes.Structure):
         ("tensor_cache", ctypes.c_char * 1024),
         ("sweep_engine", ctypes.c_int),
         ("fused_band", ctypes.c_int),
+        ("tensor_far_radius", ctypes.c_int),
     ]
 
     @classmethod
@@ -181,6 +182,8 @@ def lib(path=None):
         "mmc_farm_run_sweeps": (ctypes.c_int, [H, ctypes.c_longlong, ctypes.c_longlong, ctypes.c_longlong]),
         "mmc_farm_last_run_ms": (ctypes.c_int, [H, _dp]),
         "mmc_farm_request_stop": (None, [H]),
+        "mmc_selftest_barrier_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong,
+                                                        ctypes.POINTER(ctypes.c_int)]),
         "mmc_batch_request_stop": (None, [H]),
         "mmc_batch_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
         "mmc_batch_set_m": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
@@ -460,11 +463,11 @@ class Batch:
         return ms.value, n.value
 
     def set_launch_shape(self, shape):
-        arr = (ctypes.c_int * 8)(*[int(v) for v in shape])
+        arr = (ctypes.c_int * 9)(*[int(v) for v in shape])
         check(lib().mmc_batch_set_launch_shape(self.h, arr))
 
     def launch_shape(self):
-        out = (ctypes.c_int * 8)()
+        out = (ctypes.c_int * 9)()
         check(lib().mmc_batch_launch_shape(self.h, out))
         return tuple(out)
 

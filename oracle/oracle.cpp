@@ -26,6 +26,7 @@
 // the Philox-keyed proposals.  Elementary functions come from mmc_math.h so
 // that FP64 results can be compared bit for bit; compile with
 // -ffp-contract=off.
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <cstdint>
@@ -37,6 +38,7 @@
 
 #include "../include/mmc.h"
 #include "../micromagnetic-gpu-monte-carlo_gb300/csrc/mmc_math.h"
+#include "../micromagnetic-gpu-monte-carlo_gb300/csrc/newell_far.h"
 
 namespace {
 
@@ -104,13 +106,27 @@ int wrap_offset(int x, int n) { return (x + (n + 1) / 2 - 1) % n - (n + 1) / 2 +
 
 // ktensorCPU (src/demag_cu.cu:119-248) for one padded point; out = xx,xy,xz,yy,yz,zz.
 void newell_point(const Lat& L, double dx, double dy, double dz, double pi, int x, int y, int z,
-                  double out[6]) {
+                  double out[6], double far_r2 = 0.0) {
   int idx_x = wrap_offset(x, L.nxp), idx_y = wrap_offset(y, L.nyp), idx_z = wrap_offset(z, L.nzp);
   double kxx = 0, kxy = 0, kxz = 0, kyy = 0, kyz = 0, kzz = 0;
   for (int px = -L.P[0]; px <= L.P[0]; px++)
     for (int py = -L.P[1]; py <= L.P[1]; py++)
       for (int pz = -L.P[2]; pz <= L.P[2]; pz++) {
         int ix = idx_x + px * L.nxp, iy = idx_y + py * L.nyp, iz = idx_z + pz * L.nzp;
+        if (far_r2 > 0.0) {  // far-field form of this image's 64 terms (newell_far.h)
+          const double X = ix * dx, Y = iy * dy, Z = iz * dz;
+          if (X * X + Y * Y + Z * Z >= far_r2) {
+            double r[6];
+            mmcm::newell_far_raw(X, Y, Z, dx, dy, dz, r);
+            kxx += r[0];
+            kxy += r[1];
+            kxz += r[2];
+            kyy += r[3];
+            kyz += r[4];
+            kzz += r[5];
+            continue;
+          }
+        }
         for (int ikx = 0; ikx < 2; ikx++)
           for (int iky = 0; iky < 2; iky++)
             for (int ikz = 0; ikz < 2; ikz++)
@@ -332,6 +348,24 @@ int orc_padded_dims(const mmc_config* c, int out[3]) {
 }
 
 double orc_newell_f(double x, double y, double z) { return newell_f(x, y, z); }
+// Far-field form of the six 64-term sums of one image offset (newell_far.h).
+void orc_newell_far(double X, double Y, double Z, double dx, double dy, double dz, double out[6]) {
+  mmcm::newell_far_raw(X, Y, Z, dx, dy, dz, out);
+}
+// The exact six 64-term sums of one offset given in cells (before the -4 pi V division).
+void orc_newell_raw(int ix, int iy, int iz, double dx, double dy, double dz, double out[6]) {
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  for (int bits = 0; bits < 64; ++bits) {
+    const int ikx = (bits >> 5) & 1, iky = (bits >> 4) & 1, ikz = (bits >> 3) & 1;
+    const int ilx = (bits >> 2) & 1, ily = (bits >> 1) & 1, ilz = bits & 1;
+    const bool sign = ((ikx + iky + ikz + ilx + ily + ilz) % 2 == 0);
+    const double X = (ix + ikx - ilx) * dx, Y = (iy + iky - ily) * dy, Z = (iz + ikz - ilz) * dz;
+    const double v[6] = {newell_f(X, Y, Z), newell_g(X, Y, Z), newell_g(X, Z, Y),
+                         newell_f(Y, Z, X), newell_g(Y, Z, X), newell_f(Z, X, Y)};
+    for (int c = 0; c < 6; ++c) k[c] += sign ? v[c] : -v[c];
+  }
+  for (int c = 0; c < 6; ++c) out[c] = k[c];
+}
 double orc_newell_g(double x, double y, double z) { return newell_g(x, y, z); }
 
 void orc_math(int fn, const double* x, double* y, long n) {
@@ -367,7 +401,12 @@ int orc_newell_tensor(const mmc_config* c, double* k6) {
   for (long i = 0; i < np; ++i) {
     int x = (int)(i % L.nxp), y = (int)((i / L.nxp) % L.nyp), z = (int)(i / ((long)L.nxp * L.nyp));
     double o[6];
-    newell_point(L, c->dx, c->dy, c->dz, pi, x, y, z, o);
+    double fr2 = 0.0;
+    if (c->tensor_far_radius > 0) {
+      const double d = std::max(c->dx, std::max(c->dy, c->dz)) * (double)c->tensor_far_radius;
+      fr2 = d * d;
+    }
+    newell_point(L, c->dx, c->dy, c->dz, pi, x, y, z, o, fr2);
     for (int k = 0; k < 6; ++k) k6[k * np + i] = o[k];
   }
   return 0;

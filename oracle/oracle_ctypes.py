@@ -56,6 +56,8 @@ def lib():
         "orc_field": (ctypes.c_int, [C, ctypes.c_int, _dp, _dp, _dp]),
         "orc_energy": (ctypes.c_int, [C, _dp, _dp, _dp]),
         "orc_grad": (ctypes.c_int, [C, _dp, _dp, _dp, _dp]),
+        "orc_newell_far": (None, [ctypes.c_double] * 6 + [_dp]),
+        "orc_newell_raw": (None, [ctypes.c_int] * 3 + [ctypes.c_double] * 3 + [_dp]),
         "orc_sweeps": (ctypes.c_int, [C, _dp, ctypes.c_double, ctypes.c_longlong, ctypes.c_longlong,
                                       ctypes.c_longlong, _dp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int,
                                       ctypes.c_int]),
@@ -149,6 +151,20 @@ def energy(cfg, m, hd=None):
     out = np.zeros(9)
     hp = _p(np.ascontiguousarray(hd, dtype=np.float64)) if hd is not None else None
     lib().orc_energy(_c(cfg), _p(m), hp, _p(out))
+    return out
+
+
+def newell_far(X, Y, Z, dx, dy, dz):
+    """Far-field form of the six raw 64-term sums of one offset (metres)."""
+    out = np.zeros(6)
+    lib().orc_newell_far(X, Y, Z, dx, dy, dz, _p(out))
+    return out
+
+
+def newell_raw(ix, iy, iz, dx, dy, dz):
+    """The exact six raw 64-term sums of one offset in cells (FP64)."""
+    out = np.zeros(6)
+    lib().orc_newell_raw(ix, iy, iz, dx, dy, dz, _p(out))
     return out
 
 

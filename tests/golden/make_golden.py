@@ -8,6 +8,10 @@ newell_golden.json -- the reference's Newell potentials f, g (src/demag_cu.h:43-
     significant digits for a few small lattices.  This is an independent
     high-precision evaluation of the reference's own formulas; it needs mpmath
     (bundled with sympy) and runs in about a minute.
+newell_far_golden.json -- the six raw 64-term sums of single image offsets from
+    12 to 400 cells away, at 60 digits: the target of the far-field expansion
+    (csrc/newell_far.h), which FP64 evaluations of the sums cannot reach there.
+    `python tests/golden/make_golden.py --far` writes only this file.
 trajectory_fp64.npz -- a short FP64 Metropolis trajectory produced by the CPU
     oracle (oracle/oracle.cpp) on an 8x8x1 periodic film with demag: initial m,
     tensor, demag field, energies and m after 20 sweeps.  A regression pin for the
@@ -96,7 +100,41 @@ def tensor(nx, ny, nz, dx, dy, dz, pbc):
     return pad, out
 
 
+def raw_sums(ix, iy, iz, dx, dy, dz):
+    """The six 64-term sums (xx, xy, xz, yy, yz, zz) of one offset in cells."""
+    h = [mp.mpf(dx), mp.mpf(dy), mp.mpf(dz)]
+    acc = [mp.mpf(0)] * 6
+    for bits in range(64):
+        ikx, iky, ikz = (bits >> 5) & 1, (bits >> 4) & 1, (bits >> 3) & 1
+        ilx, ily, ilz = (bits >> 2) & 1, (bits >> 1) & 1, bits & 1
+        s = 1 if (ikx + iky + ikz + ilx + ily + ilz) % 2 == 0 else -1
+        X, Y, Z = (ix + ikx - ilx) * h[0], (iy + iky - ily) * h[1], (iz + ikz - ilz) * h[2]
+        acc[0] += s * f(X, Y, Z)
+        acc[1] += s * g(X, Y, Z)
+        acc[2] += s * g(X, Z, Y)
+        acc[3] += s * f(Y, Z, X)
+        acc[4] += s * g(Y, Z, X)
+        acc[5] += s * f(Z, X, Y)
+    return [float(a) for a in acc]
+
+
+def far_cases():
+    cases = []
+    for (ix, iy, iz, dx, dy, dz) in [
+        (12, 5, 2, 1e-9, 1e-9, 0.8e-9), (20, 7, 3, 1e-9, 1e-9, 0.8e-9), (30, -11, 4, 1e-9, 1e-9, 0.8e-9),
+        (-25, 18, 0, 1e-9, 1e-9, 0.8e-9), (0, 40, -3, 2e-9, 2e-9, 1e-9), (64, 0, 0, 1e-9, 1e-9, 0.8e-9),
+        (0, 0, 48, 1e-9, 1e-9, 1e-9), (80, -30, 12, 1e-9, 1e-9, 0.8e-9), (-128, 96, 5, 2e-9, 2e-9, 1e-9),
+        (256, 0, 0, 1e-9, 1e-9, 0.8e-9), (300, 250, 0, 1e-9, 1e-9, 0.8e-9), (17, 33, 9, 1e-9, 1.5e-9, 1e-9),
+    ]:
+        cases.append({"cell": [ix, iy, iz], "d": [dx, dy, dz], "raw": raw_sums(ix, iy, iz, dx, dy, dz)})
+    with open(os.path.join(HERE, "newell_far_golden.json"), "w") as fh:
+        json.dump({"digits": mp.mp.dps, "cases": cases}, fh)
+
+
 def main():
+    far_cases()
+    if "--far" in sys.argv:
+        return
     rng = np.random.default_rng(2024)
     pts = []
     for _ in range(40):

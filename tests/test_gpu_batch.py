@@ -135,15 +135,24 @@ def test_mc_forms_fp64_decisions_match_oracle(M, O, form):
 
 
 @pytest.mark.parametrize("prec", [32, 64])
-@pytest.mark.parametrize("geom", [dict(nx=64, ny=48, pbc_x=2, pbc_y=2), dict(nx=12, ny=10, nz=3, pbc_x=0, pbc_y=0),
-                                  dict(nx=15, ny=8, pbc_x=1, pbc_y=1)])
-def test_inline_transforms_bitwise_equal(M, prec, geom):
-    """The pass kernels with the warp-level transforms in line and out of line
-    round identically."""
+@pytest.mark.parametrize("geom", [dict(nx=64, ny=64, pbc_x=2, pbc_y=2), dict(nx=32, ny=128, pbc_x=1, pbc_y=1),
+                                  dict(nx=16, ny=32, nz=2, pbc_x=1, pbc_y=1, pbc_z=0),
+                                  dict(nx=12, ny=10, nz=3, pbc_x=0, pbc_y=0)])
+@pytest.mark.parametrize("variant", ["inline", "lean", "lean_half_threads"])
+def test_transform_variants_bitwise_equal(M, prec, geom, variant):
+    """The pass kernels with the warp-level transforms in line or out of line,
+    and the in-place column passes that read K^ from global memory (with the
+    full or half thread count), round identically."""
     cfgs = cfgs_for(M, 2, prec, sweep_engine=1, **geom)
     with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
         sa, sb = list(a.launch_shape()), list(b.launch_shape())
-        sa[7], sb[7] = 0, 1
+        sa[7] = sa[8] = 0
+        if variant == "inline":
+            sb[7] = 1
+        else:
+            sb[8] = 1
+            if variant == "lean_half_threads":
+                sb[4] = max(64, sb[4] // 2)
         a.set_launch_shape(sa)
         b.set_launch_shape(sb)
         a.run_sweeps(1, 0, 29)

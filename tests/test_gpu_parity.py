@@ -377,3 +377,32 @@ def test_engine_auto_selection(M):
     with pytest.raises(M.MmcError) as ei:
         M.Lattice(cfg(M, nx=15, ny=8, pbc_x=1, sweep_engine=M.ENGINE_FUSED))
     assert ei.value.status == M.ERR_UNSUPPORTED
+
+
+def test_device_wait_timeout_is_reported_and_device_stays_usable(M):
+    """Failure detection without a fault: a barrier wait that nothing can
+    complete runs out of its poll budget, the kernel returns, the host reads
+    MMC_ERR_TIMEOUT, and the next computation on the device is still right."""
+    import ctypes
+    st = ctypes.c_int(-1)
+    M.check(M.lib().mmc_selftest_barrier_timeout(0, 4096, ctypes.byref(st)))
+    assert st.value == 8  # MMC_ERR_TIMEOUT
+    c = cfg(M, nx=16, ny=16, precision=64)
+    with M.Lattice(c) as a:
+        a.run_sweeps(200.0, 0, 0, 5)
+        assert a.energy().accepted > 0
+
+
+@pytest.mark.parametrize("geom", [dict(nx=16, ny=12, pbc_x=2, pbc_y=1), dict(nx=10, ny=8, nz=3, pbc_x=3, pbc_y=0,
+                                                                           pbc_z=0)])
+def test_far_radius_tensor_bitwise_equals_oracle(M, O, geom, tmp_path):
+    """The far-field tensor terms (tensor_far_radius) are computed by the same
+    expression on the GPU and in the oracle; the cache keeps them apart from
+    the exact tensor's file."""
+    c = cfg(M, tensor_far_radius=12, **geom)
+    with M.Lattice(c) as lat:
+        lat.build_demag(str(tmp_path))
+        k = lat.tensor()
+    assert np.array_equal(k, O.tensor(c))
+    names = sorted(p.name for p in tmp_path.iterdir())
+    assert len(names) == 1 and names[0].endswith("_far12.ovf")

@@ -78,6 +78,9 @@ def test_optional_keys(M, tmp_path):
                                                 "tensor_cache = /tmp/cache\n"))
     assert c.precision == 64 and c.ovf_format == M.OVF_TEXT and c.use_reference_pi == 1
     assert c.tensor_cache == b"/tmp/cache"
+    c = M.load_ini(write(tmp_path, README_INI + "tensor_far_radius = 32\nsweep_engine = kernels\n"))
+    assert c.tensor_far_radius == 32 and c.sweep_engine == M.ENGINE_KERNELS
+    assert M.load_ini(write(tmp_path, README_INI)).tensor_far_radius == 0  # reference behaviour by default
 
 
 def test_comments_sections_and_bools(M, tmp_path):
@@ -96,6 +99,7 @@ def test_comments_sections_and_bools(M, tmp_path):
     (lambda s: s.replace("use_random_init = true", "use_random_init = maybe"), "bad value"),
     (lambda s: s + "precision = 16\n", "precision"),
     (lambda s: s.replace("dz = 0.8e-9", "dz = 0.8e-9 junk"), "bad value for dz"),
+    (lambda s: s + "tensor_far_radius = 5\n", "tensor_far_radius"),
 ])
 def test_ini_errors(M, tmp_path, mutate, needle):
     with pytest.raises(M.MmcError) as ei:

@@ -125,3 +125,32 @@ def test_tensor_symmetry(M, O):
     np.testing.assert_allclose(flip_x[1], -k[1], atol=1e-13)
     np.testing.assert_allclose(flip_x[2], -k[2], atol=1e-13)
     np.testing.assert_allclose(flip_x[4], k[4], atol=1e-13)
+
+
+def test_far_field_expansion_against_60_digit_sums(O):
+    """The far-field form of the 64-term sums (csrc/newell_far.h) against
+    60-digit evaluations: O((d/r)^8) truncation, so < 1e-9 of the largest
+    component at 12 cells and < 1e-12 beyond 30; the FP64 64-term sum itself
+    is worse beyond ~20 cells (cancellation)."""
+    data = json.load(open(os.path.join(GOLDEN, "newell_far_golden.json")))
+    for case in data["cases"]:
+        ix, iy, iz = case["cell"]
+        dx, dy, dz = case["d"]
+        want = np.array(case["raw"])
+        got = O.newell_far(ix * dx, iy * dy, iz * dz, dx, dy, dz)
+        r = np.sqrt((ix * dx) ** 2 + (iy * dy) ** 2 + (iz * dz) ** 2) / max(dx, dy, dz)
+        err = np.abs(got - want).max() / np.abs(want).max()
+        assert err < (1e-9 if r < 20 else 2e-11 if r < 30 else 1e-12), (case["cell"], r, err)
+        if r > 60:
+            exact64 = O.newell_raw(ix, iy, iz, dx, dy, dz)
+            assert np.abs(exact64 - want).max() / np.abs(want).max() > 100 * err
+
+
+def test_far_radius_tensor_matches_exact_tensor(O, M):
+    """A tensor with the far-field switch at 12 cells agrees with the exact one
+    to the exact sum's own rounding, and equals it where no image is far."""
+    c0 = M.Config.defaults(nx=16, ny=12, nz=1, pbc_x=2, pbc_y=1, pbc_z=0, precision=64)
+    c1 = M.Config.defaults(nx=16, ny=12, nz=1, pbc_x=2, pbc_y=1, pbc_z=0, precision=64, tensor_far_radius=12)
+    k0, k1 = O.tensor(c0), O.tensor(c1)
+    assert np.abs(k1 - k0).max() <= 1e-9 * np.abs(k0).max()
+    assert not np.array_equal(k0, k1)
