@@ -162,6 +162,13 @@ def dist_setup():
     return None, rank, local, world
 
 
+def workload_config(R, S, seeds):
+    return {"workload": f"anneal stage of {R} replicas of the 256x256x1 film, demag, PBC 20 images (x,y), "
+                        f"{S} sweeps/stage", "replicas_per_gpu": R, "seeds": f"{seeds[0]}..{seeds[-1]}",
+            "sweeps_per_step": S, "cells_per_replica": 65536, "precision": "fp32 bulk, fp64 tensor and energy",
+            "l2": "512 MB flush between timed steps"}
+
+
 def replica_seeds(rank, R):
     """Seeds of rank `rank`'s replicas: 256.. on rank 0, disjoint across ranks."""
     return [256 + rank * R + r for r in range(R)]
@@ -320,8 +327,10 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "anneal stage 256x256x1, demag, PBC 20 images (x,y), 10000 sweeps/stage",
-                   "cache": "lattice resident in host memory"},
+        "config": dict(workload_config(args.batch, args.sweeps, replica_seeds(0, args.batch)),
+                       precision="fp64 (the oracle port of the sweep)",
+                       sample="the sweeps of one replica on all host cores; trials/s per trial does not depend "
+                              "on the replica count"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference not buildable (kernel bodies unpublished); FP64 C++ port of the sweep on all host cores",
@@ -476,11 +485,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"anneal stage of {R} replicas of the 256x256x1 film, demag, PBC 20 images (x,y), "
-                               f"{S} sweeps/stage", "replicas_per_gpu": R, "seeds": f"{seeds[0]}..{seeds[-1]}",
-                   "sweeps_per_step": S, "cells_per_replica": n,
-                   "precision": "fp32 bulk, fp64 tensor and energy",
-                   "l2": "512 MB flush between timed steps"},
+        "config": workload_config(R, S, seeds),
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": R * 3 * n * 8, "d2h_bytes_per_step": R * 3 * n * 8},
         "roofline": roofline,
         "clocks": clk.summary(),
