@@ -529,7 +529,7 @@ def main():
     ap.add_argument("--no-relax", action="store_true", help="skip the gradient / relaxation line")
     ap.add_argument("--no-slab", action="store_true", help="skip the 3-D slab line")
     ap.add_argument("--launch-shape", default="",
-                    help="nine comma-separated values of a launch shape to use instead of autotuning")
+                    help="ten comma-separated values of a launch shape to use instead of autotuning")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -332,24 +332,26 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
  * a film in one tile launch, 2 one vectorised launch per colour (films with
  * nx a multiple of 4), whether the pass kernels expand their transforms in
  * line (1) or call them out of line (0), and whether the column passes
- * transform in place reading the tensor from global memory (1). */
-int mmc_batch_launch_shape(mmc_batch* b, int out[9]);
+ * transform in place reading the tensor from global memory (1), and the
+ * number of streams (1-4) the batch's replicas are split over. */
+int mmc_batch_launch_shape(mmc_batch* b, int out[10]);
 /* Autotuner: times each launch shape this batch can run with (the film row
  * kernel with each band that fits; the pass kernels with 1-16 rows per x-pass
  * CTA and 1-8 kx columns per column-pass tile, then -- one dimension at a
  * time from the fastest so far -- the transforms in and out of line, the
- * in-place column passes, every Metropolis form) for `sweeps` sweeps from the
+ * in-place column passes, every Metropolis form, 2-4 streams) for `sweeps`
+ * sweeps from the
  * current state, keeps the fastest and restores m and the acceptance
  * counters.  Every shape gives bit-identical results, so the choice changes
  * only the speed.  best_ms_per_sweep and candidates may be NULL.  No
  * counterpart in the reference, whose block shape is fixed in the source
  * (src/main.cu:275-286). */
 int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int* candidates);
-/* Sets the launch shape (the nine values of mmc_batch_launch_shape), e.g. one
+/* Sets the launch shape (the ten values of mmc_batch_launch_shape), e.g. one
  * an earlier autotune chose.  Values outside the ranges the autotuner tries,
  * or a row-kernel band that does not fit this batch, are rejected.  Results do
  * not depend on the shape.  No counterpart in the reference. */
-int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[9]);
+int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]);
 
 /* Replica farms: batches of different lattice sizes advanced together.  One
  * call runs nsweeps sweeps of every batch (each with its own temperatures,

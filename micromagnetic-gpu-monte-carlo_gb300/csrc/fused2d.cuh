@@ -44,13 +44,21 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // reduction (no round trip) and polls the counter with acquire loads.
 // spin_limit: polls before the wait gives up (the default is seconds, far
 // beyond any legitimate wait); expect: arrivals this barrier waits for.
-__device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned int& target, int* flag_smem,
-                                          unsigned long long spin_limit = 1ull << 24, unsigned int expect = 0) {
+// The barrier in two halves: grid_arrive publishes this CTA's arrival (after
+// all its threads' writes), grid_wait polls until every CTA has arrived.  Work
+// that needs nothing from other CTAs can run between the two.
+__device__ __forceinline__ void grid_arrive(GridBarrier* bar, unsigned int& target, unsigned int expect = 0) {
   __syncthreads();
   if (threadIdx.x == 0) {
     target += expect ? expect : gridDim.x;
     __threadfence();
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&bar->count), "r"(1u) : "memory");
+  }
+}
+
+__device__ __forceinline__ bool grid_wait(GridBarrier* bar, unsigned int target, int* flag_smem,
+                                          unsigned long long spin_limit = 1ull << 24) {
+  if (threadIdx.x == 0) {
     unsigned long long spins = 0;
     int ok = 1;
     while (true) {
@@ -68,6 +76,12 @@ __device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned int& target
   }
   __syncthreads();
   return *flag_smem != 0;
+}
+
+__device__ __forceinline__ bool grid_sync(GridBarrier* bar, unsigned int& target, int* flag_smem,
+                                          unsigned long long spin_limit = 1ull << 24, unsigned int expect = 0) {
+  grid_arrive(bar, target, expect);
+  return grid_wait(bar, target, flag_smem, spin_limit);
 }
 
 template <typename T>
@@ -269,7 +283,7 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(const __grid_const
     R.S = (sw & 1) ? P.S2 : P.S;
     R.So = (sw & 1) ? P.S : P.S2;
     stamp(sw, 0);
-    row_load<T>(R, c, P.stage, sweep);
+    row_load<T>(R, c, P.stage, sweep, sw == 0);  // later sweeps' proposals were made during barrier 2
     stamp(sw, 1);
     row_field<T>(R);
     stamp(sw, 2);
@@ -283,7 +297,11 @@ __global__ void __launch_bounds__(FUSED_THREADS, 1) k_fused2d(const __grid_const
     stamp(sw, 5);
     column_phase(sw, R.So);
     stamp(sw, 7);
-    if (!grid_sync(P.bar, target, &s_flag)) return;
+    // the next sweep's proposals depend on nothing other CTAs write: make them
+    // while the barrier's arrivals come in
+    grid_arrive(P.bar, target);
+    row_proposals<T>(R, c, P.stage, sweep + 1);
+    if (!grid_wait(P.bar, target, &s_flag)) return;
     stamp(sw, 8);
   }
   unsigned int v = my_acc;

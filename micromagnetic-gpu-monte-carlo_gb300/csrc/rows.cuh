@@ -98,9 +98,29 @@ __device__ __forceinline__ void row_phase_carve(RowPhase<T>& R, unsigned char*& 
   if (two_fft) ptr += fl;
 }
 
-// copy + proposals (ends with the data in shared memory, after __syncthreads)
+// Philox proposals of the sweep for colour 0 on the work rows and colour 1 on
+// the band rows (they depend only on cell, stage and sweep).
 template <typename T>
-__device__ __forceinline__ void row_load(const RowPhase<T>& R, const McCoef<T>& c, uint32_t stage, uint32_t sweep) {
+__device__ __forceinline__ void row_proposals(const RowPhase<T>& R, const McCoef<T>& c, uint32_t stage,
+                                              uint32_t sweep) {
+  const int nx = R.g.nx, nwork = R.nb + 2, half = (nx + 1) >> 1;
+  for (int idx = threadIdx.x; idx < (nwork + R.nb) * half; idx += blockDim.x) {
+    const int k = R.g.dhxc.div(idx), j = idx - k * half;
+    const int color = k < nwork ? 0 : 1;
+    const int slot = color == 0 ? 1 + k : 2 + (k - nwork);
+    const int y = R.rows[slot];
+    if (y < 0) continue;
+    const int x = 2 * j + ((color + y) & 1);
+    if (x >= nx) continue;
+    R.prop[idx] = mc_propose<T>(c, (uint32_t)(x + nx * y), stage, sweep);
+  }
+}
+
+// copy (+ proposals, while the copies land); ends with the data in shared
+// memory, after __syncthreads
+template <typename T>
+__device__ __forceinline__ void row_load(const RowPhase<T>& R, const McCoef<T>& c, uint32_t stage, uint32_t sweep,
+                                         bool with_proposals = true) {
   using V = C<T>;
   const int nx = R.g.nx, hxp = R.g.hxp;
   const long long n = R.g.n, nspec = R.g.nspec;
@@ -123,16 +143,7 @@ __device__ __forceinline__ void row_load(const RowPhase<T>& R, const McCoef<T>& 
     const int cc = ds.div(rem), q = rem - cc * per_s;
     cp_async16(R.specraw + ((size_t)w * 3 + cc) * hxp + q * ve, R.S + cc * nspec + (long long)r * hxp + q * ve);
   }
-  for (int idx = threadIdx.x; idx < (nwork + R.nb) * half; idx += blockDim.x) {
-    const int k = R.g.dhxc.div(idx), j = idx - k * half;
-    const int color = k < nwork ? 0 : 1;
-    const int slot = color == 0 ? 1 + k : 2 + (k - nwork);
-    const int y = R.rows[slot];
-    if (y < 0) continue;
-    const int x = 2 * j + ((color + y) & 1);
-    if (x >= nx) continue;
-    R.prop[idx] = mc_propose<T>(c, (uint32_t)(x + nx * y), stage, sweep);
-  }
+  if (with_proposals) row_proposals<T>(R, c, stage, sweep);
   cp_async_wait_all();
   __syncthreads();
 }

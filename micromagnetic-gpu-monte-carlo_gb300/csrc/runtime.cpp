@@ -1117,6 +1117,9 @@ struct mmc_batch {
   mmc_handle* base = nullptr;  // geometry, plans, tensor (replica 0's config)
   int R = 0;
   DemagTuning tun{};
+  int streams = 1;               // > 1: the batch's replicas split in that many parts on as many streams
+  cudaStream_t sts[3] = {nullptr, nullptr, nullptr};  // the extra streams, created on first use
+  cudaEvent_t fork = nullptr, joins[3] = {nullptr, nullptr, nullptr};
   int rows_band = 0;  // > 0: film sweeps run as row kernel + column pass
   std::vector<int> row_bands;  // bands the row kernel can run with on this device
   std::vector<mmc_config> cfgs;
@@ -1164,6 +1167,11 @@ void batch_free(mmc_batch* b) {
   if (!b) return;
   if (b->base) cudaSetDevice(b->base->device);
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->fork) cudaEventDestroy(b->fork);
+  for (int k = 0; k < 3; ++k) {
+    if (b->joins[k]) cudaEventDestroy(b->joins[k]);
+    if (b->sts[k]) cudaStreamDestroy(b->sts[k]);
+  }
   void* bufs[] = {b->params,   b->m,           b->h,          b->spec,        b->coef,   b->ecoef,
                   b->partials, b->red,         b->acc,        b->ctr,         b->d_replica_at,
                   b->d_temps,  b->d_replica_T, b->d_round,    b->d_counts,    b->m2,     b->spec2};
@@ -1242,9 +1250,54 @@ cudaError_t batch_rows_settle(mmc_batch* b) {
                          h->st);
 }
 
+// The extra streams and their fork/join events.
+int batch_alloc_streams(mmc_batch* b) {
+  if (!b->fork) CU(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  for (int k = 0; k < 3; ++k) {
+    if (!b->sts[k]) CU(cudaStreamCreateWithFlags(&b->sts[k], cudaStreamNonBlocking));
+    if (!b->joins[k]) CU(cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming));
+  }
+  return MMC_OK;
+}
+
+// One sweep of replicas [r0, r0 + nr) on stream st.
+template <typename T>
+cudaError_t batch_sweep_part(mmc_batch* b, int r0, int nr, cudaStream_t st) {
+  mmc_handle* h = b->base;
+  const long long ms = 3 * h->g.n, ss = 3 * h->g.nspec;
+  T* m = (T*)b->m + r0 * ms;
+  T* hh = (T*)b->h + r0 * ms;
+  cudaError_t e = cudaSuccess;
+  if (h->cfg.cal_demag_flag)
+    e = launch_demag<T>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, m, hh,
+                        (char*)b->spec + (size_t)r0 * ss * 2 * sizeof(T), h->khat, st, nr);
+  if (e != cudaSuccess) return e;
+  return launch_mc<T>(h->g, (const McCoef<T>*)b->coef + r0, m, hh, b->ctr, -1, b->acc + r0, st, nr,
+                      b->tun.mc_form);
+}
+
 cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
   mmc_handle* h = b->base;
   cudaError_t e;
+  const int parts = std::min(b->streams, b->R);
+  if (parts > 1 && !ev && b->sts[0]) {
+    // replica parts on their own streams: kernels of different kinds overlap
+    // on the SMs; part 0 stays on the batch's stream
+    if ((e = cudaEventRecord(b->fork, h->st)) != cudaSuccess) return e;
+    for (int k = 1; k < parts; ++k)
+      if ((e = cudaStreamWaitEvent(b->sts[k - 1], b->fork, 0)) != cudaSuccess) return e;
+    for (int k = parts - 1; k >= 0; --k) {
+      const int r0 = (int)((long long)b->R * k / parts), r1 = (int)((long long)b->R * (k + 1) / parts);
+      cudaStream_t st = k == 0 ? h->st : b->sts[k - 1];
+      e = h->prec == 32 ? batch_sweep_part<float>(b, r0, r1 - r0, st) : batch_sweep_part<double>(b, r0, r1 - r0, st);
+      if (e != cudaSuccess) return e;
+    }
+    for (int k = 1; k < parts; ++k) {
+      if ((e = cudaEventRecord(b->joins[k - 1], b->sts[k - 1])) != cudaSuccess) return e;
+      if ((e = cudaStreamWaitEvent(h->st, b->joins[k - 1], 0)) != cudaSuccess) return e;
+    }
+    return launch_advance(b->ctr, 1, h->st);
+  }
   if (h->cfg.cal_demag_flag && (e = batch_demag(b, ev)) != cudaSuccess) return e;
   e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h, b->ctr,
                                        -1, b->acc, h->st, b->R, b->tun.mc_form)
@@ -1407,6 +1460,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   struct Cand {
     int rows_band;
     DemagTuning tun;
+    int streams = 1;
   };
   const Geom& g = h->g;
   const size_t cs = 2 * h->tsize;
@@ -1427,9 +1481,11 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   auto trial = [&](const Cand& cd) {
     if (e != cudaSuccess || status != MMC_OK) return;
     if (cd.rows_band > 0 && (status = batch_alloc_rows(b)) != MMC_OK) return;
+    if (cd.streams > 1 && (status = batch_alloc_streams(b)) != MMC_OK) return;
     ++tried;
     b->rows_band = cd.rows_band;
     b->tun = cd.tun;
+    b->streams = cd.streams;
     SweepCounters c0{0, 0};
     e = cudaMemcpyAsync(b->m, saved, mbytes, cudaMemcpyDeviceToDevice, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st);
@@ -1490,15 +1546,25 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
         trial(c);
       }
   }
+  {  // replica parts on 2, 3 or 4 streams
+    const Cand one = best;
+    for (int k = 2; k <= std::min(4, b->R); ++k) {
+      Cand c = one;
+      c.streams = k;
+      trial(c);
+    }
+  }
   if (h->cfg.cal_demag_flag)
     for (int bd : b->row_bands) {
       Cand c = best;
       c.rows_band = bd;
+      c.streams = 1;
       trial(c);
     }
   if (e == cudaSuccess && status == MMC_OK && best_t >= 0) {
     b->rows_band = best.rows_band;
     b->tun = best.tun;
+    b->streams = best.streams;
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(b->m, saved, mbytes, cudaMemcpyDeviceToDevice, h->st);
   if (e == cudaSuccess)
@@ -2081,12 +2147,14 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
   return MMC_OK;
 }
 
-int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[9]) {
+int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
   if (!b || !shape) return fail(MMC_ERR_INVALID, "null argument");
   mmc_handle* h = b->base;
   const Geom& g = h->g;
   const size_t cs = 2 * h->tsize;
   DemagTuning t{shape[0], shape[1], shape[2], shape[3], shape[4], shape[6], shape[7], shape[8]};
+  const int streams = shape[9];
+  if (streams < 1 || streams > 4) return fail(MMC_ERR_INVALID, "streams must be in [1, 4]");
   const int band = shape[5];
   auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
   if (!pow2(t.x_rows_per_cta) || t.x_rows_per_cta > 16 || x_pass_smem(h->px.p, t.x_rows_per_cta, cs) > smem_limit() ||
@@ -2101,8 +2169,10 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[9]) {
     return fail(MMC_ERR_UNSUPPORTED, "row-kernel band not available for this batch");
   TRY(set_dev(h));
   if (band > 0) TRY(batch_alloc_rows(b));
+  if (streams > 1) TRY(batch_alloc_streams(b));
   b->tun = t;
   b->rows_band = band;
+  b->streams = streams;
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
   b->gexec = nullptr;
   b->graph_len = 0;
@@ -2116,8 +2186,9 @@ int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int*
   return batch_autotune(b, sweeps, best_ms_per_sweep, candidates);
 }
 
-int mmc_batch_launch_shape(mmc_batch* b, int out[9]) {
+int mmc_batch_launch_shape(mmc_batch* b, int out[10]) {
   if (!b || !out) return fail(MMC_ERR_INVALID, "null argument");
+  out[9] = b->streams;
   out[5] = b->rows_band;
   out[6] = b->tun.mc_form;
   out[7] = b->tun.fft_inline;

@@ -463,11 +463,11 @@ class Batch:
         return ms.value, n.value
 
     def set_launch_shape(self, shape):
-        arr = (ctypes.c_int * 9)(*[int(v) for v in shape])
+        arr = (ctypes.c_int * 10)(*[int(v) for v in shape])
         check(lib().mmc_batch_set_launch_shape(self.h, arr))
 
     def launch_shape(self):
-        out = (ctypes.c_int * 9)()
+        out = (ctypes.c_int * 10)()
         check(lib().mmc_batch_launch_shape(self.h, out))
         return tuple(out)
 

@@ -138,7 +138,7 @@ def test_mc_forms_fp64_decisions_match_oracle(M, O, form):
 @pytest.mark.parametrize("geom", [dict(nx=64, ny=64, pbc_x=2, pbc_y=2), dict(nx=32, ny=128, pbc_x=1, pbc_y=1),
                                   dict(nx=16, ny=32, nz=2, pbc_x=1, pbc_y=1, pbc_z=0),
                                   dict(nx=12, ny=10, nz=3, pbc_x=0, pbc_y=0)])
-@pytest.mark.parametrize("variant", ["inline", "lean", "lean_half_threads"])
+@pytest.mark.parametrize("variant", ["inline", "lean", "lean_half_threads", "two_streams"])
 def test_transform_variants_bitwise_equal(M, prec, geom, variant):
     """The pass kernels with the warp-level transforms in line or out of line,
     and the in-place column passes that read K^ from global memory (with the
@@ -149,6 +149,8 @@ def test_transform_variants_bitwise_equal(M, prec, geom, variant):
         sa[7] = sa[8] = 0
         if variant == "inline":
             sb[7] = 1
+        elif variant == "two_streams":
+            sb[9] = 2
         else:
             sb[8] = 1
             if variant == "lean_half_threads":
@@ -157,8 +159,11 @@ def test_transform_variants_bitwise_equal(M, prec, geom, variant):
         b.set_launch_shape(sb)
         a.run_sweeps(1, 0, 29)
         b.run_sweeps(1, 0, 29)
+        a.run_sweeps(1, 29, 64)  # graph replays
+        b.run_sweeps(1, 29, 64)
         for r in range(2):
             assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
 
 
 def test_mc_forms_rejected_where_ineligible(M):
@@ -251,3 +256,22 @@ def test_batch_rejects_mixed_geometry(M):
     b = M.Config.defaults(nx=16, ny=8)
     with pytest.raises(M.MmcError):
         M.Batch([a, b])
+
+
+@pytest.mark.parametrize("streams", [2, 3, 4])
+def test_streams_with_tempering_and_odd_batch(M, streams):
+    """Replica parts on several streams for a batch of odd size with
+    parallel-tempering ladders: the swap pass runs after every part, results
+    equal the one-stream batch."""
+    cfgs = cfgs_for(M, 5, 32, sweep_engine=1, nx=32, ny=32, pbc_x=1, pbc_y=1)
+    temps = np.array([[60.0, 100.0, 170.0, 290.0, 500.0]])
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        s = list(b.launch_shape())
+        s[9] = streams
+        b.set_launch_shape(s)
+        for x in (a, b):
+            x.set_ladders(np.arange(5).reshape(1, 5), temps, 10, 3)
+            x.run_sweeps(0, 0, 95)
+        for r in range(5):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        assert np.array_equal(a.temperatures(), b.temperatures())
