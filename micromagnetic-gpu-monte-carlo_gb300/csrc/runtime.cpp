@@ -1491,12 +1491,17 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess && b->rows_band > 0) e = batch_demag(b);
     if (e == cudaSuccess) e = batch_sweeps(b, 2);  // warm-up
-    if (e == cudaSuccess) e = cudaEventRecord(h->ev[0], h->st);
-    if (e == cudaSuccess) e = batch_sweeps(b, sweeps);
-    if (e == cudaSuccess) e = cudaEventRecord(h->ev[1], h->st);
-    if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[1]);
-    float ms = 0;
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]);
+    // the faster of two timed repetitions
+    float ms = -1;
+    for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+      if (e == cudaSuccess) e = cudaEventRecord(h->ev[0], h->st);
+      if (e == cudaSuccess) e = batch_sweeps(b, sweeps);
+      if (e == cudaSuccess) e = cudaEventRecord(h->ev[1], h->st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[1]);
+      float t = 0;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&t, h->ev[0], h->ev[1]);
+      if (e == cudaSuccess && (ms < 0 || t < ms)) ms = t;
+    }
     if (e == cudaSuccess && (best_t < 0 || ms < best_t)) {
       best = cd;
       best_t = ms;
