@@ -317,6 +317,13 @@ int mmc_batch_set_ladders(mmc_batch* b, int nladders, int per_ladder, const int*
 /* Current replica at each ladder slot and the swap counts {attempted, accepted}. */
 int mmc_batch_ladder_state(mmc_batch* b, int* replicas, unsigned long long counts[2]);
 int mmc_batch_run_sweeps(mmc_batch* b, long long stage, long long sweep0, long long nsweeps);
+/* The stage loop of mmc_run_anneal (src/main.cu:801-1139) for every replica at
+ * once: replica r writes energy.txt and its snapshots into
+ * <output_dir>/replica_<rrr>/, the same files a single run of its config
+ * writes (and with the same numbers: a replica's trajectory is the single
+ * run's).  All replicas must share the temperature schedule and the output
+ * periods.  Parameter sweeps (the CLI's -farm-Bz= / -farm-D=) run this way. */
+int mmc_batch_run_anneal(mmc_batch* b, const char* output_dir, int verbose);
 int mmc_batch_last_run_ms(mmc_batch* b, double* ms);
 /* Runs nsweeps sweeps without graphs and times each kernel family with CUDA
  * events on the batch's stream (totals in ms).  One kernel per pass:

@@ -1,12 +1,17 @@
 // mmc_main.cpp -- command-line driver, a drop-in for the reference binary.
 //
-//   mmc <cfg.ini> [-gpu=N] [-tensorcache="/path/"]
+//   mmc <cfg.ini> [-gpu=N] [-tensorcache="/path/"] [-farm-Bz=b1,b2,...] [-farm-D=d1,d2,...]
 //
 // Argument handling follows src/main.cu:97-105 and src/GPU_selector.h:11-76:
 // the first argument not starting with '-' is the ini file, -gpu=N picks the
 // device (default 0), -tensorcache= names the demag-tensor cache folder.
 // Outputs go to <ini dir>/<ini stem>.output/ (src/main.cu:193-231): energy.txt
 // and the OVF snapshots.  Ctrl-C stops the anneal at the next sweep boundary.
+//
+// -farm-Bz= / -farm-D= (not in the reference) anneal a parameter sweep from the
+// same ini: one replica per (B_z, D) pair, replica k seeded randomseed + k,
+// all in one batch on the GPU; replica k writes into replica_<kkk>/ of the
+// output folder and farm.txt lists k, B_z, D and the seed.
 #include <csignal>
 #include <cstdio>
 #include <cstdlib>
@@ -19,9 +24,63 @@
 #include "mmc.h"
 
 static mmc_handle* g_handle = nullptr;
+static mmc_batch* g_batch = nullptr;
 
 static void on_sigint(int) {
   if (g_handle) mmc_request_stop(g_handle);
+  if (g_batch) mmc_batch_request_stop(g_batch);
+}
+
+// "a,b,c" -> values; false on a malformed number
+static bool parse_list(const std::string& s, std::vector<double>& out) {
+  size_t i = 0;
+  while (i <= s.size()) {
+    size_t j = s.find(',', i);
+    if (j == std::string::npos) j = s.size();
+    const std::string tok = s.substr(i, j - i);
+    char* end = nullptr;
+    const double v = std::strtod(tok.c_str(), &end);
+    if (tok.empty() || *end != '\0') return false;
+    out.push_back(v);
+    i = j + 1;
+  }
+  return !out.empty();
+}
+
+// The parameter sweep: one batch of replicas, the stage loop for all of them.
+static int run_farm(const mmc_config& cfg, int gpu, const std::vector<double>& bz, const std::vector<double>& dm,
+                    const std::string& out) {
+  std::vector<mmc_config> cfgs;
+  for (double b : bz)
+    for (double d : dm) {
+      mmc_config c = cfg;
+      c.Bextz = b;
+      c.Dind = d;
+      if (cfg.randomseed >= 0) c.randomseed = cfg.randomseed + (long long)cfgs.size();
+      cfgs.push_back(c);
+    }
+  std::printf("farm: %zu replicas\n", cfgs.size());
+  int st = mmc_batch_create(cfgs.data(), (int)cfgs.size(), gpu, &g_batch);
+  if (st != MMC_OK) return st;
+  std::signal(SIGINT, on_sigint);
+  if (cfg.cal_demag_flag) {
+    std::printf("Calculating demag tensor...\n");
+    st = mmc_batch_build_demag(g_batch, cfg.tensor_cache);
+  }
+  if (st == MMC_OK) st = mmc_batch_autotune(g_batch, 8, nullptr, nullptr);
+  if (st == MMC_OK) {
+    std::printf("Start...\n");
+    st = mmc_batch_run_anneal(g_batch, out.c_str(), 1);
+  }
+  if (st == MMC_OK || st == MMC_ERR_INTERRUPTED) {
+    FILE* fp = std::fopen((out + "/farm.txt").c_str(), "w");
+    if (fp) {
+      for (size_t k = 0; k < cfgs.size(); ++k)
+        std::fprintf(fp, "%zu %g %g %lld\n", k, cfgs[k].Bextz, cfgs[k].Dind, cfgs[k].randomseed);
+      std::fclose(fp);
+    }
+  }
+  return st;
 }
 
 static std::string abspath(const std::string& p) {
@@ -40,6 +99,7 @@ int main(int argc, char** argv) {
   }
   std::string cfg_path, cache;
   int gpu = 0;
+  std::vector<double> farm_bz, farm_d;
   for (int i = 1; i < argc; ++i) {
     std::string a = argv[i];
     if (a.empty()) continue;
@@ -57,6 +117,16 @@ int main(int argc, char** argv) {
     } else if (key.rfind("tensorcache=", 0) == 0) {
       cache = key.substr(12);
       if (cache.size() >= 2 && cache.front() == '"' && cache.back() == '"') cache = cache.substr(1, cache.size() - 2);
+    } else if (key.rfind("farm-Bz=", 0) == 0) {
+      if (!parse_list(key.substr(8), farm_bz)) {
+        std::printf("Invalid command line parameter: -farm-Bz=\n");
+        return 1;
+      }
+    } else if (key.rfind("farm-D=", 0) == 0) {
+      if (!parse_list(key.substr(7), farm_d)) {
+        std::printf("Invalid command line parameter: -farm-D=\n");
+        return 1;
+      }
     }
   }
   cfg_path = abspath(cfg_path);
@@ -80,6 +150,22 @@ int main(int argc, char** argv) {
   std::string stem = base.substr(0, base.find_last_of('.'));
   std::string out = dir + "/" + stem + ".output";
   std::printf("output_path: %s\n", out.c_str());
+
+  if (!farm_bz.empty() || !farm_d.empty()) {
+    if (farm_bz.empty()) farm_bz.push_back(cfg.Bextz);
+    if (farm_d.empty()) farm_d.push_back(cfg.Dind);
+    st = run_farm(cfg, gpu, farm_bz, farm_d, out);
+    int rc = 0;
+    if (st == MMC_ERR_INTERRUPTED) {
+      std::printf("interrupted\n");
+    } else if (st != MMC_OK) {
+      std::fprintf(stderr, "error: %s\n", mmc_last_error());
+      rc = 5;
+    }
+    mmc_batch_destroy(g_batch);
+    g_batch = nullptr;
+    return rc;
+  }
 
   st = mmc_create(&cfg, gpu, &g_handle);
   if (st != MMC_OK) {

@@ -2350,6 +2350,93 @@ int mmc_batch_get_m(mmc_batch* b, int r, double* mx, double* my, double* mz) {
   return MMC_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The stage loop of mmc_run_anneal for every replica of a batch at once: the
+// schedule of replica 0 (all replicas must share it), one output folder per
+// replica holding what a single run writes there.
+template <typename R>
+int batch_anneal_loop(mmc_batch* b, const std::string& dir, int verbose) {
+  const mmc_config& c = b->cfgs[0];
+  for (const mmc_config& q : b->cfgs)
+    if (q.Temperature_start != c.Temperature_start || q.Temperature_end != c.Temperature_end ||
+        q.Temperature_step != c.Temperature_step || q.Temperature_use_exp != c.Temperature_use_exp ||
+        q.circle_per_stage != c.circle_per_stage || q.energy_output_period != c.energy_output_period ||
+        q.ms_output_period != c.ms_output_period)
+      return fail(MMC_ERR_INVALID, "batch anneals need one temperature schedule and output periods for all replicas");
+  const int Rn = b->R;
+  const mmc_handle* h = b->base;
+  const long long n = h->g.n;
+  std::vector<std::string> dirs(Rn), efiles(Rn);
+  for (int r = 0; r < Rn; ++r) {
+    char sub[32];
+    std::snprintf(sub, sizeof sub, "replica_%03d", r);
+    dirs[r] = join(dir, sub);
+    TRY(prepare_output_dir(dirs[r]));
+    efiles[r] = join(dirs[r], "energy.txt");
+    FILE* fp = std::fopen(efiles[r].c_str(), "w");
+    if (!fp) return fail(MMC_ERR_IO, "cannot create " + efiles[r]);
+    std::fclose(fp);
+  }
+  std::vector<double> mm(3 * n), temps(Rn);
+  std::vector<mmc_observables> obs(Rn);
+  R T = (R)c.Temperature_start;
+  const R Tend = (R)c.Temperature_end, Tstep = (R)c.Temperature_step;
+  long long out_count = 0, stage = 0;
+  while (T > Tend) {
+    if (verbose) std::printf("\n\nTemperature: %.2f K (%d replicas)\n", (double)T, Rn);
+    for (int r = 0; r < Rn; ++r) temps[r] = (double)T;
+    TRY(mmc_batch_set_temperatures(b, temps.data()));
+    long long s = 0;
+    while (s < c.circle_per_stage) {
+      if (b->stop.load()) return fail(MMC_ERR_INTERRUPTED, "stop requested");
+      if (s % c.ms_output_period == 0) {
+        for (int r = 0; r < Rn; ++r) {
+          TRY(mmc_batch_get_m(b, r, mm.data(), mm.data() + n, mm.data() + 2 * n));
+          char name[256];
+          std::snprintf(name, sizeof name, "%06lld_%.2fK_%lld.ovf", out_count, (double)T, s);
+          TRY(ovf_write(join(dirs[r], name), h->g.nx, h->g.ny, h->g.nz, b->cfgs[r].dx, b->cfgs[r].dy,
+                        b->cfgs[r].dz, mm.data(), mm.data() + n, mm.data() + 2 * n, b->cfgs[r].ovf_format, "m"));
+        }
+        ++out_count;
+      }
+      if (s % c.energy_output_period == 0) {
+        TRY(mmc_batch_energy(b, obs.data()));
+        for (int r = 0; r < Rn; ++r) {
+          FILE* fp = std::fopen(efiles[r].c_str(), "a");
+          if (!fp) return fail(MMC_ERR_IO, "cannot append to " + efiles[r]);
+          std::fprintf(fp, "%f %lld %g\n", (double)T, s, obs[r].e_total);
+          std::fclose(fp);
+        }
+      }
+      long long next = c.circle_per_stage;
+      const long long per[2] = {c.ms_output_period, c.energy_output_period};
+      for (long long p : per) next = std::min(next, (s / p + 1) * p);
+      TRY(batch_run(b, stage, s, next - s));
+      s = next;
+    }
+    T = c.Temperature_use_exp ? (R)(T * Tstep) : (R)(T - Tstep);
+    ++stage;
+  }
+  if (verbose) std::printf("~~~~~~~~~~~~~~END~~~~~~~~~~~~~~~~~~~~~~~~~ \n");
+  return MMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mmc_batch_run_anneal(mmc_batch* b, const char* output_dir, int verbose) {
+  if (!b || !output_dir) return fail(MMC_ERR_INVALID, "null argument");
+  TRY(set_dev(b->base));
+  b->stop.store(0);
+  TRY(prepare_output_dir(output_dir));
+  return b->base->prec == 32 ? batch_anneal_loop<float>(b, output_dir, verbose)
+                             : batch_anneal_loop<double>(b, output_dir, verbose);
+}
+
 int mmc_batch_build_demag(mmc_batch* b, const char* cache_dir) {
   if (!b) return fail(MMC_ERR_INVALID, "null batch");
   if (!b->base->cfg.cal_demag_flag) return fail(MMC_ERR_STATE, "cal_demag_flag is off");

@@ -304,6 +304,48 @@ def test_cli_end_to_end(M, tmp_path):
     assert len(list(out.glob("*.ovf"))) == 3
 
 
+def test_cli_parameter_farm_equals_single_runs(M, tmp_path):
+    """-farm-Bz= / -farm-D= anneal every (B_z, D) pair as a replica of one
+    batch; each replica's energy.txt and snapshots equal those of a single CLI
+    run of the ini with that B_z, D and seed."""
+    import shutil
+    import subprocess
+    text = open(os.path.join(os.path.dirname(__file__), "test_host_io.py")).read()
+    body = text.split('README_INI = """')[1].split('"""')[0]
+    body = (body.replace("nx = 256", "nx = 16").replace("ny = 256", "ny = 16")
+            .replace("circle_per_stage  = 100000", "circle_per_stage = 40")
+            .replace("Temperature_end = 40", "Temperature_end = 1100")
+            .replace("pbc_x = 20", "pbc_x = 2").replace("pbc_y = 20", "pbc_y = 2"))
+    cli = os.path.join(M.HERE, "bin", "mmc")
+    farm_dir = tmp_path / "farm"
+    farm_dir.mkdir()
+    (farm_dir / "f.ini").write_text(body)
+    r = subprocess.run([cli, str(farm_dir / "f.ini"), "-farm-Bz=0.1,0.4", "-farm-D=3e-3,5e-3"],
+                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    out = farm_dir / "f.output"
+    rows = [l.split() for l in (out / "farm.txt").read_text().splitlines()]
+    assert len(rows) == 4
+    base_seed = int(M.load_ini(str(farm_dir / "f.ini")).randomseed)
+    for k, bz, dm, seed in rows:
+        assert int(seed) == base_seed + int(k)
+        single = tmp_path / f"single{k}"
+        single.mkdir()
+        one = (body.replace("Bextz = 0.3", f"Bextz = {bz}").replace("Dind = 6e-3", f"Dind = {dm}")
+               .replace(f"randomseed = {base_seed}", f"randomseed = {seed}"))
+        (single / "s.ini").write_text(one)
+        r1 = subprocess.run([cli, str(single / "s.ini")], stdout=subprocess.PIPE, stderr=subprocess.PIPE,
+                            text=True, timeout=300)
+        assert r1.returncode == 0, r1.stdout + r1.stderr
+        rep = out / f"replica_{int(k):03d}"
+        assert (rep / "energy.txt").read_text() == (single / "s.output" / "energy.txt").read_text()
+        snaps = sorted(p.name for p in rep.glob("*.ovf"))
+        assert snaps and snaps == sorted(p.name for p in (single / "s.output").glob("*.ovf"))
+        for name in snaps:
+            assert (rep / name).read_bytes() == (single / "s.output" / name).read_bytes()
+        shutil.rmtree(single)
+
+
 FILMS = {
     "periodic32": dict(nx=32, ny=32, pbc_x=2, pbc_y=2),
     "open20x12": dict(nx=20, ny=12, pbc_x=0, pbc_y=0),
