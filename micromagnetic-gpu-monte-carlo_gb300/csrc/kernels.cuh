@@ -25,10 +25,13 @@ namespace mmc {
 // Rows that are pure zero padding are never loaded (pruned transform).
 
 // Real rows in[c][row][x] (x < xdata, zero up to p.n) -> S[c][z][y][kx], kx < hx.
-template <typename T, bool INL>
-__global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
+// NC: components (3 for m, 6 for the tensor), fixed at compile time so the
+// per-element work covers only the components that exist.
+template <typename T, bool INL, int NC>
+__global__ void k_x_forward(FftPlan p, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
                             long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, FastDiv dhx,
                             int pitch, int rows_per_cta, long long in_rstride, long long s_rstride) {
+  constexpr int ncomp = NC;
   const int hx = (int)dhx.d, ydata = (int)dyd.d;
   using V = C<T>;
   in += blockIdx.z * in_rstride;  // replica of a batch
@@ -36,7 +39,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nr
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw = reinterpret_cast<V*>(smem_raw);
   const int L = p.n;
-  const int npairs = (ncomp + 1) / 2;
+  constexpr int npairs = (ncomp + 1) / 2;
   const int row0 = blockIdx.x * rows_per_cta;
   const int nr = min(rows_per_cta, nrows - row0);
   V* bufA = tw + ((p.tw_total + 1) & ~1);
@@ -46,7 +49,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nr
   // their latencies overlap
   const int total = nr * L;
   for (int base = threadIdx.x; base < total; base += 4 * blockDim.x) {
-    T v[4][6];
+    T v[4][2 * npairs];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int idx = base + u * blockDim.x;
@@ -54,7 +57,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nr
       const bool ok = idx < total && x < xdata;
       const long long rbase = (long long)(row0 + rr) * xdata + x;
 #pragma unroll
-      for (int c = 0; c < 6; ++c) v[u][c] = (ok && c < ncomp) ? in[c * in_cstride + rbase] : (T)0;
+      for (int c = 0; c < 2 * npairs; ++c) v[u][c] = (ok && c < ncomp) ? in[c * in_cstride + rbase] : (T)0;
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
@@ -62,8 +65,8 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nr
       if (idx < total) {
         const int rr = p.dn.div(idx), x = idx - rr * L;
 #pragma unroll
-        for (int pr = 0; pr < 3; ++pr)
-          if (pr < npairs) bufA[(long long)(rr * npairs + pr) * L + x] = cmk<V>(v[u][2 * pr], v[u][2 * pr + 1]);
+        for (int pr = 0; pr < npairs; ++pr)
+          bufA[(long long)(rr * npairs + pr) * L + x] = cmk<V>(v[u][2 * pr], v[u][2 * pr + 1]);
       }
     }
   }
@@ -72,7 +75,7 @@ __global__ void k_x_forward(FftPlan p, int ncomp, int xdata, FastDiv dyd, int nr
   for (int idx = threadIdx.x; idx < nr * npairs * hx; idx += blockDim.x) {
     const int rest = dhx.div(idx);
     const int k = idx - rest * hx;
-    const int rr = npairs == 2 ? rest >> 1 : rest / npairs, pr = rest - rr * npairs;
+    const int rr = rest / npairs, pr = rest - rr * npairs;  // npairs is a compile-time 2 or 3
     const V* line = res + (long long)(rr * npairs + pr) * L;
     const V A = line[k];
     const V B = line[k == 0 ? 0 : L - k];
@@ -1060,7 +1063,8 @@ inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize, b
 // inside a stream capture.
 template <typename T>
 cudaError_t prepare_impl(int max_dyn_smem) {
-  const void* fns[] = {(const void*)k_x_forward<T, false>, (const void*)k_x_forward<T, true>,
+  const void* fns[] = {(const void*)k_x_forward<T, false, 3>, (const void*)k_x_forward<T, true, 3>,
+                       (const void*)k_x_forward<T, false, 6>, (const void*)k_x_forward<T, true, 6>,
                        (const void*)k_x_inverse<T, false>, (const void*)k_x_inverse<T, true>,
                        (const void*)k_col_pass<T, false>,  (const void*)k_col_pass<T, true>};
   for (const void* f : fns) MMC_TRY_ATTR(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem));
@@ -1077,8 +1081,10 @@ cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int
   const int lines = (ncomp + 1) / 2;
   size_t sm = x_pass_smem(p, lines, rpc, sizeof(C<T>));
   dim3 grid((nrows + rpc - 1) / rpc, 1, nrep);
-  auto kern = inl ? k_x_forward<T, true> : k_x_forward<T, false>;
-  kern<<<grid, threads, sm, st>>>(p, ncomp, xdata, FastDiv((uint32_t)ydata), nrows, in, in_cstride, S, nspec, nyp,
+  if (ncomp != 3 && ncomp != 6) return cudaErrorInvalidValue;
+  auto kern = ncomp == 3 ? (inl ? k_x_forward<T, true, 3> : k_x_forward<T, false, 3>)
+                         : (inl ? k_x_forward<T, true, 6> : k_x_forward<T, false, 6>);
+  kern<<<grid, threads, sm, st>>>(p, xdata, FastDiv((uint32_t)ydata), nrows, in, in_cstride, S, nspec, nyp,
                                   FastDiv((uint32_t)hx), pitch, rpc, in_rstride, s_rstride);
   return cudaGetLastError();
 }
