@@ -212,15 +212,56 @@ struct RegDft<T, INV, 1> {
   __device__ __forceinline__ static void run(C<T>*) {}
 };
 
-// Transforms `nlines` lines of length N = A * B in place; each line is owned by
-// a group of B lanes of one warp, so only __syncwarp is needed inside.
+// One line of length N = A * B owned by B lanes of one warp (lane b of the
+// group), with the input already in registers: v[a] = x[b + B a].
 //   x[b + B a] --(A-point DFT over a)--> Y[b][ka] --(* W_N^(b ka))-->
 //   transpose in the line (swizzled) --(B-point DFT over b)--> X[ka + A kb].
-// `roots` holds exp(-2 pi i j / N), j < N.
+// Lp is the line in shared memory, used for the transpose; it holds X in
+// natural order on return.  All lanes of the warp must call it (inactive
+// groups with active = false); `roots` holds exp(-2 pi i j / N), j < N.
+template <typename T, bool INV, int A, int B>
+__device__ __forceinline__ void fft_line_regs(C<T> (&v)[A], C<T>* Lp, int b, bool active, const C<T>* roots) {
+  using V = C<T>;
+  constexpr int Q = A / B;
+  RegDft<T, INV, A>::run(v);
+#pragma unroll
+  for (int ka = 1; ka < A; ++ka) {
+    const V w = roots[b * ka];
+    v[ka] = INV ? cmulc(v[ka], w) : cmul(v[ka], w);
+  }
+  __syncwarp();
+  if (active) {
+#pragma unroll
+    for (int ka = 0; ka < A; ++ka) Lp[ka * B + ((b + ka) & (B - 1))] = v[ka];
+  }
+  __syncwarp();
+  // v is dead after the transpose: reuse it for the columns
+  if (active) {
+#pragma unroll
+    for (int t = 0; t < Q; ++t) {
+      const int ka = b * Q + t;
+#pragma unroll
+      for (int bb = 0; bb < B; ++bb) v[t * B + bb] = Lp[ka * B + ((bb + ka) & (B - 1))];
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < Q; ++t) RegDft<T, INV, B>::run(v + t * B);
+  __syncwarp();
+  if (active) {
+#pragma unroll
+    for (int t = 0; t < Q; ++t)
+#pragma unroll
+      for (int kb = 0; kb < B; ++kb) Lp[(b * Q + t) + A * kb] = v[t * B + kb];
+  }
+  __syncwarp();
+}
+
+// Transforms `nlines` lines of length N = A * B in place (line l at
+// buf + l * stride), 32 / B lines per warp at a time; only __syncwarp is
+// needed inside.
 template <typename T, bool INV, int A, int B>
 __device__ __forceinline__ void fft_lines_warp_body(C<T>* buf, int nlines, int stride, const C<T>* roots) {
   using V = C<T>;
-  constexpr int Q = A / B;
   constexpr int GPW = 32 / B;  // lines per warp
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int grp = lane / B, b = lane - grp * B;
@@ -233,37 +274,7 @@ __device__ __forceinline__ void fft_lines_warp_body(C<T>* buf, int nlines, int s
 #pragma unroll
       for (int a = 0; a < A; ++a) v[a] = Lp[b + B * a];
     }
-    RegDft<T, INV, A>::run(v);
-#pragma unroll
-    for (int ka = 1; ka < A; ++ka) {
-      const V w = roots[b * ka];
-      v[ka] = INV ? cmulc(v[ka], w) : cmul(v[ka], w);
-    }
-    __syncwarp();
-    if (active) {
-#pragma unroll
-      for (int ka = 0; ka < A; ++ka) Lp[ka * B + ((b + ka) & (B - 1))] = v[ka];
-    }
-    __syncwarp();
-    // v is dead after the transpose: reuse it for the columns
-    if (active) {
-#pragma unroll
-      for (int t = 0; t < Q; ++t) {
-        const int ka = b * Q + t;
-#pragma unroll
-        for (int bb = 0; bb < B; ++bb) v[t * B + bb] = Lp[ka * B + ((bb + ka) & (B - 1))];
-      }
-    }
-#pragma unroll
-    for (int t = 0; t < Q; ++t) RegDft<T, INV, B>::run(v + t * B);
-    __syncwarp();
-    if (active) {
-#pragma unroll
-      for (int t = 0; t < Q; ++t)
-#pragma unroll
-        for (int kb = 0; kb < B; ++kb) Lp[(b * Q + t) + A * kb] = v[t * B + kb];
-    }
-    __syncwarp();
+    fft_line_regs<T, INV, A, B>(v, Lp, b, active, roots);
   }
 }
 

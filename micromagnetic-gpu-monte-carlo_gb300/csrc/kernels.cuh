@@ -147,6 +147,134 @@ __global__ void k_x_inverse(FftPlan p, const C<T>* __restrict__ S, long long nsp
   }
 }
 
+// ----------------------------------------------------- warp-shaped x passes
+// The same two transforms for lengths with a warp-level plan (L = A * B):
+// each line (a pair of components of one row) goes straight from global
+// memory into the registers of its B lanes in the order the transform takes
+// it (element b + B a in lane b of the group), so the input is never staged
+// in shared memory, and the loops over rows and columns need no division.
+// Same arithmetic as k_x_forward / k_x_inverse, so the results are the same
+// bit for bit.  Shared memory: the L roots and one L-element line per
+// (row, pair).
+template <typename T>
+__device__ __forceinline__ void load_roots(const FftPlan& p, C<T>* dst) {
+  const C<T>* src = plan_tw<T>(p) + p.full_off;
+  for (int i = threadIdx.x; i < p.n; i += blockDim.x) dst[i] = src[i];
+}
+
+template <typename T, int A, int B>
+__global__ void k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
+                              long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, int hx,
+                              int pitch, int rows_per_cta, long long in_rstride, long long s_rstride) {
+  constexpr int L = A * B, GPW = 32 / B;
+  using V = C<T>;
+  const int ydata = (int)dyd.d;
+  in += blockIdx.z * in_rstride;
+  S += blockIdx.z * s_rstride;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* roots = reinterpret_cast<V*>(smem_raw);
+  V* buf = roots + L;  // line 2 rr + pr: row rr, pair pr (mx + i my, mz + 0 i)
+  load_roots<T>(p, roots);
+  __syncthreads();
+  const int row0 = blockIdx.x * rows_per_cta;
+  const int nr = min(rows_per_cta, nrows - row0);
+  const int nlines = 2 * nr;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int grp = lane / B, b = lane - grp * B;
+  for (int line0 = warp * GPW; line0 < nlines; line0 += nwarps * GPW) {
+    const int line = line0 + grp;
+    const bool active = line < nlines;
+    const int rr = line >> 1, pr = line & 1;
+    V v[A];
+    if (active) {
+      const T* re = in + (long long)(2 * pr) * in_cstride + (long long)(row0 + rr) * xdata;
+#pragma unroll
+      for (int a = 0; a < A; ++a) {
+        const int x = b + B * a;
+        const bool ok = x < xdata;
+        v[a] = cmk<V>(ok ? re[x] : (T)0, (ok && pr == 0) ? re[in_cstride + x] : (T)0);
+      }
+    }
+    fft_line_regs<T, false, A, B>(v, buf + (active ? line : 0) * L, b, active, roots);
+  }
+  __syncthreads();
+  // split each pair into the half spectra of its two real rows
+  for (int line = warp; line < nlines; line += nwarps) {
+    const int rr = line >> 1, pr = line & 1;
+    const V* ln = buf + line * L;
+    const int row = row0 + rr;
+    const int z = dyd.div(row), y = row - z * ydata;
+    V* so = S + (long long)(2 * pr) * nspec + ((long long)z * nyp + y) * pitch;
+    for (int k = lane; k < hx; k += 32) {
+      const V Av = ln[k];
+      const V Bv = ln[k == 0 ? 0 : L - k];
+      so[k] = cmk<V>((T)0.5 * (Av.x + Bv.x), (T)0.5 * (Av.y - Bv.y));
+      if (pr == 0) so[nspec + k] = cmk<V>((T)0.5 * (Av.y + Bv.y), (T)-0.5 * (Av.x - Bv.x));
+    }
+  }
+}
+
+template <typename T, int A, int B>
+__global__ void k_x_inverse_w(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
+                              FastDiv dxo, FastDiv dyo, int nrows, T* __restrict__ out, long long out_cstride,
+                              int rows_per_cta, long long s_rstride, long long out_rstride) {
+  constexpr int L = A * B, GPW = 32 / B;
+  using V = C<T>;
+  const int xout = (int)dxo.d, yout = (int)dyo.d;
+  S += blockIdx.z * s_rstride;
+  out += blockIdx.z * out_rstride;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* roots = reinterpret_cast<V*>(smem_raw);
+  V* buf = roots + L;  // line 2 rr: hx + i hy of row rr; line 2 rr + 1: hz
+  load_roots<T>(p, roots);
+  __syncthreads();
+  const int row0 = blockIdx.x * rows_per_cta;
+  const int nr = min(rows_per_cta, nrows - row0);
+  const int nlines = 2 * nr;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int grp = lane / B, b = lane - grp * B;
+  for (int line0 = warp * GPW; line0 < nlines; line0 += nwarps * GPW) {
+    const int line = line0 + grp;
+    const bool active = line < nlines;
+    const int rr = line >> 1, pr = line & 1;
+    V v[A];
+    if (active) {
+      const int row = row0 + rr;
+      const int z = dyo.div(row), y = row - z * yout;
+      const V* si = S + (long long)(2 * pr) * nspec + ((long long)z * nyp + y) * pitch;
+#pragma unroll
+      for (int a = 0; a < A; ++a) {
+        const int k = b + B * a;
+        const int kk = k < hx ? k : L - k;
+        V u0 = si[kk];
+        if (k >= hx) u0.y = -u0.y;
+        if (k == 0 || 2 * k == L) u0.y = 0;  // bins that are real for a real output
+        if (pr == 0) {
+          V u1 = si[nspec + kk];
+          if (k >= hx) u1.y = -u1.y;
+          if (k == 0 || 2 * k == L) u1.y = 0;
+          v[a] = cmk<V>(u0.x - u1.y, u0.y + u1.x);
+        } else {
+          v[a] = u0;
+        }
+      }
+    }
+    fft_line_regs<T, true, A, B>(v, buf + (active ? line : 0) * L, b, active, roots);
+  }
+  __syncthreads();
+  for (int rr = warp; rr < nr; rr += nwarps) {
+    const V* l0 = buf + (2 * rr) * L;
+    const V* l1 = l0 + L;
+    T* o = out + (long long)(row0 + rr) * xout;
+    for (int x = lane; x < xout; x += 32) {
+      const V a = l0[x];
+      o[x] = a.x;
+      o[out_cstride + x] = a.y;
+      o[2 * out_cstride + x] = l1[x].x;
+    }
+  }
+}
+
 // PASS_SYM (with PASS_MUL): multiply by the real part of K^ only, i.e. by the
 // spectrum of (K(r) + K(-r)) / 2 -- the symmetrised tensor of the energy's
 // adjoint.
@@ -203,24 +331,26 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
       }
     }
   }
-  const int total = ncomp * L * ntx;
+  // thread -> (column t, first position pos0); positions advance by pstep, so
+  // the loops below need no division (tx is a power of two)
+  const int lg = __ffs(tx) - 1;
+  const int t = threadIdx.x & (tx - 1), pos0 = threadIdx.x >> lg, pstep = blockDim.x >> lg;
+  const bool tok = t < ntx;
   constexpr int LB = 8;  // loads in flight per thread
-  for (int base = threadIdx.x; base < total; base += LB * blockDim.x) {
-    V v[LB];
+  for (int c = 0; c < ncomp; ++c) {
+    const V* src = S + c * nspec + pbase + t;
+    V* dst = bufA + (long long)(c * ntx + t) * stride;
+    for (int pos = pos0; pos < L; pos += LB * pstep) {
+      V v[LB];
 #pragma unroll
-    for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * blockDim.x;
-      const int rest = dt.div(idx), t = idx - rest * ntx;
-      const int c = p.dn.div(rest), pos = rest - c * L;
-      v[u] = (idx < total && pos < load_lim) ? S[c * nspec + pbase + pos * pos_stride + t] : cmk<V>(0, 0);
-    }
+      for (int u = 0; u < LB; ++u) {
+        const int q = pos + u * pstep;
+        v[u] = (tok && q < load_lim) ? src[(long long)q * pos_stride] : cmk<V>(0, 0);
+      }
 #pragma unroll
-    for (int u = 0; u < LB; ++u) {
-      const int idx = base + u * blockDim.x;
-      if (idx < total) {
-        const int rest = dt.div(idx), t = idx - rest * ntx;
-        const int c = p.dn.div(rest), pos = rest - c * L;
-        bufA[(long long)(c * ntx + t) * stride + pos] = v[u];
+      for (int u = 0; u < LB; ++u) {
+        const int q = pos + u * pstep;
+        if (tok && q < L) dst[q] = v[u];
       }
     }
   }
@@ -237,8 +367,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
   if (flags & PASS_MUL) {
     if (kasync) asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
-    for (int idx = threadIdx.x; idx < L * ntx; idx += blockDim.x) {
-      const int pos = dt.div(idx), t = idx - pos * ntx;
+    for (int pos = pos0; tok && pos < L; pos += pstep) {
       const V* kk = lean ? khat + pbase + pos * pos_stride + t : ktile + (long long)pos * ntx + t;
       const long long ks = lean ? nspec : (long long)L * ntx;
       V kxx = kk[0], kxy = kk[ks], kxz = kk[2 * ks];
@@ -268,11 +397,12 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
       cur = r;
     }
   }
-  const FastDiv dsl((uint32_t)store_lim);
-  for (int idx = threadIdx.x; idx < ncomp * store_lim * ntx; idx += blockDim.x) {
-    const int rest = dt.div(idx), t = idx - rest * ntx;
-    const int c = dsl.div(rest), pos = rest - c * store_lim;
-    S[c * nspec + pbase + pos * pos_stride + t] = cur[(long long)(c * ntx + t) * stride + pos];
+  if (tok) {
+    for (int c = 0; c < ncomp; ++c) {
+      V* dst = S + c * nspec + pbase + t;
+      const V* src = cur + (long long)(c * ntx + t) * stride;
+      for (int pos = pos0; pos < store_lim; pos += pstep) dst[(long long)pos * pos_stride] = src[pos];
+    }
   }
 }
 
@@ -1058,6 +1188,30 @@ inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize, b
          csize;
 }
 
+// The warp-shaped x-pass kernels for the plan's (A, B), or null.
+template <typename T>
+struct XPassW {
+  void (*fwd)(FftPlan, int, FastDiv, int, const T*, long long, C<T>*, long long, int, int, int, int, long long,
+              long long);
+  void (*inv)(FftPlan, const C<T>*, long long, int, int, int, FastDiv, FastDiv, int, T*, long long, int, long long,
+              long long);
+};
+template <typename T>
+XPassW<T> x_pass_w(const FftPlan& p) {
+#define MMC_XW(A_, B_) \
+  if (p.warp_a == A_ && p.warp_b == B_) return {k_x_forward_w<T, A_, B_>, k_x_inverse_w<T, A_, B_>};
+  MMC_XW(16, 16)
+  MMC_XW(16, 8)
+  MMC_XW(8, 8)
+  MMC_XW(16, 2)
+  MMC_XW(8, 4)
+#undef MMC_XW
+  return {nullptr, nullptr};
+}
+inline size_t x_pass_w_smem(const FftPlan& p, int rows, size_t csize) {
+  return ((size_t)p.n + 2 * (size_t)rows * p.n) * csize;
+}
+
 // Raises the dynamic shared-memory limit of the FFT pass kernels to the
 // device's opt-in maximum.  Called once per device at handle creation, never
 // inside a stream capture.
@@ -1068,6 +1222,15 @@ cudaError_t prepare_impl(int max_dyn_smem) {
                        (const void*)k_x_inverse<T, false>, (const void*)k_x_inverse<T, true>,
                        (const void*)k_col_pass<T, false>,  (const void*)k_col_pass<T, true>};
   for (const void* f : fns) MMC_TRY_ATTR(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem));
+  for (int s = 0; s < 5; ++s) {
+    FftPlan p{};
+    const int ab[5][2] = {{16, 16}, {16, 8}, {8, 8}, {16, 2}, {8, 4}};
+    p.warp_a = ab[s][0];
+    p.warp_b = ab[s][1];
+    const XPassW<T> w = x_pass_w<T>(p);
+    MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)w.fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem));
+    MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)w.inv, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem));
+  }
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)mc_tile_smem<T>()));
   return cudaSuccess;
@@ -1078,6 +1241,16 @@ cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int
                           long long in_cstride, C<T>* S, long long nspec, int nyp, int hx, int pitch, int rpc,
                           int threads, cudaStream_t st, int nrep = 1, long long in_rstride = 0,
                           long long s_rstride = 0, bool inl = false) {
+  if (ncomp == 3) {
+    const XPassW<T> w = x_pass_w<T>(p);
+    if (w.fwd) {
+      dim3 grid((nrows + rpc - 1) / rpc, 1, nrep);
+      w.fwd<<<grid, threads, x_pass_w_smem(p, rpc, sizeof(C<T>)), st>>>(
+          p, xdata, FastDiv((uint32_t)ydata), nrows, in, in_cstride, S, nspec, nyp, hx, pitch, rpc, in_rstride,
+          s_rstride);
+      return cudaGetLastError();
+    }
+  }
   const int lines = (ncomp + 1) / 2;
   size_t sm = x_pass_smem(p, lines, rpc, sizeof(C<T>));
   dim3 grid((nrows + rpc - 1) / rpc, 1, nrep);
@@ -1094,6 +1267,7 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
                          int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
                          int flags, T inv_n, int tx, int threads, cudaStream_t st, int nrep = 1,
                          long long s_rstride = 0, bool inl = false, bool lean = false) {
+  if (tx < 1 || (tx & (tx - 1)) != 0 || threads % tx != 0) return cudaErrorInvalidValue;  // see k_col_pass
   lean = lean && p.warp_a != 0;  // in-place transforms exist for the warp path only
   size_t sm = lean ? col_pass_smem_lean(p, ncomp, tx, sizeof(C<T>))
                    : col_pass_smem(p, ncomp, tx, sizeof(C<T>), (flags & PASS_MUL) != 0);
@@ -1140,11 +1314,16 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
   }
   if (ev) MMC_TRY(cudaEventRecord(ev[2], st));
   const int rpc = tun.x_rows_per_cta;
-  size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
   dim3 grid((rows + rpc - 1) / rpc, 1, nrep);
-  auto kinv = tun.fft_inline ? k_x_inverse<T, true> : k_x_inverse<T, false>;
-  kinv<<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx, g.dny, rows, h, g.n, rpc,
-                                                  sr, mr);
+  const XPassW<T> w = x_pass_w<T>(px);
+  if (w.inv) {
+    w.inv<<<grid, tun.x_threads, x_pass_w_smem(px, rpc, sizeof(C<T>)), st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx,
+                                                                           g.dny, rows, h, g.n, rpc, sr, mr);
+  } else {
+    size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
+    auto kinv = tun.fft_inline ? k_x_inverse<T, true> : k_x_inverse<T, false>;
+    kinv<<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx, g.dny, rows, h, g.n, rpc, sr, mr);
+  }
   MMC_TRY(cudaGetLastError());
   if (ev) MMC_TRY(cudaEventRecord(ev[3], st));
   return cudaSuccess;
