@@ -43,6 +43,7 @@ MMC_COEF_HD inline McCoef<T> mc_coef_from(const McParams& p, double T_K) {
   k.cz[2] = (T)(p.ms * p.v * p.b[2] / kT);
   k.cd = (T)(p.demag ? p.mu0 * p.ms * p.ms * p.v / kT : 0.0);
   for (int q = 0; q < 6; ++q) k.k0[q] = (T)(p.demag ? p.k0[q] : 0.0);
+  for (int q = 0; q < 6; ++q) k.k0h[q] = (T)(p.demag ? 0.5 * (p.mu0 * p.ms * p.ms * p.v / kT) * p.k0[q] : 0.0);
   k.key0 = p.key0;
   k.key1 = p.key1;
   return k;

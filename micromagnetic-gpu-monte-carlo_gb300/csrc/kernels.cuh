@@ -539,6 +539,25 @@ __device__ __forceinline__ bool mc_accept(const McCoef<T>& c, const Nbrs<T>& nb,
   Fx = Fx + c.cz[0];
   Fy = Fy + c.cz[1];
   Fz = Fz + c.cz[2];
+  if constexpr (sizeof(T) == 4) {
+    // FP32: the same energy difference regrouped with d = m' - m, s = m' + m
+    // and K0 symmetric,
+    //   dE = -d . [F_local + cd h + (cd / 2) K0 d + can (s . u) u],
+    // where F_local is the exchange, DMI and Zeeman part of F: the terms in
+    // K0 m cancel, and the quadratic forms need no difference of squares.
+    const T ddx = p.x - ox, ddy = p.y - oy, ddz = p.z - oz;
+    if (c.cd != (T)0) {
+      Fx = Fx + c.cd * hx + (c.k0h[0] * ddx + c.k0h[1] * ddy + c.k0h[2] * ddz);
+      Fy = Fy + c.cd * hy + (c.k0h[1] * ddx + c.k0h[3] * ddy + c.k0h[4] * ddz);
+      Fz = Fz + c.cd * hz + (c.k0h[2] * ddx + c.k0h[4] * ddy + c.k0h[5] * ddz);
+    }
+    const T su = (p.x + ox) * c.u[0] + (p.y + oy) * c.u[1] + (p.z + oz) * c.u[2];
+    const T cs = c.can * su;
+    Fx = Fx + cs * c.u[0];
+    Fy = Fy + cs * c.u[1];
+    Fz = Fz + cs * c.u[2];
+    return Prop<T>::accept(-(ddx * Fx + ddy * Fy + ddz * Fz), p.ua);
+  }
   if (c.cd != (T)0) {
     const T sx = c.k0[0] * ox + c.k0[1] * oy + c.k0[2] * oz;
     const T sy = c.k0[1] * ox + c.k0[3] * oy + c.k0[4] * oz;
@@ -766,6 +785,10 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
     bool hl = true, hr = true;
     if (xl < 0) { if (g.per[0]) xl += g.nx; else hl = false; }
     if (xr >= g.nx) { if (g.per[0]) xr -= g.nx; else hr = false; }
+    // this colour's cells sit at offsets p0 and p0 + 2 (x0 is even), so only
+    // one side cell is a neighbour: the left one for p0 = 0, the right one
+    // for p0 = 1
+    const int p0 = (color + y) & 1;
     Vec4<T> own[3], up[3], dn[3];
     T lft[3], rgt[3];
 #pragma unroll
@@ -774,8 +797,8 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
       own[k] = ld4<T>(base + rowb + x0);
       up[k] = hu ? ld4<T>(base + (long long)yu * g.nx + x0) : own[k];
       dn[k] = hd ? ld4<T>(base + (long long)yd * g.nx + x0) : own[k];
-      lft[k] = hl ? base[rowb + xl] : (T)0;
-      rgt[k] = hr ? base[rowb + xr] : (T)0;
+      lft[k] = (hl && p0 == 0) ? base[rowb + xl] : (T)0;
+      rgt[k] = (hr && p0 == 1) ? base[rowb + xr] : (T)0;
     }
     Vec4<T> hh[3];
     const bool dm = c.cd != (T)0;
@@ -784,10 +807,10 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
       if (dm) hh[k] = ld4<T>(h + k * n + rowb + x0);
       else hh[k].v[0] = hh[k].v[1] = hh[k].v[2] = hh[k].v[3] = (T)0;
     }
-    // this colour's cells sit at offsets p0 and p0 + 2 (x0 is even); the
-    // offsets are compile-time inside quad_cells so the vectors stay in registers
+    // the offsets are compile-time inside quad_cells so the vectors stay in
+    // registers
     bool changed;
-    if (((color + y) & 1) == 0)
+    if (p0 == 0)
       changed = quad_cells<T, 0>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
                                  ctr->sweep, mine);
     else

@@ -84,6 +84,7 @@ struct McCoef {
   T cz[3];    // Ms V B / kT
   T cd;       // mu0 Ms^2 V / kT, 0 when demag is off
   T k0[6];    // self tensor xx, xy, xz, yy, yz, zz
+  T k0h[6];   // cd / 2 * k0 (the FP32 form of dE)
   uint32_t key0, key1;  // Philox key = seed
 };
 
