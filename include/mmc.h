@@ -337,7 +337,8 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
  * passes, the band of the film row kernel (0 when sweeps use one kernel per
  * pass), and the Metropolis form: 0 one launch per colour, 1 both colours of
  * a film in one tile launch, 2 one vectorised launch per colour (films with
- * nx a multiple of 4), whether the pass kernels expand their transforms in
+ * nx a multiple of 4), 3 the same with each CTA's rows staged in shared
+ * memory by asynchronous copies (nx also at most 1024), whether the pass kernels expand their transforms in
  * line (1) or call them out of line (0), and whether the column passes
  * transform in place reading the tensor from global memory (1), and the
  * number of streams (1-4) the batch's replicas are split over. */

@@ -7,6 +7,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "fft.cuh"
 #include "mmc_internal.h"
 #include "mmc_math.h"
@@ -478,12 +480,18 @@ struct Prop<double> {
 
 template <>
 struct Prop<float> {
+  // FP32: the hardware sine and cosine of phi - pi in (-pi, pi), where their
+  // absolute error is about 4e-7, negated (exact), and sqrt(t) as t / sqrt(t)
+  // from the hardware reciprocal square root; t = 1 - z^2 >= 2^-22 because
+  // u01_f32 never returns 0 or 1.
   __device__ static void draw(mmcm::u32x4 r, float& px, float& py, float& pz, float& ua) {
     pz = 2.0f * mmcm::u01_f32(r.x) - 1.0f;
-    float s = sqrtf(fmaxf(0.0f, 1.0f - pz * pz)), sn, cs;
-    sincospif(2.0f * mmcm::u01_f32(r.y), &sn, &cs);
-    px = s * cs;
-    py = s * sn;
+    const float t = 1.0f - pz * pz;
+    const float s = t * rsqrtf(t);
+    float sn, cs;
+    __sincosf(6.28318530717958647692f * mmcm::u01_f32(r.y) - 3.14159265358979323846f, &sn, &cs);
+    px = -(s * cs);
+    py = -(s * sn);
     ua = mmcm::u01_f32(r.z);
   }
   __device__ static bool accept(float dE, float ua) { return dE <= 0.0f || ua < __expf(-dE); }
@@ -718,11 +726,14 @@ __device__ __forceinline__ void st4(T* p, const Vec4<T>& r) {
 }
 
 // The decisions of the two cells at offsets P0 and P0 + 2 of a segment.
-template <typename T, int P0>
+// ALLB: every x and y bond exists (both axes periodic, ny > 1), so the
+// availability flags are compile-time true.
+template <typename T, int P0, bool ALLB>
 __device__ __forceinline__ bool quad_cells(const McCoef<T>& c, Vec4<T> (&own)[3], const Vec4<T> (&up)[3],
                                            const Vec4<T> (&dn)[3], const T (&lft)[3], const T (&rgt)[3],
                                            const Vec4<T> (&hh)[3], bool hl, bool hr, bool hd, bool hu,
                                            uint32_t cell0, uint32_t stage, uint32_t sweep, unsigned int& mine) {
+  if constexpr (ALLB) hl = hr = hd = hu = true;
   bool changed = false;
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
@@ -756,8 +767,14 @@ __device__ __forceinline__ bool quad_cells(const McCoef<T>& c, Vec4<T> (&own)[3]
 }
 
 __host__ __device__ inline bool mc_quad_ok(const Geom& g) { return g.nz == 1 && g.ncolors == 2 && g.nx % 4 == 0; }
+// every x and y bond of a film exists
+__host__ __device__ inline bool mc_all_bonds(const Geom& g) { return g.per[0] && g.per[1] && g.nx > 1 && g.ny > 1; }
+// the staged form (k_mc_band) for the same lattices, up to 1024 cells per row
+// (a band of one row then fits in 96 KB of shared memory in FP64)
+constexpr size_t MC_BAND_SMEM_MAX = 96 * 1024;
+__host__ __device__ inline bool mc_band_ok(const Geom& g) { return mc_quad_ok(g) && g.nx <= 1024; }
 
-template <typename T>
+template <typename T, bool ALLB>
 __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m,
                                                  const T* __restrict__ h, const SweepCounters* __restrict__ ctr,
                                                  int color, unsigned long long* acc) {
@@ -785,6 +802,7 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
     bool hl = true, hr = true;
     if (xl < 0) { if (g.per[0]) xl += g.nx; else hl = false; }
     if (xr >= g.nx) { if (g.per[0]) xr -= g.nx; else hr = false; }
+    if constexpr (ALLB) hu = hd = hl = hr = true;
     // this colour's cells sit at offsets p0 and p0 + 2 (x0 is even), so only
     // one side cell is a neighbour: the left one for p0 = 0, the right one
     // for p0 = 1
@@ -811,10 +829,127 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
     // registers
     bool changed;
     if (p0 == 0)
-      changed = quad_cells<T, 0>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
+      changed = quad_cells<T, 0, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
                                  ctr->sweep, mine);
     else
-      changed = quad_cells<T, 1>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
+      changed = quad_cells<T, 1, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
+                                 ctr->sweep, mine);
+    if (changed) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) st4<T>(m + k * n + rowb + x0, own[k]);
+    }
+  }
+  unsigned int v = mine;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, (unsigned long long)v);
+}
+
+// One colour of a two-colour film sweep (the k_mc_quad cases) with the rows
+// a CTA needs staged in shared memory first: the CTA owns a band of `band`
+// rows of one replica, copies m rows y0-1 .. y0+band (wrapped on a periodic
+// axis) and h rows y0 .. y0+band-1 with 16-byte asynchronous copies, which
+// hold no registers while they land, and then runs k_mc_quad's per-thread
+// work (4-cell segments, the same quad_cells) from shared memory.  Fewer
+// registers per thread than k_mc_quad, whose vector loads all sit in
+// registers at once, so more warps per SM hide the copies' latency.
+// Shared memory: (band + 2) x 3 rows of m and band x 3 rows of h.
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+template <typename T>
+__host__ __device__ inline size_t mc_band_smem(const Geom& g, int band) {
+  return (size_t)(2 * band + 2) * 3 * g.nx * sizeof(T);
+}
+// rows per CTA: about one 4-cell segment per thread
+template <typename T>
+inline int mc_band_rows(const Geom& g, int threads) {
+  int band = std::max(1, std::min(g.ny, 4 * threads / g.nx));
+  while (band > 1 && mc_band_smem<T>(g, band) > MC_BAND_SMEM_MAX) band /= 2;
+  return band;
+}
+
+// (Three CTAs of 256 threads per SM in FP32 -- 80 registers, a few spilled
+// -- and two in FP64.)
+template <typename T, bool ALLB>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_mc_band(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m,
+                                                    const T* __restrict__ h, const SweepCounters* __restrict__ ctr,
+                                                    int color, int band, FastDiv dchunk, FastDiv dseg,
+                                                    unsigned long long* acc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nx = g.nx, ny = g.ny;
+  const long long n = g.n;
+  T* ms = reinterpret_cast<T*>(smem_raw);  // [slot][comp][x], slot s = row y0 - 1 + s
+  T* hs = ms + (size_t)(band + 2) * 3 * nx;  // [row][comp][x]
+  const McCoef<T> c = cp[blockIdx.z];
+  m += blockIdx.z * 3 * n;
+  h += blockIdx.z * 3 * n;
+  acc += blockIdx.z;
+  const int y0 = blockIdx.x * band;
+  const int nb = min(band, ny - y0);
+  const bool dm = c.cd != (T)0;
+  const int per = (int)dchunk.d;  // 16-byte chunks per row
+  constexpr int E = 16 / (int)sizeof(T);
+  const int nm = (nb + 2) * 3 * per, nh = dm ? nb * 3 * per : 0;
+  for (int i = threadIdx.x; i < nm + nh; i += blockDim.x) {
+    const bool isM = i < nm;
+    const int j = isM ? i : i - nm;
+    const int row = dchunk.div(j), q = j - row * per;  // row = slot * 3 + comp (m) or r * 3 + comp (h)
+    const int slot = row / 3, comp = row - slot * 3;
+    if (isM) {
+      int y = y0 - 1 + slot;
+      if (y < 0 || y >= ny) {
+        if (!g.per[1] || ny == 1) continue;
+        y = y < 0 ? y + ny : y - ny;
+      }
+      cp_async16(ms + (size_t)row * nx + q * E, m + comp * n + (long long)y * nx + q * E);
+    } else {
+      cp_async16(hs + (size_t)row * nx + q * E, h + comp * n + (long long)(y0 + slot) * nx + q * E);
+    }
+  }
+  cp_async_wait_all();
+  __syncthreads();
+  const int nseg = (int)dseg.d;
+  unsigned int mine = 0;
+  for (int t = threadIdx.x; t < nb * nseg; t += blockDim.x) {
+    const int rr = dseg.div(t), s = t - rr * nseg;
+    const int y = y0 + rr;
+    const int x0 = 4 * s;
+    bool hu = true, hd = true;
+    if (y + 1 >= ny && !g.per[1]) hu = false;
+    if (y - 1 < 0 && !g.per[1]) hd = false;
+    if (ny == 1) hu = hd = false;
+    int xl = x0 - 1, xr = x0 + 4;
+    bool hl = true, hr = true;
+    if (xl < 0) { if (g.per[0]) xl += nx; else hl = false; }
+    if (xr >= nx) { if (g.per[0]) xr -= nx; else hr = false; }
+    if constexpr (ALLB) hu = hd = hl = hr = true;
+    const int p0 = (color + y) & 1;
+    const T* own_r = ms + (size_t)(rr + 1) * 3 * nx;
+    const T* up_r = own_r + 3 * nx;
+    const T* dn_r = own_r - 3 * nx;
+    Vec4<T> own[3], up[3], dn[3], hh[3];
+    T lft[3], rgt[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      own[k] = ld4<T>(own_r + k * nx + x0);
+      up[k] = hu ? ld4<T>(up_r + k * nx + x0) : own[k];
+      dn[k] = hd ? ld4<T>(dn_r + k * nx + x0) : own[k];
+      lft[k] = (hl && p0 == 0) ? own_r[k * nx + xl] : (T)0;
+      rgt[k] = (hr && p0 == 1) ? own_r[k * nx + xr] : (T)0;
+      if (dm) hh[k] = ld4<T>(hs + ((size_t)rr * 3 + k) * nx + x0);
+      else hh[k].v[0] = hh[k].v[1] = hh[k].v[2] = hh[k].v[3] = (T)0;
+    }
+    const long long rowb = (long long)y * nx;
+    bool changed;
+    if (p0 == 0)
+      changed = quad_cells<T, 0, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
+                                 ctr->sweep, mine);
+    else
+      changed = quad_cells<T, 1, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
                                  ctr->sweep, mine);
     if (changed) {
 #pragma unroll
@@ -1256,6 +1391,10 @@ cudaError_t prepare_impl(int max_dyn_smem) {
   }
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_tile<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)mc_tile_smem<T>()));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_band<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)MC_BAND_SMEM_MAX));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_band<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)MC_BAND_SMEM_MAX));
   return cudaSuccess;
 }
 
@@ -1367,10 +1506,19 @@ cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const S
     for (int col = 0; col < g.ncolors; ++col) MMC_TRY(mc_impl<T>(g, c, m, h, ctr, col, acc, st, nrep, form));
     return cudaSuccess;
   }
+  if (form == MC_FORM_BAND && mc_band_ok(g)) {
+    const int band = mc_band_rows<T>(g, threads);
+    dim3 grid((unsigned)((g.ny + band - 1) / band), 1, nrep);
+    auto kern = mc_all_bonds(g) ? k_mc_band<T, true> : k_mc_band<T, false>;
+    kern<<<grid, threads, mc_band_smem<T>(g, band), st>>>(
+        g, c, m, h, ctr, color, band, FastDiv((uint32_t)(g.nx * sizeof(T) / 16)), FastDiv((uint32_t)(g.nx / 4)), acc);
+    return cudaGetLastError();
+  }
   if (form == MC_FORM_QUAD && mc_quad_ok(g)) {
     const long long total = (long long)g.ny * (g.nx >> 2);
     dim3 grid((unsigned)((total + threads - 1) / threads), 1, nrep);
-    k_mc_quad<T><<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);
+    auto kern = mc_all_bonds(g) ? k_mc_quad<T, true> : k_mc_quad<T, false>;
+    kern<<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);
     return cudaGetLastError();
   }
   if (g.ncolors == 2) {

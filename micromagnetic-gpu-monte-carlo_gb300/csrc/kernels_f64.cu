@@ -14,6 +14,7 @@ MMC_INSTANTIATE_LAUNCHERS(double)
 static_assert(MCT == MC_TILE_SIDE, "tile side");
 bool mc_tile_eligible(const Geom& g) { return mc_tile_ok(g); }
 bool mc_quad_eligible(const Geom& g) { return mc_quad_ok(g); }
+bool mc_band_eligible(const Geom& g) { return mc_band_ok(g); }
 MMC_INSTANTIATE_FUSED(double)
 MMC_INSTANTIATE_GRAD(double)
 

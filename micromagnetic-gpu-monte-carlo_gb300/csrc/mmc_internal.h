@@ -142,7 +142,9 @@ cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, co
 // Metropolis kernel forms (all make the same decisions): one scalar launch
 // per colour; both colours of a film in one tile launch; one vectorised launch
 // per colour for films with nx a multiple of 4.
-enum : int { MC_FORM_SCALAR = 0, MC_FORM_TILE = 1, MC_FORM_QUAD = 2 };
+// (MC_FORM_BAND: the vectorised form with the CTA's rows staged in shared
+// memory by asynchronous copies.)
+enum : int { MC_FORM_SCALAR = 0, MC_FORM_TILE = 1, MC_FORM_QUAD = 2, MC_FORM_BAND = 3 };
 // color < 0: every colour of the sweep in the given form (falls back to the
 // scalar form where the lattice does not qualify).
 template <typename T>
@@ -151,6 +153,7 @@ cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const
 // Whether a lattice can use the tile form (and its tile side) or the vector form.
 bool mc_tile_eligible(const Geom& g);
 bool mc_quad_eligible(const Geom& g);
+bool mc_band_eligible(const Geom& g);
 constexpr int MC_TILE_SIDE = 32;
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials,

@@ -300,18 +300,13 @@ struct u32x4 {
   uint32_t x, y, z, w;
 };
 
-MMC_HD uint32_t mulhi32(uint32_t a, uint32_t b) {
-#if defined(__CUDA_ARCH__)
-  return __umulhi(a, b);
-#else
-  return (uint32_t)(((uint64_t)a * (uint64_t)b) >> 32);
-#endif
-}
-
 MMC_HD u32x4 philox_round(u32x4 c, uint32_t k0, uint32_t k1) {
   const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
-  uint32_t hi0 = mulhi32(M0, c.x), lo0 = M0 * c.x;
-  uint32_t hi1 = mulhi32(M1, c.z), lo1 = M1 * c.z;
+  // one 32 x 32 -> 64-bit product per multiplier (a single wide multiply-add
+  // on the GPU); hi and lo are its halves
+  const uint64_t p0 = (uint64_t)M0 * c.x, p1 = (uint64_t)M1 * c.z;
+  const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+  const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
   u32x4 r;
   r.x = hi1 ^ c.y ^ k0;
   r.y = lo1;

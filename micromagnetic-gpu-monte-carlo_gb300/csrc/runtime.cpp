@@ -1541,6 +1541,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   {
     std::vector<int> forms;
     if (mc_quad_eligible(g)) forms.push_back(MC_FORM_QUAD);
+    if (mc_band_eligible(g)) forms.push_back(MC_FORM_BAND);
     if (mc_tile_eligible(g)) forms.push_back(MC_FORM_TILE);
     forms.push_back(MC_FORM_SCALAR);
     const Cand pass_best = best;
@@ -2166,8 +2167,9 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
       !pow2(t.col_tx) || t.col_tx > 8 || col_pass_smem(h->py.p, t.col_tx, cs) > smem_limit() || !pow2(t.col_tx_z) ||
       t.col_tx_z > 8 || col_pass_smem(h->pz.p, t.col_tx_z, cs) > smem_limit() ||
       (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
-      t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_QUAD ||
+      t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_BAND ||
       (t.mc_form == MC_FORM_TILE && !mc_tile_eligible(g)) || (t.mc_form == MC_FORM_QUAD && !mc_quad_eligible(g)) ||
+      (t.mc_form == MC_FORM_BAND && !mc_band_eligible(g)) ||
       (t.fft_inline != 0 && t.fft_inline != 1) || (t.col_lean != 0 && t.col_lean != 1))
     return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
   if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())

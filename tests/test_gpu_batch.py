@@ -83,20 +83,24 @@ TILE_GEOMS = [dict(nx=64, ny=64, pbc_x=1, pbc_y=1), dict(nx=96, ny=41, pbc_x=1, 
 
 
 def form_ok(geom, form):
-    """Eligibility of the tile (1) and vector (2) forms for a two-colour film."""
+    """Eligibility of the tile (1), vector (2) and staged vector (3) forms for a
+    two-colour film."""
     nx, ny = geom["nx"], geom["ny"]
     if form == 2:
         return nx % 4 == 0
+    if form == 3:
+        return nx % 4 == 0 and nx <= 1024
     per_ok = lambda n, p: p == 0 or (n % 32 == 0 and n >= 64)
     return per_ok(nx, geom.get("pbc_x", 2)) and per_ok(ny, geom.get("pbc_y", 1))
 
 
 @pytest.mark.parametrize("prec", [32, 64])
 @pytest.mark.parametrize("geom", TILE_GEOMS)
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("form", [1, 2, 3])
 def test_mc_forms_bitwise_equal_scalar_kernels(M, prec, geom, form):
-    """Both colours in one tile launch (ring of colour-0 cells recomputed), or
-    the vectorised per-colour form, against the scalar per-colour form."""
+    """Both colours in one tile launch (ring of colour-0 cells recomputed), the
+    vectorised per-colour form, or the same with the rows staged in shared
+    memory, against the scalar per-colour form."""
     if not form_ok(geom, form):
         pytest.skip("form not available for this lattice (checked in test_mc_forms_rejected_where_ineligible)")
     cfgs = cfgs_for(M, 3, prec, sweep_engine=1, **geom)
@@ -114,7 +118,7 @@ def test_mc_forms_bitwise_equal_scalar_kernels(M, prec, geom, form):
         assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
 
 
-@pytest.mark.parametrize("form", [1, 2])
+@pytest.mark.parametrize("form", [1, 2, 3])
 def test_mc_forms_fp64_decisions_match_oracle(M, O, form):
     c = cfgs_for(M, 1, 64, sweep_engine=1, nx=64, ny=64, pbc_x=1, pbc_y=1)[0]
     with M.Batch([c]) as b:
@@ -174,11 +178,19 @@ def test_mc_forms_rejected_where_ineligible(M):
         s[6] = 1
         with pytest.raises(M.MmcError):
             b.set_launch_shape(s)
-    # the vector form needs nx % 4 == 0
+    # the vector forms need nx % 4 == 0, the staged one also nx <= 1024
     with M.Batch(cfgs_for(M, 1, 32, nx=18, ny=8, pbc_x=1, pbc_y=1)) as b:
         s = list(b.launch_shape())
         assert s[6] == 0
+        for form in (2, 3):
+            s[6] = form
+            with pytest.raises(M.MmcError):
+                b.set_launch_shape(s)
+    with M.Batch(cfgs_for(M, 1, 32, nx=1040, ny=2, pbc_x=1, pbc_y=1)) as b:
+        s = list(b.launch_shape())
         s[6] = 2
+        b.set_launch_shape(s)
+        s[6] = 3
         with pytest.raises(M.MmcError):
             b.set_launch_shape(s)
 
