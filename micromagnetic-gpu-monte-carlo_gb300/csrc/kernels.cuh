@@ -296,7 +296,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw = reinterpret_cast<V*>(smem_raw);
   const int L = p.n;
-  const int stride = L + 1;
+  const int stride = col_line_stride(L, sizeof(V));
   const int kx0 = blockIdx.x * tx;
   const int ntx = min(tx, hx - kx0);
   const long long pbase = (long long)blockIdx.y * plane_stride + kx0;
@@ -1339,10 +1339,11 @@ inline size_t x_pass_smem(const FftPlan& p, int lines_per_row, int rows, size_t 
   return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)rows * lines_per_row * p.n) * csize;
 }
 inline size_t col_pass_smem_lean(const FftPlan& p, int ncomp, int tx, size_t csize) {
-  return ((size_t)((p.tw_total + 1) & ~1) + (size_t)ncomp * tx * (p.n + 1)) * csize;
+  return ((size_t)((p.tw_total + 1) & ~1) + (size_t)ncomp * tx * col_line_stride(p.n, csize)) * csize;
 }
 inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize, bool mul) {
-  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)ncomp * tx * (p.n + 1) + (mul ? 6 * (size_t)p.n * tx : 0)) *
+  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)ncomp * tx * col_line_stride(p.n, csize) +
+          (mul ? 6 * (size_t)p.n * tx : 0)) *
          csize;
 }
 

@@ -176,7 +176,7 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   while (r > 1 && xsm(r) > 96 * 1024) r /= 2;
   t.x_rows_per_cta = r;
   auto csm = [&](const FftPlan& p, int tx) {
-    return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * (p.n + 1) + 6 * (size_t)p.n * tx) * csize;
+    return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * col_line_stride(p.n, csize) + 6 * (size_t)p.n * tx) * csize;
   };
   auto pick = [&](const FftPlan& p, int planes) {
     int tx = 8;
@@ -202,7 +202,7 @@ size_t x_pass_smem(const FftPlan& px, int r, size_t csize) {
   return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize;
 }
 size_t col_pass_smem(const FftPlan& p, int tx, size_t csize) {
-  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * (p.n + 1) + 6 * (size_t)p.n * tx) * csize;
+  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * col_line_stride(p.n, csize) + 6 * (size_t)p.n * tx) * csize;
 }
 
 }  // namespace
@@ -694,10 +694,10 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
     }
     DemagTuning tt = h->tun;
     // six-component setup transform: narrower tiles keep shared memory in budget
-    while (tt.col_tx > 1 && ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx * (h->py.p.n + 1)) *
+    while (tt.col_tx > 1 && ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx * col_line_stride(h->py.p.n, sizeof(double2))) *
                                     sizeof(double2) > smem_limit())
       tt.col_tx /= 2;
-    while (tt.col_tx_z > 1 && ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx_z * (h->pz.p.n + 1)) *
+    while (tt.col_tx_z > 1 && ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx_z * col_line_stride(h->pz.p.n, sizeof(double2))) *
                                       sizeof(double2) > smem_limit())
       tt.col_tx_z /= 2;
     tt.col_tx = std::min(tt.col_tx, tt.col_tx_z);
@@ -951,8 +951,8 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   h->nsm = nsm;
   // shared-memory feasibility of the per-sweep passes
   if (((size_t)((h->px.p.tw_total + 1) & ~1) + 2 * 2 * (size_t)h->px.p.n) * csize > smem_limit() ||
-      ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)(h->py.p.n + 1)) * csize > smem_limit() ||
-      ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)(h->pz.p.n + 1)) * csize > smem_limit() ||
+      ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)col_line_stride(h->py.p.n, csize)) * csize > smem_limit() ||
+      ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)col_line_stride(h->pz.p.n, csize)) * csize > smem_limit() ||
       ((size_t)((h->px.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)h->px.p.n) * 16 > smem_limit())
     return bail(fail(MMC_ERR_UNSUPPORTED, "padded lattice dimension too large for the shared-memory FFT"));
   auto alloc = [&](void** p, size_t bytes) -> int {
