@@ -363,7 +363,7 @@ def run_ours(args):
         batch.set_launch_shape([int(v) for v in args.launch_shape.split(",")])
         tune_ms, tune_n = None, 0
     else:
-        tune_ms, tune_n = batch.autotune(32)
+        tune_ms, tune_n = batch.autotune(96)
     tune_s = time.perf_counter() - t0
     n = 65536
 

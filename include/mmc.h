@@ -348,7 +348,8 @@ int mmc_batch_launch_shape(mmc_batch* b, int out[10]);
  * CTA and 1-8 kx columns per column-pass tile, then -- one dimension at a
  * time from the fastest so far -- the transforms in and out of line, the
  * in-place column passes, every Metropolis form, 2-4 streams) for `sweeps`
- * sweeps (the faster of two repetitions) from the
+ * sweeps (the faster of two repetitions; replays of the 32-sweep graph that
+ * runs execute, so `sweeps` is rounded up to a multiple of 32) from the
  * current state, keeps the fastest and restores m and the acceptance
  * counters.  Every shape gives bit-identical results, so the choice changes
  * only the speed.  best_ms_per_sweep and candidates may be NULL.  No

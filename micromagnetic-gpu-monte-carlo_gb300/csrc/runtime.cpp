@@ -1280,9 +1280,14 @@ cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
   mmc_handle* h = b->base;
   cudaError_t e;
   const int parts = std::min(b->streams, b->R);
-  if (parts > 1 && !ev && b->sts[0]) {
-    // replica parts on their own streams: kernels of different kinds overlap
-    // on the SMs; part 0 stays on the batch's stream
+  // replica parts on their own streams while a graph is captured (as parallel
+  // branches, kernels of different kinds overlap on the SMs); launched
+  // directly, the extra launches and events cost more than they give, and
+  // every launch shape gives the same results, so direct sweeps use one stream
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (parts > 1 && (e = cudaStreamIsCapturing(h->st, &cap)) != cudaSuccess) return e;
+  if (parts > 1 && !ev && b->sts[0] && cap == cudaStreamCaptureStatusActive) {
+    // part 0 stays on the batch's stream
     if ((e = cudaEventRecord(b->fork, h->st)) != cudaSuccess) return e;
     for (int k = 1; k < parts; ++k)
       if ((e = cudaStreamWaitEvent(b->sts[k - 1], b->fork, 0)) != cudaSuccess) return e;
@@ -1490,16 +1495,26 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     e = cudaMemcpyAsync(b->m, saved, mbytes, cudaMemcpyDeviceToDevice, h->st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st);
     if (e == cudaSuccess && b->rows_band > 0) e = batch_demag(b);
-    if (e == cudaSuccess) e = batch_sweeps(b, 2);  // warm-up
-    // the faster of two timed repetitions
+    // timed the way runs execute: replays of a captured graph of
+    // BATCH_GRAPH_SWEEPS sweeps with this shape
+    if (e == cudaSuccess) {
+      if (b->gexec) cudaGraphExecDestroy(b->gexec);
+      b->gexec = nullptr;
+      b->graph_len = 0;
+      if ((status = batch_graph(b, BATCH_GRAPH_SWEEPS, false)) != MMC_OK) return;
+    }
+    const int reps = std::max(1, (sweeps + BATCH_GRAPH_SWEEPS - 1) / BATCH_GRAPH_SWEEPS);
+    if (e == cudaSuccess) e = cudaGraphLaunch(b->gexec, h->st);  // warm-up
+    // the faster of two timed repetitions, per sweep
     float ms = -1;
     for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
       if (e == cudaSuccess) e = cudaEventRecord(h->ev[0], h->st);
-      if (e == cudaSuccess) e = batch_sweeps(b, sweeps);
+      for (int i = 0; i < reps && e == cudaSuccess; ++i) e = cudaGraphLaunch(b->gexec, h->st);
       if (e == cudaSuccess) e = cudaEventRecord(h->ev[1], h->st);
       if (e == cudaSuccess) e = cudaEventSynchronize(h->ev[1]);
       float t = 0;
       if (e == cudaSuccess) e = cudaEventElapsedTime(&t, h->ev[0], h->ev[1]);
+      t /= (float)(reps * BATCH_GRAPH_SWEEPS);
       if (e == cudaSuccess && (ms < 0 || t < ms)) ms = t;
     }
     if (e == cudaSuccess && (best_t < 0 || ms < best_t)) {
@@ -1582,7 +1597,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   b->graph_len = 0;
   if (status != MMC_OK) return status;
   CU(e);
-  if (best_ms) *best_ms = best_t / sweeps;
+  if (best_ms) *best_ms = best_t;
   if (ncand) *ncand = tried;
   return MMC_OK;
 }
