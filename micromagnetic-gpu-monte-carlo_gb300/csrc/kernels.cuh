@@ -164,8 +164,10 @@ __device__ __forceinline__ void load_roots(const FftPlan& p, C<T>* dst) {
   for (int i = threadIdx.x; i < p.n; i += blockDim.x) dst[i] = src[i];
 }
 
+// (Register budget: 64 per thread in FP32, so that eight 128-thread CTAs fit
+// on an SM; 128 in FP64.)
 template <typename T, int A, int B>
-__global__ void k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
                               long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, int hx,
                               int pitch, int rows_per_cta, long long in_rstride, long long s_rstride) {
   constexpr int L = A * B, GPW = 32 / B;
@@ -175,7 +177,7 @@ __global__ void k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, cons
   S += blockIdx.z * s_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* roots = reinterpret_cast<V*>(smem_raw);
-  V* buf = roots + L;  // line 2 rr + pr: row rr, pair pr (mx + i my, mz + 0 i)
+  V* buf = roots + L;  // line pr * nr + rr: row rr, pair pr (mx + i my, mz + 0 i)
   load_roots<T>(p, roots);
   __syncthreads();
   const int row0 = blockIdx.x * rows_per_cta;
@@ -183,10 +185,11 @@ __global__ void k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, cons
   const int nlines = 2 * nr;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int grp = lane / B, b = lane - grp * B;
+  // pair-major line order: the groups of a warp mostly load the same pair
   for (int line0 = warp * GPW; line0 < nlines; line0 += nwarps * GPW) {
     const int line = line0 + grp;
     const bool active = line < nlines;
-    const int rr = line >> 1, pr = line & 1;
+    const int pr = line >= nr ? 1 : 0, rr = line - pr * nr;
     V v[A];
     if (active) {
       const T* re = in + (long long)(2 * pr) * in_cstride + (long long)(row0 + rr) * xdata;
@@ -202,7 +205,7 @@ __global__ void k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, cons
   __syncthreads();
   // split each pair into the half spectra of its two real rows
   for (int line = warp; line < nlines; line += nwarps) {
-    const int rr = line >> 1, pr = line & 1;
+    const int pr = line >= nr ? 1 : 0, rr = line - pr * nr;
     const V* ln = buf + line * L;
     const int row = row0 + rr;
     const int z = dyd.div(row), y = row - z * ydata;
@@ -217,7 +220,7 @@ __global__ void k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, cons
 }
 
 template <typename T, int A, int B>
-__global__ void k_x_inverse_w(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_x_inverse_w(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
                               FastDiv dxo, FastDiv dyo, int nrows, T* __restrict__ out, long long out_cstride,
                               int rows_per_cta, long long s_rstride, long long out_rstride) {
   constexpr int L = A * B, GPW = 32 / B;
@@ -227,7 +230,7 @@ __global__ void k_x_inverse_w(FftPlan p, const C<T>* __restrict__ S, long long n
   out += blockIdx.z * out_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* roots = reinterpret_cast<V*>(smem_raw);
-  V* buf = roots + L;  // line 2 rr: hx + i hy of row rr; line 2 rr + 1: hz
+  V* buf = roots + L;  // line rr: hx + i hy of row rr; line nr + rr: hz
   load_roots<T>(p, roots);
   __syncthreads();
   const int row0 = blockIdx.x * rows_per_cta;
@@ -238,7 +241,7 @@ __global__ void k_x_inverse_w(FftPlan p, const C<T>* __restrict__ S, long long n
   for (int line0 = warp * GPW; line0 < nlines; line0 += nwarps * GPW) {
     const int line = line0 + grp;
     const bool active = line < nlines;
-    const int rr = line >> 1, pr = line & 1;
+    const int pr = line >= nr ? 1 : 0, rr = line - pr * nr;
     V v[A];
     if (active) {
       const int row = row0 + rr;
@@ -265,8 +268,8 @@ __global__ void k_x_inverse_w(FftPlan p, const C<T>* __restrict__ S, long long n
   }
   __syncthreads();
   for (int rr = warp; rr < nr; rr += nwarps) {
-    const V* l0 = buf + (2 * rr) * L;
-    const V* l1 = l0 + L;
+    const V* l0 = buf + rr * L;
+    const V* l1 = buf + (nr + rr) * L;
     T* o = out + (long long)(row0 + rr) * xout;
     for (int x = lane; x < xout; x += 32) {
       const V a = l0[x];
