@@ -59,10 +59,13 @@ cudaError_t launch_tensor_fft(const Geom& g, const FftPlan& px, const FftPlan& p
   return cudaSuccess;
 }
 
-__global__ void k_advance(SweepCounters* ctr, uint32_t delta) { ctr->sweep += delta; }
+__global__ void k_advance(SweepCounters* ctr, uint32_t delta, int count) {
+  if ((int)threadIdx.x < count) ctr[threadIdx.x].sweep += delta;
+}
 
-cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st) {
-  k_advance<<<1, 1, 0, st>>>(ctr, delta);
+cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st, int count) {
+  if (count < 1 || count > 32) return cudaErrorInvalidValue;
+  k_advance<<<1, 32, 0, st>>>(ctr, delta, count);
   return cudaGetLastError();
 }
 

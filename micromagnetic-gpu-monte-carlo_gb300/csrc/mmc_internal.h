@@ -204,7 +204,8 @@ cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px
                           double far_r2 = 0.0);
 cudaError_t launch_tensor_fft(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                               const DemagTuning& tun, const double* k6, double2* spec64, cudaStream_t st);
-cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st);
+// Advances the sweep counter of `count` (<= 32) consecutive SweepCounters.
+cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st, int count = 1);
 cudaError_t launch_philox_selftest(long long n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out,
                                    uint32_t* out_curand, cudaStream_t st);
 

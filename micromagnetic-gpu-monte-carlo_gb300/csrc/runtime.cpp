@@ -1113,6 +1113,8 @@ int anneal_loop(mmc_handle* h, const std::string& dir, int verbose) {
 // fills a corner of it.  Replicas may differ in material, field, seed and
 // temperature; the tensor spectrum is shared.  Optional parallel-tempering
 // ladders swap temperatures on the device every `swap_interval` sweeps.
+constexpr int CTR_SLOTS = 32;
+
 struct mmc_batch {
   mmc_handle* base = nullptr;  // geometry, plans, tensor (replica 0's config)
   int R = 0;
@@ -1137,7 +1139,10 @@ struct mmc_batch {
   double* red = nullptr;
   double* red_host = nullptr;
   unsigned long long* acc = nullptr;
+  // CTR_SLOTS counters, slot q = (stage, sweep + q): sweep q of a captured
+  // graph reads slot q, and one advance per graph moves them all on
   SweepCounters* ctr = nullptr;
+  SweepCounters ctr_host[CTR_SLOTS];
   // parallel tempering
   int interval = 0;
   PtDevice pt{};
@@ -1218,7 +1223,7 @@ int batch_alloc_rows(mmc_batch* b) {
 // the read spectrum to hold K^.M^/N of the read m (the previous sweep's column
 // pass, or batch_demag).  ev (optional): [0] before the row kernel, [1] before
 // the column pass, [2] after it.
-cudaError_t batch_sweep_rows(mmc_batch* b, int parity, cudaEvent_t* ev = nullptr) {
+cudaError_t batch_sweep_rows(mmc_batch* b, int parity, cudaEvent_t* ev, int slot) {
   mmc_handle* h = b->base;
   void* mi = parity ? b->m2 : b->m;
   void* mo = parity ? b->m : b->m2;
@@ -1227,9 +1232,9 @@ cudaError_t batch_sweep_rows(mmc_batch* b, int parity, cudaEvent_t* ev = nullptr
   cudaError_t e;
   if (ev && (e = cudaEventRecord(ev[0], h->st)) != cudaSuccess) return e;
   e = h->prec == 32 ? launch_rows<float>(h->g, h->px.p, (const McCoef<float>*)b->coef, (const float*)mi, (float*)mo,
-                                         (float*)b->h, si, so, b->acc, b->ctr, b->rows_band, b->R, false, true, h->st)
+                                         (float*)b->h, si, so, b->acc, b->ctr + slot, b->rows_band, b->R, false, true, h->st)
                     : launch_rows<double>(h->g, h->px.p, (const McCoef<double>*)b->coef, (const double*)mi,
-                                          (double*)mo, (double*)b->h, si, so, b->acc, b->ctr, b->rows_band, b->R,
+                                          (double*)mo, (double*)b->h, si, so, b->acc, b->ctr + slot, b->rows_band, b->R,
                                           false, true, h->st);
   if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[1], h->st)) != cudaSuccess) return e;
@@ -1237,7 +1242,7 @@ cudaError_t batch_sweep_rows(mmc_batch* b, int parity, cudaEvent_t* ev = nullptr
                     : launch_col_pass_2d<double>(h->g, h->py.p, b->tun, so, h->khat, h->st, b->R);
   if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[2], h->st)) != cudaSuccess) return e;
-  return launch_advance(b->ctr, 1, h->st);
+  return cudaSuccess;
 }
 
 // After an odd number of row-kernel sweeps the state sits in the second
@@ -1262,7 +1267,7 @@ int batch_alloc_streams(mmc_batch* b) {
 
 // One sweep of replicas [r0, r0 + nr) on stream st.
 template <typename T>
-cudaError_t batch_sweep_part(mmc_batch* b, int r0, int nr, cudaStream_t st) {
+cudaError_t batch_sweep_part(mmc_batch* b, int r0, int nr, cudaStream_t st, int slot) {
   mmc_handle* h = b->base;
   const long long ms = 3 * h->g.n, ss = 3 * h->g.nspec;
   T* m = (T*)b->m + r0 * ms;
@@ -1272,11 +1277,12 @@ cudaError_t batch_sweep_part(mmc_batch* b, int r0, int nr, cudaStream_t st) {
     e = launch_demag<T>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, m, hh,
                         (char*)b->spec + (size_t)r0 * ss * 2 * sizeof(T), h->khat, st, nr);
   if (e != cudaSuccess) return e;
-  return launch_mc<T>(h->g, (const McCoef<T>*)b->coef + r0, m, hh, b->ctr, -1, b->acc + r0, st, nr,
+  return launch_mc<T>(h->g, (const McCoef<T>*)b->coef + r0, m, hh, b->ctr + slot, -1, b->acc + r0, st, nr,
                       b->tun.mc_form);
 }
 
-cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
+// One sweep reading counter slot `slot` (the caller advances the counters).
+cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev, int slot) {
   mmc_handle* h = b->base;
   cudaError_t e;
   const int parts = std::min(b->streams, b->R);
@@ -1294,36 +1300,47 @@ cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev = nullptr) {
     for (int k = parts - 1; k >= 0; --k) {
       const int r0 = (int)((long long)b->R * k / parts), r1 = (int)((long long)b->R * (k + 1) / parts);
       cudaStream_t st = k == 0 ? h->st : b->sts[k - 1];
-      e = h->prec == 32 ? batch_sweep_part<float>(b, r0, r1 - r0, st) : batch_sweep_part<double>(b, r0, r1 - r0, st);
+      e = h->prec == 32 ? batch_sweep_part<float>(b, r0, r1 - r0, st, slot)
+                        : batch_sweep_part<double>(b, r0, r1 - r0, st, slot);
       if (e != cudaSuccess) return e;
     }
     for (int k = 1; k < parts; ++k) {
       if ((e = cudaEventRecord(b->joins[k - 1], b->sts[k - 1])) != cudaSuccess) return e;
       if ((e = cudaStreamWaitEvent(h->st, b->joins[k - 1], 0)) != cudaSuccess) return e;
     }
-    return launch_advance(b->ctr, 1, h->st);
+    return cudaSuccess;
   }
   if (h->cfg.cal_demag_flag && (e = batch_demag(b, ev)) != cudaSuccess) return e;
-  e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h, b->ctr,
-                                       -1, b->acc, h->st, b->R, b->tun.mc_form)
+  e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h,
+                                       b->ctr + slot, -1, b->acc, h->st, b->R, b->tun.mc_form)
                     : launch_mc<double>(h->g, (const McCoef<double>*)b->coef, (double*)b->m, (const double*)b->h,
-                                        b->ctr, -1, b->acc, h->st, b->R, b->tun.mc_form);
+                                        b->ctr + slot, -1, b->acc, h->st, b->R, b->tun.mc_form);
   if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[4], h->st)) != cudaSuccess) return e;
-  return launch_advance(b->ctr, 1, h->st);
+  return cudaSuccess;
 }
 
 // k sweeps; on the row kernel path they alternate between the two copies and
 // end in m and spec.
+// Sweep q reads counter slot q mod CTR_SLOTS; the counters advance after
+// every CTR_SLOTS sweeps and after the last one (one small launch per graph
+// of 32 sweeps instead of one per sweep).
 cudaError_t batch_sweeps(mmc_batch* b, long long k) {
   cudaError_t e = cudaSuccess;
-  if (b->rows_band > 0) {
-    for (long long q = 0; q < k && e == cudaSuccess; ++q) e = batch_sweep_rows(b, (int)(q & 1));
-    if (e == cudaSuccess && (k & 1)) e = batch_rows_settle(b);
-    return e;
+  for (long long q = 0; q < k && e == cudaSuccess; ++q) {
+    const int slot = (int)(q % CTR_SLOTS);
+    e = b->rows_band > 0 ? batch_sweep_rows(b, (int)(q & 1), nullptr, slot) : batch_sweep(b, nullptr, slot);
+    if (e == cudaSuccess && (slot == CTR_SLOTS - 1 || q == k - 1))
+      e = launch_advance(b->ctr, (uint32_t)(slot + 1), b->base->st, CTR_SLOTS);
   }
-  for (long long q = 0; q < k && e == cudaSuccess; ++q) e = batch_sweep(b);
+  if (e == cudaSuccess && b->rows_band > 0 && (k & 1)) e = batch_rows_settle(b);
   return e;
+}
+
+// Sets the counter slots to (stage, sweep0 + q).
+cudaError_t batch_set_counters(mmc_batch* b, long long stage, long long sweep0) {
+  for (int q = 0; q < CTR_SLOTS; ++q) b->ctr_host[q] = SweepCounters{(uint32_t)stage, (uint32_t)(sweep0 + q)};
+  return cudaMemcpyAsync(b->ctr, b->ctr_host, sizeof b->ctr_host, cudaMemcpyHostToDevice, b->base->st);
 }
 
 cudaError_t batch_energy_kernels(mmc_batch* b) {
@@ -1387,8 +1404,7 @@ int batch_run_begin(mmc_batch* b, BatchRun& r, long long stage, long long sweep0
   TRY(ensure_demag(h));
   TRY(batch_sync_temperatures(b));
   TRY(h->prec == 32 ? batch_upload_coefs<float>(b) : batch_upload_coefs<double>(b));
-  SweepCounters c0{(uint32_t)stage, (uint32_t)sweep0};
-  CU(cudaMemcpy(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice));
+  CU(batch_set_counters(b, stage, sweep0));
   CU(cudaEventRecord(h->ev[0], h->st));
   if (b->rows_band > 0) CU(batch_demag(b));  // the row kernel starts from the spectrum of m
   r = BatchRun{stage, sweep0, nsweeps, 0, 0};
@@ -1491,9 +1507,8 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     b->rows_band = cd.rows_band;
     b->tun = cd.tun;
     b->streams = cd.streams;
-    SweepCounters c0{0, 0};
     e = cudaMemcpyAsync(b->m, saved, mbytes, cudaMemcpyDeviceToDevice, h->st);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice, h->st);
+    if (e == cudaSuccess) e = batch_set_counters(b, 0, 0);
     if (e == cudaSuccess && b->rows_band > 0) e = batch_demag(b);
     // timed the way runs execute: replays of a captured graph of
     // BATCH_GRAPH_SWEEPS sweeps with this shape
@@ -1680,7 +1695,7 @@ int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out
   if ((st = alloc((void**)&b->partials, (size_t)R * h->npartials * NQ * sizeof(double))) != MMC_OK) return bail(st);
   if ((st = alloc((void**)&b->red, (size_t)R * NQ * sizeof(double))) != MMC_OK) return bail(st);
   if ((st = alloc((void**)&b->acc, R * sizeof(unsigned long long))) != MMC_OK) return bail(st);
-  if ((st = alloc((void**)&b->ctr, sizeof(SweepCounters))) != MMC_OK) return bail(st);
+  if ((st = alloc((void**)&b->ctr, CTR_SLOTS * sizeof(SweepCounters))) != MMC_OK) return bail(st);
   if (cudaMallocHost(&b->red_host, (size_t)R * NQ * sizeof(double)) != cudaSuccess)
     return bail(fail(MMC_ERR_OOM, "pinned allocation failed"));
   if (cudaMemset(b->acc, 0, R * sizeof(unsigned long long)) != cudaSuccess ||
@@ -2128,8 +2143,7 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
   TRY(ensure_demag(h));
   TRY(batch_sync_temperatures(b));
   TRY(h->prec == 32 ? batch_upload_coefs<float>(b) : batch_upload_coefs<double>(b));
-  SweepCounters c0{(uint32_t)stage, (uint32_t)sweep0};
-  CU(cudaMemcpy(b->ctr, &c0, sizeof c0, cudaMemcpyHostToDevice));
+  CU(batch_set_counters(b, stage, sweep0));
   cudaEvent_t ev[5];
   for (auto& e : ev) CU(cudaEventCreate(&e));
   double acc[4] = {0, 0, 0, 0};
@@ -2138,7 +2152,8 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
     // film sweeps: [0] row kernel, [1] column pass
     cudaError_t e = batch_demag(b);
     for (long long s = 0; s < nsweeps && e == cudaSuccess; ++s) {
-      e = batch_sweep_rows(b, (int)(s & 1), ev);
+      e = batch_sweep_rows(b, (int)(s & 1), ev, 0);
+      if (e == cudaSuccess) e = launch_advance(b->ctr, 1, h->st, CTR_SLOTS);
       if (e == cudaSuccess) e = cudaEventSynchronize(ev[2]);
       float x = 0, y = 0;
       if (e == cudaSuccess) e = cudaEventElapsedTime(&x, ev[0], ev[1]);
@@ -2150,7 +2165,8 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
     if (e != cudaSuccess) status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
   }
   for (long long s = 0; b->rows_band == 0 && s < nsweeps && status == MMC_OK; ++s) {
-    cudaError_t e = batch_sweep(b, ev);
+    cudaError_t e = batch_sweep(b, ev, 0);
+    if (e == cudaSuccess) e = launch_advance(b->ctr, 1, h->st, CTR_SLOTS);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
     for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
       float ms = 0;
