@@ -164,19 +164,48 @@ __device__ __noinline__ C<T>* fft_lines(C<T>* a, C<T>* b, int nlines, int stride
 }
 
 // ------------------------------------------------------------ warp-level FFT
-// 16th roots of unity exp(-2 pi i k / 16), k = 0..7 (cos, -sin).
-__device__ __forceinline__ double w16_re(int k) {
-  const double c[8] = {1.0, 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173,
-                       0.0, -0.38268343236508977173, -0.70710678118654752440, -0.92387953251128675613};
+// 32nd roots of unity exp(-2 pi i k / 32), k = 0..15 (cos, -sin): cos(pi k / 16)
+// and -sin(pi k / 16) to 20 digits.
+__device__ __forceinline__ double w32_re(int k) {
+  const double c[16] = {1.0,
+                        0.98078528040323044913,
+                        0.92387953251128675613,
+                        0.83146961230254523708,
+                        0.70710678118654752440,
+                        0.55557023301960222474,
+                        0.38268343236508977173,
+                        0.19509032201612826785,
+                        0.0,
+                        -0.19509032201612826785,
+                        -0.38268343236508977173,
+                        -0.55557023301960222474,
+                        -0.70710678118654752440,
+                        -0.83146961230254523708,
+                        -0.92387953251128675613,
+                        -0.98078528040323044913};
   return c[k];
 }
-__device__ __forceinline__ double w16_im(int k) {
-  const double s[8] = {0.0, -0.38268343236508977173, -0.70710678118654752440, -0.92387953251128675613,
-                       -1.0, -0.92387953251128675613, -0.70710678118654752440, -0.38268343236508977173};
+__device__ __forceinline__ double w32_im(int k) {
+  const double s[16] = {0.0,
+                        -0.19509032201612826785,
+                        -0.38268343236508977173,
+                        -0.55557023301960222474,
+                        -0.70710678118654752440,
+                        -0.83146961230254523708,
+                        -0.92387953251128675613,
+                        -0.98078528040323044913,
+                        -1.0,
+                        -0.98078528040323044913,
+                        -0.92387953251128675613,
+                        -0.83146961230254523708,
+                        -0.70710678118654752440,
+                        -0.55557023301960222474,
+                        -0.38268343236508977173,
+                        -0.19509032201612826785};
   return s[k];
 }
 
-// In-register DFT of N in {1, 2, 4, 8, 16} values, natural order in and out,
+// In-register DFT of N in {1, 2, 4, 8, 16, 32} values, natural order in and out,
 // by radix-2 decimation in time.  INV uses the conjugate roots.
 template <typename T, bool INV, int N>
 struct RegDft {
@@ -198,8 +227,8 @@ struct RegDft {
       } else if (4 * k == N) {  // multiply by -i (forward) or +i (inverse)
         t = INV ? cmk<V>(-o[k].y, o[k].x) : cmk<V>(o[k].y, -o[k].x);
       } else {
-        const T wr = (T)w16_re(k * (16 / N));
-        const T wi = INV ? (T)-w16_im(k * (16 / N)) : (T)w16_im(k * (16 / N));
+        const T wr = (T)w32_re(k * (32 / N));
+        const T wi = INV ? (T)-w32_im(k * (32 / N)) : (T)w32_im(k * (32 / N));
         t = cmk<V>(o[k].x * wr - o[k].y * wi, o[k].x * wi + o[k].y * wr);
       }
       v[k] = cadd(e[k], t);
@@ -298,8 +327,22 @@ __device__ __forceinline__ void fft_warp_call(C<T>* buf, int nlines, int stride,
 }
 
 // INL: expand the warp-level transforms into the calling kernel.
-template <typename T, bool INV, bool INL = false>
+// WIDE: also the 32-value shapes (lengths 512 and 1024).  They need about
+// twice the registers, and a kernel's register allocation covers everything
+// it calls, so only kernels instantiated with WIDE = true contain them; a
+// plan with warp_a == 32 must only reach those (the host checks).
+template <typename T, bool INV, bool INL = false, bool WIDE = false>
 __device__ C<T>* fft_run(C<T>* a, C<T>* b, int nlines, int stride, const FftPlan& p, const C<T>* tw) {
+  if constexpr (WIDE) {
+    if (p.warp_a == 32) {
+      if (p.warp_b == 32)
+        fft_warp_call<T, INV, 32, 32, INL>(a, nlines, stride, tw + p.full_off);
+      else
+        fft_warp_call<T, INV, 32, 16, INL>(a, nlines, stride, tw + p.full_off);
+      __syncthreads();
+      return a;
+    }
+  }
   if (p.warp_a == 16 && p.warp_b == 16) {
     fft_warp_call<T, INV, 16, 16, INL>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 16 && p.warp_b == 8) {

@@ -73,7 +73,7 @@ __global__ void k_x_forward(FftPlan p, int xdata, FastDiv dyd, int nrows, const 
     }
   }
   __syncthreads();
-  V* res = fft_run<T, false, INL>(bufA, bufB, nr * npairs, L, p, tw);
+  V* res = fft_run<T, false, INL, NC == 6>(bufA, bufB, nr * npairs, L, p, tw);
   for (int idx = threadIdx.x; idx < nr * npairs * hx; idx += blockDim.x) {
     const int rest = dhx.div(idx);
     const int k = idx - rest * hx;
@@ -164,10 +164,14 @@ __device__ __forceinline__ void load_roots(const FftPlan& p, C<T>* dst) {
   for (int i = threadIdx.x; i < p.n; i += blockDim.x) dst[i] = src[i];
 }
 
-// (Register budget: 64 per thread in FP32, so that eight 128-thread CTAs fit
-// on an SM; 128 in FP64.)
+// (Register budget: 64 per thread in FP32 with 16 values per lane, so that
+// eight 128-thread CTAs fit on an SM; twice that in FP64 or with 32 values.)
+template <typename T, int A>
+constexpr int x_w_min_blocks() {
+  return (sizeof(T) == 4 ? 4 : 2) / (A >= 32 ? 2 : 1);
+}
 template <typename T, int A, int B>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
+__global__ void __launch_bounds__(256, x_w_min_blocks<T, A>()) k_x_forward_w(FftPlan p, int xdata, FastDiv dyd, int nrows, const T* __restrict__ in,
                               long long in_cstride, C<T>* __restrict__ S, long long nspec, int nyp, int hx,
                               int pitch, int rows_per_cta, long long in_rstride, long long s_rstride) {
   constexpr int L = A * B, GPW = 32 / B;
@@ -220,7 +224,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_x_forward_w(Fft
 }
 
 template <typename T, int A, int B>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 4 : 2) k_x_inverse_w(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
+__global__ void __launch_bounds__(256, x_w_min_blocks<T, A>()) k_x_inverse_w(FftPlan p, const C<T>* __restrict__ S, long long nspec, int nyp, int hx, int pitch,
                               FastDiv dxo, FastDiv dyo, int nrows, T* __restrict__ out, long long out_cstride,
                               int rows_per_cta, long long s_rstride, long long out_rstride) {
   constexpr int L = A * B, GPW = 32 / B;
@@ -290,10 +294,11 @@ enum : int { PASS_FWD = 1, PASS_MUL = 2, PASS_INV = 4, PASS_SYM = 8 };
 // pos*pos_stride + kx0 + col].  Loads pos < load_lim (zero above), stores
 // pos < store_lim.  With PASS_MUL the tile is multiplied by the symmetric
 // tensor spectrum (K^ . M^ / N, calHexchangeKernel) between the transforms.
-template <typename T, bool INL>
-__global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long nspec, const C<T>* __restrict__ khat,
-                           int hx, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
-                           int flags, T inv_n, int tx, long long s_rstride, int lean) {
+template <typename T, bool INL, bool WIDE>
+__device__ __forceinline__ void col_pass_body(const FftPlan& p, int ncomp, C<T>* __restrict__ S, long long nspec,
+                                              const C<T>* __restrict__ khat, int hx, long long plane_stride,
+                                              long long pos_stride, int load_lim, int store_lim, int flags, T inv_n,
+                                              int tx, long long s_rstride, int lean) {
   using V = C<T>;
   S += blockIdx.z * s_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -363,7 +368,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
   V* cur = bufA;
   V* oth = bufB;
   if (flags & PASS_FWD) {
-    V* r = fft_run<T, false, INL>(cur, oth, nlines, stride, p, tw);
+    V* r = fft_run<T, false, INL, WIDE>(cur, oth, nlines, stride, p, tw);
     if (r != cur) {
       oth = cur;
       cur = r;
@@ -396,7 +401,7 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
     __syncthreads();
   }
   if (flags & PASS_INV) {
-    V* r = fft_run<T, true, INL>(cur, oth, nlines, stride, p, tw);
+    V* r = fft_run<T, true, INL, WIDE>(cur, oth, nlines, stride, p, tw);
     if (r != cur) {
       oth = cur;
       cur = r;
@@ -409,6 +414,24 @@ __global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long
       for (int pos = pos0; pos < store_lim; pos += pstep) dst[(long long)pos * pos_stride] = src[pos];
     }
   }
+}
+
+template <typename T, bool INL>
+__global__ void k_col_pass(FftPlan p, int ncomp, C<T>* __restrict__ S, long long nspec,
+                           const C<T>* __restrict__ khat, int hx, long long plane_stride, long long pos_stride,
+                           int load_lim, int store_lim, int flags, T inv_n, int tx, long long s_rstride, int lean) {
+  col_pass_body<T, INL, false>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim, store_lim, flags,
+                               inv_n, tx, s_rstride, lean);
+}
+// The same for the 32-value warp shapes (lengths 512 and 1024), at most 256
+// threads: their registers would not fit more.
+template <typename T, bool INL>
+__global__ void __launch_bounds__(256) k_col_pass_wide(FftPlan p, int ncomp, C<T>* __restrict__ S, long long nspec,
+                                                       const C<T>* __restrict__ khat, int hx, long long plane_stride,
+                                                       long long pos_stride, int load_lim, int store_lim, int flags,
+                                                       T inv_n, int tx, long long s_rstride, int lean) {
+  col_pass_body<T, INL, true>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim, store_lim, flags,
+                              inv_n, tx, s_rstride, lean);
 }
 
 // =========================================================== lattice helpers
@@ -1362,6 +1385,8 @@ template <typename T>
 XPassW<T> x_pass_w(const FftPlan& p) {
 #define MMC_XW(A_, B_) \
   if (p.warp_a == A_ && p.warp_b == B_) return {k_x_forward_w<T, A_, B_>, k_x_inverse_w<T, A_, B_>};
+  MMC_XW(32, 32)
+  MMC_XW(32, 16)
   MMC_XW(16, 16)
   MMC_XW(16, 8)
   MMC_XW(8, 8)
@@ -1382,11 +1407,12 @@ cudaError_t prepare_impl(int max_dyn_smem) {
   const void* fns[] = {(const void*)k_x_forward<T, false, 3>, (const void*)k_x_forward<T, true, 3>,
                        (const void*)k_x_forward<T, false, 6>, (const void*)k_x_forward<T, true, 6>,
                        (const void*)k_x_inverse<T, false>, (const void*)k_x_inverse<T, true>,
-                       (const void*)k_col_pass<T, false>,  (const void*)k_col_pass<T, true>};
+                       (const void*)k_col_pass<T, false>,      (const void*)k_col_pass<T, true>,
+                       (const void*)k_col_pass_wide<T, false>, (const void*)k_col_pass_wide<T, true>};
   for (const void* f : fns) MMC_TRY_ATTR(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, max_dyn_smem));
-  for (int s = 0; s < 5; ++s) {
+  for (int s = 0; s < 7; ++s) {
     FftPlan p{};
-    const int ab[5][2] = {{16, 16}, {16, 8}, {8, 8}, {16, 2}, {8, 4}};
+    const int ab[7][2] = {{32, 32}, {32, 16}, {16, 16}, {16, 8}, {8, 8}, {16, 2}, {8, 4}};
     p.warp_a = ab[s][0];
     p.warp_b = ab[s][1];
     const XPassW<T> w = x_pass_w<T>(p);
@@ -1417,6 +1443,7 @@ cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int
       return cudaGetLastError();
     }
   }
+  if (ncomp == 3 && p.warp_a == 32) return cudaErrorInvalidValue;  // handled by k_x_forward_w above
   const int lines = (ncomp + 1) / 2;
   size_t sm = x_pass_smem(p, lines, rpc, sizeof(C<T>));
   dim3 grid((nrows + rpc - 1) / rpc, 1, nrep);
@@ -1438,7 +1465,15 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
   size_t sm = lean ? col_pass_smem_lean(p, ncomp, tx, sizeof(C<T>))
                    : col_pass_smem(p, ncomp, tx, sizeof(C<T>), (flags & PASS_MUL) != 0);
   dim3 grid((hx + tx - 1) / tx, planes, nrep);
-  auto kern = inl ? k_col_pass<T, true> : k_col_pass<T, false>;
+  auto kern = p.warp_a == 32 ? (inl ? k_col_pass_wide<T, true> : k_col_pass_wide<T, false>)
+                             : (inl ? k_col_pass<T, true> : k_col_pass<T, false>);
+  // no more threads than the kernel's registers allow (the split of the work
+  // does not change the results)
+  cudaFuncAttributes fa;
+  MMC_TRY_ATTR(cudaFuncGetAttributes(&fa, (const void*)kern));
+  threads = std::min(threads, fa.maxThreadsPerBlock & ~31);
+  threads -= threads % std::max(tx, 32);
+  if (threads < 32) return cudaErrorInvalidValue;
   kern<<<grid, threads, sm, st>>>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
                                            store_lim, flags, inv_n, tx, s_rstride, lean ? 1 : 0);
   return cudaGetLastError();
@@ -1486,6 +1521,7 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
     w.inv<<<grid, tun.x_threads, x_pass_w_smem(px, rpc, sizeof(C<T>)), st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx,
                                                                            g.dny, rows, h, g.n, rpc, sr, mr);
   } else {
+    if (px.warp_a == 32) return cudaErrorInvalidValue;  // the wide shapes have warp-shaped x passes
     size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
     auto kinv = tun.fft_inline ? k_x_inverse<T, true> : k_x_inverse<T, false>;
     kinv<<<grid, tun.x_threads, sm, st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx, g.dny, rows, h, g.n, rpc, sr, mr);

@@ -102,11 +102,11 @@ int make_plan(int n, PlanHost* ph) {
     ns *= R;
   }
   p.nstages = (int)rad.size();
-  // warp-level transform for power-of-two lengths up to 256: n = A * B
+  // warp-level transform for power-of-two lengths 32 .. 1024: n = A * B
   p.warp_a = p.warp_b = 0;
   p.full_off = 0;
   p.dn = FastDiv((uint32_t)n);
-  const int wa[4][3] = {{256, 16, 16}, {128, 16, 8}, {64, 8, 8}, {32, 8, 4}};
+  const int wa[6][3] = {{1024, 32, 32}, {512, 32, 16}, {256, 16, 16}, {128, 16, 8}, {64, 8, 8}, {32, 8, 4}};
   for (const auto& w : wa)
     if (n == w[0]) {
       p.warp_a = w[1];
@@ -175,24 +175,34 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   while (r > 1 && ((rows + r - 1) / r) * nrep < want) r /= 2;
   while (r > 1 && xsm(r) > 96 * 1024) r /= 2;
   t.x_rows_per_cta = r;
-  auto csm = [&](const FftPlan& p, int tx) {
-    return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * col_line_stride(p.n, csize) + 6 * (size_t)p.n * tx) * csize;
+  // in-place column passes reading K^ from global memory for the long
+  // warp-shaped lines, where the copies of the tile and of K^ would leave room
+  // for one column per CTA (the autotuner tries both forms)
+  t.col_lean = py.warp_a != 0 && py.n >= 512 ? 1 : 0;
+  // shared memory of a column pass: the in-place form holds the tile once,
+  // the other twice plus the K^ tile when the pass multiplies
+  auto csm = [&](const FftPlan& p, int tx, bool mul) {
+    const size_t tw = (size_t)((p.tw_total + 1) & ~1), lines = (size_t)3 * tx * col_line_stride(p.n, csize);
+    if (t.col_lean && p.warp_a) return (tw + lines) * csize;
+    return (tw + 2 * lines + (mul ? 6 * (size_t)p.n * tx : 0)) * csize;
   };
-  auto pick = [&](const FftPlan& p, int planes) {
+  auto pick = [&](const FftPlan& p, int planes, bool mul) {
+    // short lines (a few padded z layers) take wider tiles, up to 64 columns
     int tx = 8;
-    while (tx > 1 && (((long long)(g.hx + tx - 1) / tx) * planes * nrep < want || csm(p, tx) > 96 * 1024)) tx /= 2;
-    while (tx > 1 && csm(p, tx) > smem_limit()) tx /= 2;
+    while (tx < 64 && tx * p.n < 1024) tx *= 2;
+    while (tx > 1 && (((long long)(g.hx + tx - 1) / tx) * planes * nrep < want || csm(p, tx, mul) > 96 * 1024))
+      tx /= 2;
+    while (tx > 1 && csm(p, tx, mul) > smem_limit()) tx /= 2;
     return tx;
   };
-  t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz);
-  t.col_tx_z = pick(pz, g.nyp);
+  t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz, g.nzp == 1);
+  t.col_tx_z = pick(pz, g.nyp, true);
   t.col_threads = col_threads_for(g, py, pz, t.col_tx, t.col_tx_z);
   // FP32 film batches: the vectorised per-colour sweep, measured faster from
   // about 8 replicas; single lattices and FP64 keep the scalar form (the
   // autotuner tries every form)
   t.mc_form = csize == 8 && nrep >= 8 && mc_quad_eligible(g) ? MC_FORM_QUAD : MC_FORM_SCALAR;
   t.fft_inline = 0;
-  t.col_lean = 0;
   return t;
 }
 
@@ -469,15 +479,16 @@ int setup_engine(mmc_handle* h, int nsm) {
   const Geom& g = h->g;
   // films with demag and two colours whose m rows are whole 16-byte chunks
   const bool eligible = c.cal_demag_flag && g.nz == 1 && g.nzp == 1 && g.ncolors == 2 &&
-                        ((size_t)g.nx * h->tsize) % 16 == 0 && g.ny >= 1;
+                        ((size_t)g.nx * h->tsize) % 16 == 0 && g.ny >= 1 && h->px.p.warp_a != 32 &&
+                        h->py.p.warp_a != 32;
   if (c.sweep_engine == MMC_ENGINE_KERNELS || (c.sweep_engine == MMC_ENGINE_AUTO && !eligible)) {
     h->engine = MMC_ENGINE_KERNELS;
     return MMC_OK;
   }
   if (!eligible)
     return fail(MMC_ERR_UNSUPPORTED,
-                "the fused engine needs a film (nz = 1), demag on, an even or open lattice and nx * sizeof(real) "
-                "a multiple of 16 bytes");
+                "the fused engine needs a film (nz = 1), demag on, an even or open lattice, nx * sizeof(real) "
+                "a multiple of 16 bytes and padded sides other than 512 and 1024");
   int optin = 48 * 1024;
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
   std::vector<int> bands;
@@ -1557,15 +1568,20 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     Cand c = best;
     c.tun.fft_inline = 1 - c.tun.fft_inline;
     trial(c);
-    // in-place column passes with the full and half thread count
+    // the other column-pass form (in place or with copies) with the full and
+    // half thread count, and the half thread count of the current form
     if (h->py.p.warp_a) {
-      for (int half = 0; half < 2; ++half) {
-        Cand d = best;
-        d.tun.col_lean = 1;
-        if (half) d.tun.col_threads = std::max(64, best.tun.col_threads / 2);
-        if (half && d.tun.col_threads == best.tun.col_threads) continue;
-        trial(d);
-      }
+      const Cand cur = best;
+      for (int flip = 0; flip < 2; ++flip)
+        for (int half = 0; half < 2; ++half) {
+          if (!flip && !half) continue;
+          Cand d = cur;
+          if (flip) d.tun.col_lean = 1 - cur.tun.col_lean;
+          if (half) d.tun.col_threads = std::max(64, cur.tun.col_threads / 2);
+          if (half && d.tun.col_threads == cur.tun.col_threads) continue;
+          if (!d.tun.col_lean && col_pass_smem(h->py.p, d.tun.col_tx, cs) > smem_limit()) continue;
+          trial(d);
+        }
     }
   }
   {
@@ -1640,7 +1656,8 @@ int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out
   {
     const Geom& gg = h->g;
     const bool film = h->cfg.cal_demag_flag && gg.nz == 1 && gg.nzp == 1 && gg.ncolors == 2 &&
-                      ((size_t)gg.nx * h->tsize) % 16 == 0 && ((size_t)gg.hxp * 2 * h->tsize) % 16 == 0;
+                      ((size_t)gg.nx * h->tsize) % 16 == 0 && ((size_t)gg.hxp * 2 * h->tsize) % 16 == 0 &&
+                      h->px.p.warp_a != 32 && h->py.p.warp_a != 32;
     int optin = 48 * 1024;
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, h->device);
     if (film) {
@@ -1661,7 +1678,8 @@ int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out
       if (b->row_bands.empty()) {
         batch_free(b);
         return fail(MMC_ERR_UNSUPPORTED,
-                    "the row-kernel batch path needs films (nz = 1) with demag, two colours and 16-byte rows");
+                    "the row-kernel batch path needs films (nz = 1) with demag, two colours, 16-byte rows and "
+                    "padded sides other than 512 and 1024");
       }
       b->rows_band = b->row_bands[0];
     }
@@ -2195,8 +2213,9 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
   const int band = shape[5];
   auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
   if (!pow2(t.x_rows_per_cta) || t.x_rows_per_cta > 16 || x_pass_smem(h->px.p, t.x_rows_per_cta, cs) > smem_limit() ||
-      !pow2(t.col_tx) || t.col_tx > 8 || col_pass_smem(h->py.p, t.col_tx, cs) > smem_limit() || !pow2(t.col_tx_z) ||
-      t.col_tx_z > 8 || col_pass_smem(h->pz.p, t.col_tx_z, cs) > smem_limit() ||
+      !pow2(t.col_tx) || t.col_tx > 64 || col_pass_smem(h->py.p, t.col_tx, cs) > smem_limit() || !pow2(t.col_tx_z) ||
+      t.col_tx_z > 64 || col_pass_smem(h->pz.p, t.col_tx_z, cs) > smem_limit() || t.col_threads % t.col_tx != 0 ||
+      t.col_threads % t.col_tx_z != 0 ||
       (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
       t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_BAND ||
       (t.mc_form == MC_FORM_TILE && !mc_tile_eligible(g)) || (t.mc_form == MC_FORM_QUAD && !mc_quad_eligible(g)) ||
