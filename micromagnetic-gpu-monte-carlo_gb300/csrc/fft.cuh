@@ -81,12 +81,13 @@ __device__ __noinline__ C<T>* fft_lines(C<T>* a, C<T>* b, int nlines, int stride
   const int n = p.n;
   for (int s = 0; s < p.nstages; ++s) {
     const int R = p.radix[s], Ns = p.ns[s], nb = n / R;
+    const FastDiv dnb = p.dnb[s], dns = p.dns[s];
     const V* W = tw + p.tw_off[s];
     const int total = nlines * nb;
     for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-      const int line = idx / nb;
+      const int line = dnb.div(idx);
       const int j = idx - line * nb;
-      const int k = j % Ns;
+      const int k = j - dns.div(j) * Ns;
       const V* in = src + (long long)line * stride + j;
       V* out = dst + (long long)line * stride + (j - k) * R + k;
       if (R == 4) {
@@ -134,6 +135,39 @@ __device__ __noinline__ C<T>* fft_lines(C<T>* a, C<T>* b, int nlines, int stride
         out[0] = cadd(v0, t1);
         out[Ns] = cadd(t2, r);
         out[2 * Ns] = csub(t2, r);
+      } else if (R == 5) {
+        V v0 = in[0], v1 = in[nb], v2 = in[2 * nb], v3 = in[3 * nb], v4 = in[4 * nb];
+        if (k) {
+          const V w1 = W[k], w2 = W[Ns + k], w3 = W[2 * Ns + k], w4 = W[3 * Ns + k];
+          if (INV) {
+            v1 = cmulc(v1, w1);
+            v2 = cmulc(v2, w2);
+            v3 = cmulc(v3, w3);
+            v4 = cmulc(v4, w4);
+          } else {
+            v1 = cmul(v1, w1);
+            v2 = cmul(v2, w2);
+            v3 = cmul(v3, w3);
+            v4 = cmul(v4, w4);
+          }
+        }
+        // 5-point DFT from the symmetric and antisymmetric pairs:
+        // cos(2 pi / 5), cos(4 pi / 5), sin(2 pi / 5), sin(4 pi / 5)
+        const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+        const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;
+        const V t1 = cadd(v1, v4), t2 = cadd(v2, v3), t3 = csub(v1, v4), t4 = csub(v2, v3);
+        const V a1 = cmk<V>(v0.x + c1 * t1.x + c2 * t2.x, v0.y + c1 * t1.y + c2 * t2.y);
+        const V a2 = cmk<V>(v0.x + c2 * t1.x + c1 * t2.x, v0.y + c2 * t1.y + c1 * t2.y);
+        const V b1 = cmk<V>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+        const V b2 = cmk<V>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+        // forward: X1 = a1 - i b1, X4 = a1 + i b1, X2 = a2 - i b2, X3 = a2 + i b2
+        const V mb1 = INV ? cmk<V>(-b1.y, b1.x) : cmk<V>(b1.y, -b1.x);  // -+ i b1
+        const V mb2 = INV ? cmk<V>(-b2.y, b2.x) : cmk<V>(b2.y, -b2.x);
+        out[0] = cadd(v0, cadd(t1, t2));
+        out[Ns] = cadd(a1, mb1);
+        out[2 * Ns] = cadd(a2, mb2);
+        out[3 * Ns] = csub(a2, mb2);
+        out[4 * Ns] = csub(a1, mb1);
       } else {
         // generic odd radix: direct R-point DFT with the stage's roots of unity
         const V* RT = tw + p.root_off[s];

@@ -52,6 +52,8 @@ struct FftPlan {
   int warp_a, warp_b;
   int full_off;
   FastDiv dn;  // n
+  FastDiv dnb[FFT_MAX_STAGES];  // n / radix[s]
+  FastDiv dns[FFT_MAX_STAGES];  // ns[s]
   const double2* tw64;
   const float2* tw32;
 };

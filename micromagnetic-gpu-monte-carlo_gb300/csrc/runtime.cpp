@@ -83,6 +83,8 @@ int make_plan(int n, PlanHost* ph) {
     int R = rad[s];
     p.radix[s] = R;
     p.ns[s] = ns;
+    p.dnb[s] = FastDiv((uint32_t)(n / R));
+    p.dns[s] = FastDiv((uint32_t)ns);
     p.tw_off[s] = (int)(tw.size() / 2);
     for (int t = 1; t < R; ++t)
       for (int k = 0; k < ns; ++k) {
