@@ -278,11 +278,15 @@ struct RegDft<T, INV, 1> {
 // One line of length N = A * B owned by B lanes of one warp (lane b of the
 // group), with the input already in registers: v[a] = x[b + B a].
 //   x[b + B a] --(A-point DFT over a)--> Y[b][ka] --(* W_N^(b ka))-->
-//   transpose in the line (swizzled) --(B-point DFT over b)--> X[ka + A kb].
+//   transpose in the line --(B-point DFT over b)--> X[ka + A kb].
 // Lp is the line in shared memory, used for the transpose; it holds X in
 // natural order on return.  All lanes of the warp must call it (inactive
 // groups with active = false); `roots` holds exp(-2 pi i j / N), j < N.
-template <typename T, bool INV, int A, int B>
+// The transpose goes through rows of B + 1 elements when PAD (row ka at
+// ka (B + 1): every address is the lane's base plus a compile-time offset,
+// and the line then needs N + A - 1 elements of room), else through rows of
+// B with the columns rotated by ka (N elements of room).
+template <typename T, bool INV, int A, int B, bool PAD = false>
 __device__ __forceinline__ void fft_line_regs(C<T> (&v)[A], C<T>* Lp, int b, bool active, const C<T>* roots) {
   using V = C<T>;
   constexpr int Q = A / B;
@@ -294,17 +298,31 @@ __device__ __forceinline__ void fft_line_regs(C<T> (&v)[A], C<T>* Lp, int b, boo
   }
   __syncwarp();
   if (active) {
+    if constexpr (PAD) {
+      C<T>* row = Lp + b;
 #pragma unroll
-    for (int ka = 0; ka < A; ++ka) Lp[ka * B + ((b + ka) & (B - 1))] = v[ka];
+      for (int ka = 0; ka < A; ++ka) row[ka * (B + 1)] = v[ka];
+    } else {
+#pragma unroll
+      for (int ka = 0; ka < A; ++ka) Lp[ka * B + ((b + ka) & (B - 1))] = v[ka];
+    }
   }
   __syncwarp();
   // v is dead after the transpose: reuse it for the columns
   if (active) {
+    if constexpr (PAD) {
+      const C<T>* col = Lp + b * Q * (B + 1);
 #pragma unroll
-    for (int t = 0; t < Q; ++t) {
-      const int ka = b * Q + t;
+      for (int t = 0; t < Q; ++t)
 #pragma unroll
-      for (int bb = 0; bb < B; ++bb) v[t * B + bb] = Lp[ka * B + ((bb + ka) & (B - 1))];
+        for (int bb = 0; bb < B; ++bb) v[t * B + bb] = col[t * (B + 1) + bb];
+    } else {
+#pragma unroll
+      for (int t = 0; t < Q; ++t) {
+        const int ka = b * Q + t;
+#pragma unroll
+        for (int bb = 0; bb < B; ++bb) v[t * B + bb] = Lp[ka * B + ((bb + ka) & (B - 1))];
+      }
     }
   }
 #pragma unroll
@@ -320,9 +338,9 @@ __device__ __forceinline__ void fft_line_regs(C<T> (&v)[A], C<T>* Lp, int b, boo
 }
 
 // Transforms `nlines` lines of length N = A * B in place (line l at
-// buf + l * stride), 32 / B lines per warp at a time; only __syncwarp is
-// needed inside.
-template <typename T, bool INV, int A, int B>
+// buf + l * stride, stride >= N + A - 1 when PAD), 32 / B lines per warp at
+// a time; only __syncwarp is needed inside.
+template <typename T, bool INV, int A, int B, bool PAD = false>
 __device__ __forceinline__ void fft_lines_warp_body(C<T>* buf, int nlines, int stride, const C<T>* roots) {
   using V = C<T>;
   constexpr int GPW = 32 / B;  // lines per warp
@@ -337,27 +355,27 @@ __device__ __forceinline__ void fft_lines_warp_body(C<T>* buf, int nlines, int s
 #pragma unroll
       for (int a = 0; a < A; ++a) v[a] = Lp[b + B * a];
     }
-    fft_line_regs<T, INV, A, B>(v, Lp, b, active, roots);
+    fft_line_regs<T, INV, A, B, PAD>(v, Lp, b, active, roots);
   }
 }
 
 // Out-of-line copy (kernels that hold much state around the transform call it
 // so that the transform's registers are not added to theirs).
-template <typename T, bool INV, int A, int B>
+template <typename T, bool INV, int A, int B, bool PAD = false>
 __device__ __noinline__ void fft_lines_warp(C<T>* buf, int nlines, int stride, const C<T>* roots) {
-  fft_lines_warp_body<T, INV, A, B>(buf, nlines, stride, roots);
+  fft_lines_warp_body<T, INV, A, B, PAD>(buf, nlines, stride, roots);
 }
 
 // Transform dispatcher: the warp-level path for the lengths the plan marks,
 // the Stockham stages otherwise.  Returns the buffer holding the result; all
 // threads of the block must call it after the input is complete
 // (__syncthreads()), and the result is complete for all threads on return.
-template <typename T, bool INV, int A, int B, bool INL>
+template <typename T, bool INV, int A, int B, bool INL, bool PAD = false>
 __device__ __forceinline__ void fft_warp_call(C<T>* buf, int nlines, int stride, const C<T>* roots) {
   if constexpr (INL)
-    fft_lines_warp_body<T, INV, A, B>(buf, nlines, stride, roots);
+    fft_lines_warp_body<T, INV, A, B, PAD>(buf, nlines, stride, roots);
   else
-    fft_lines_warp<T, INV, A, B>(buf, nlines, stride, roots);
+    fft_lines_warp<T, INV, A, B, PAD>(buf, nlines, stride, roots);
 }
 
 // INL: expand the warp-level transforms into the calling kernel.
@@ -365,28 +383,30 @@ __device__ __forceinline__ void fft_warp_call(C<T>* buf, int nlines, int stride,
 // twice the registers, and a kernel's register allocation covers everything
 // it calls, so only kernels instantiated with WIDE = true contain them; a
 // plan with warp_a == 32 must only reach those (the host checks).
-template <typename T, bool INV, bool INL = false, bool WIDE = false>
+// PAD: the warp-level transforms use padded transpose rows (stride >=
+// n + warp_a - 1).
+template <typename T, bool INV, bool INL = false, bool WIDE = false, bool PAD = false>
 __device__ C<T>* fft_run(C<T>* a, C<T>* b, int nlines, int stride, const FftPlan& p, const C<T>* tw) {
   if constexpr (WIDE) {
     if (p.warp_a == 32) {
       if (p.warp_b == 32)
-        fft_warp_call<T, INV, 32, 32, INL>(a, nlines, stride, tw + p.full_off);
+        fft_warp_call<T, INV, 32, 32, INL, PAD>(a, nlines, stride, tw + p.full_off);
       else
-        fft_warp_call<T, INV, 32, 16, INL>(a, nlines, stride, tw + p.full_off);
+        fft_warp_call<T, INV, 32, 16, INL, PAD>(a, nlines, stride, tw + p.full_off);
       __syncthreads();
       return a;
     }
   }
   if (p.warp_a == 16 && p.warp_b == 16) {
-    fft_warp_call<T, INV, 16, 16, INL>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 16, 16, INL, PAD>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 16 && p.warp_b == 8) {
-    fft_warp_call<T, INV, 16, 8, INL>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 16, 8, INL, PAD>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 8 && p.warp_b == 8) {
-    fft_warp_call<T, INV, 8, 8, INL>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 8, 8, INL, PAD>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 16 && p.warp_b == 2) {
-    fft_warp_call<T, INV, 16, 2, INL>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 16, 2, INL, PAD>(a, nlines, stride, tw + p.full_off);
   } else if (p.warp_a == 8 && p.warp_b == 4) {
-    fft_warp_call<T, INV, 8, 4, INL>(a, nlines, stride, tw + p.full_off);
+    fft_warp_call<T, INV, 8, 4, INL, PAD>(a, nlines, stride, tw + p.full_off);
   } else {
     return fft_lines<T, INV>(a, b, nlines, stride, p, tw);
   }

@@ -180,6 +180,7 @@ __global__ void __launch_bounds__(256, x_w_min_blocks<T, A>()) k_x_forward_w(Fft
   in += blockIdx.z * in_rstride;
   S += blockIdx.z * s_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int LS = L + A;  // line stride: room for the padded transpose
   V* roots = reinterpret_cast<V*>(smem_raw);
   V* buf = roots + L;  // line pr * nr + rr: row rr, pair pr (mx + i my, mz + 0 i)
   load_roots<T>(p, roots);
@@ -204,13 +205,13 @@ __global__ void __launch_bounds__(256, x_w_min_blocks<T, A>()) k_x_forward_w(Fft
         v[a] = cmk<V>(ok ? re[x] : (T)0, (ok && pr == 0) ? re[in_cstride + x] : (T)0);
       }
     }
-    fft_line_regs<T, false, A, B>(v, buf + (active ? line : 0) * L, b, active, roots);
+    fft_line_regs<T, false, A, B, true>(v, buf + (active ? line : 0) * LS, b, active, roots);
   }
   __syncthreads();
   // split each pair into the half spectra of its two real rows
   for (int line = warp; line < nlines; line += nwarps) {
     const int pr = line >= nr ? 1 : 0, rr = line - pr * nr;
-    const V* ln = buf + line * L;
+    const V* ln = buf + line * LS;
     const int row = row0 + rr;
     const int z = dyd.div(row), y = row - z * ydata;
     V* so = S + (long long)(2 * pr) * nspec + ((long long)z * nyp + y) * pitch;
@@ -233,6 +234,7 @@ __global__ void __launch_bounds__(256, x_w_min_blocks<T, A>()) k_x_inverse_w(Fft
   S += blockIdx.z * s_rstride;
   out += blockIdx.z * out_rstride;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int LS = L + A;  // line stride: room for the padded transpose
   V* roots = reinterpret_cast<V*>(smem_raw);
   V* buf = roots + L;  // line rr: hx + i hy of row rr; line nr + rr: hz
   load_roots<T>(p, roots);
@@ -268,12 +270,12 @@ __global__ void __launch_bounds__(256, x_w_min_blocks<T, A>()) k_x_inverse_w(Fft
         }
       }
     }
-    fft_line_regs<T, true, A, B>(v, buf + (active ? line : 0) * L, b, active, roots);
+    fft_line_regs<T, true, A, B, true>(v, buf + (active ? line : 0) * LS, b, active, roots);
   }
   __syncthreads();
   for (int rr = warp; rr < nr; rr += nwarps) {
-    const V* l0 = buf + rr * L;
-    const V* l1 = buf + (nr + rr) * L;
+    const V* l0 = buf + rr * LS;
+    const V* l1 = buf + (nr + rr) * LS;
     T* o = out + (long long)(row0 + rr) * xout;
     for (int x = lane; x < xout; x += 32) {
       const V a = l0[x];
@@ -304,7 +306,7 @@ __device__ __forceinline__ void col_pass_body(const FftPlan& p, int ncomp, C<T>*
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V* tw = reinterpret_cast<V*>(smem_raw);
   const int L = p.n;
-  const int stride = col_line_stride(L, sizeof(V));
+  const int stride = col_line_stride(p, sizeof(V));
   const int kx0 = blockIdx.x * tx;
   const int ntx = min(tx, hx - kx0);
   const long long pbase = (long long)blockIdx.y * plane_stride + kx0;
@@ -368,7 +370,7 @@ __device__ __forceinline__ void col_pass_body(const FftPlan& p, int ncomp, C<T>*
   V* cur = bufA;
   V* oth = bufB;
   if (flags & PASS_FWD) {
-    V* r = fft_run<T, false, INL, WIDE>(cur, oth, nlines, stride, p, tw);
+    V* r = fft_run<T, false, INL, WIDE, true>(cur, oth, nlines, stride, p, tw);
     if (r != cur) {
       oth = cur;
       cur = r;
@@ -401,7 +403,7 @@ __device__ __forceinline__ void col_pass_body(const FftPlan& p, int ncomp, C<T>*
     __syncthreads();
   }
   if (flags & PASS_INV) {
-    V* r = fft_run<T, true, INL, WIDE>(cur, oth, nlines, stride, p, tw);
+    V* r = fft_run<T, true, INL, WIDE, true>(cur, oth, nlines, stride, p, tw);
     if (r != cur) {
       oth = cur;
       cur = r;
@@ -1365,10 +1367,10 @@ inline size_t x_pass_smem(const FftPlan& p, int lines_per_row, int rows, size_t 
   return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)rows * lines_per_row * p.n) * csize;
 }
 inline size_t col_pass_smem_lean(const FftPlan& p, int ncomp, int tx, size_t csize) {
-  return ((size_t)((p.tw_total + 1) & ~1) + (size_t)ncomp * tx * col_line_stride(p.n, csize)) * csize;
+  return ((size_t)((p.tw_total + 1) & ~1) + (size_t)ncomp * tx * col_line_stride(p, csize)) * csize;
 }
 inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize, bool mul) {
-  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)ncomp * tx * col_line_stride(p.n, csize) +
+  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)ncomp * tx * col_line_stride(p, csize) +
           (mul ? 6 * (size_t)p.n * tx : 0)) *
          csize;
 }
@@ -1396,7 +1398,7 @@ XPassW<T> x_pass_w(const FftPlan& p) {
   return {nullptr, nullptr};
 }
 inline size_t x_pass_w_smem(const FftPlan& p, int rows, size_t csize) {
-  return ((size_t)p.n + 2 * (size_t)rows * p.n) * csize;
+  return ((size_t)p.n + 2 * (size_t)rows * (p.n + p.warp_a)) * csize;
 }
 
 // Raises the dynamic shared-memory limit of the FFT pass kernels to the

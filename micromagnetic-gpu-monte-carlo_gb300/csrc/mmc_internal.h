@@ -114,12 +114,15 @@ struct HCoef {
 // E_ex, E_dmi, E_an, E_zeeman, E_demag, sum mx, sum my, sum mz, sum solid angle.
 constexpr int NQ = 9;
 
-// Shared-memory line stride (elements) of the column passes for transform
-// length n and complex size csize: a padding that spreads both the
-// transforms' lines and the tile's 8 columns over the banks (n + 2 for 8-byte
-// FP32 complex values, whose 16-lane wavefronts then touch distinct banks;
-// n + 1 for 16-byte FP64 ones).
-MMC_HD inline int col_line_stride(int n, size_t csize) { return n + (csize == 8 ? 2 : 1); }
+// Shared-memory line stride (elements) of the column passes for a transform
+// plan and complex size csize: room for the padded transpose rows of the
+// warp-level transforms (n + warp_a - 1 elements), plus a padding that spreads
+// the tile's 8 columns over the banks (+2 for 8-byte FP32 complex values,
+// whose 16-lane wavefronts then touch distinct banks; +1 for 16-byte FP64
+// ones).
+MMC_HD inline int col_line_stride(const FftPlan& p, size_t csize) {
+  return p.n + p.warp_a + (csize == 8 ? 2 : 1);
+}
 
 // Launch shapes chosen by the host (autotuned).
 struct DemagTuning {

@@ -142,7 +142,7 @@ void free_plan(PlanHost* ph) {
   ph->d32 = nullptr;
 }
 
-size_t smem_limit() { return 200 * 1024; }
+size_t smem_limit() { return 220 * 1024; }  // below the 227 KB opt-in limit of a CTA
 
 // Launch shapes for `nrep` replicas.  The warp-level FFT gives each warp
 // 32 / B lines, so a CTA takes enough rows / columns to keep all its warps
@@ -184,7 +184,7 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   // shared memory of a column pass: the in-place form holds the tile once,
   // the other twice plus the K^ tile when the pass multiplies
   auto csm = [&](const FftPlan& p, int tx, bool mul) {
-    const size_t tw = (size_t)((p.tw_total + 1) & ~1), lines = (size_t)3 * tx * col_line_stride(p.n, csize);
+    const size_t tw = (size_t)((p.tw_total + 1) & ~1), lines = (size_t)3 * tx * col_line_stride(p, csize);
     if (t.col_lean && p.warp_a) return (tw + lines) * csize;
     return (tw + 2 * lines + (mul ? 6 * (size_t)p.n * tx : 0)) * csize;
   };
@@ -213,8 +213,12 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
 size_t x_pass_smem(const FftPlan& px, int r, size_t csize) {
   return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize;
 }
-size_t col_pass_smem(const FftPlan& p, int tx, size_t csize) {
-  return ((size_t)((p.tw_total + 1) & ~1) + 2 * (size_t)3 * tx * col_line_stride(p.n, csize) + 6 * (size_t)p.n * tx) * csize;
+// (lean: the in-place form, which exists for warp-shaped lengths only and
+// holds the tile once without a K^ tile)
+size_t col_pass_smem(const FftPlan& p, int tx, size_t csize, bool lean = false) {
+  const size_t tw = (size_t)((p.tw_total + 1) & ~1), lines = (size_t)3 * tx * col_line_stride(p, csize);
+  if (lean && p.warp_a) return (tw + lines) * csize;
+  return (tw + 2 * lines + 6 * (size_t)p.n * tx) * csize;
 }
 
 }  // namespace
@@ -707,10 +711,10 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
     }
     DemagTuning tt = h->tun;
     // six-component setup transform: narrower tiles keep shared memory in budget
-    while (tt.col_tx > 1 && ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx * col_line_stride(h->py.p.n, sizeof(double2))) *
+    while (tt.col_tx > 1 && ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx * col_line_stride(h->py.p, sizeof(double2))) *
                                     sizeof(double2) > smem_limit())
       tt.col_tx /= 2;
-    while (tt.col_tx_z > 1 && ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx_z * col_line_stride(h->pz.p.n, sizeof(double2))) *
+    while (tt.col_tx_z > 1 && ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)tt.col_tx_z * col_line_stride(h->pz.p, sizeof(double2))) *
                                       sizeof(double2) > smem_limit())
       tt.col_tx_z /= 2;
     tt.col_tx = std::min(tt.col_tx, tt.col_tx_z);
@@ -964,8 +968,8 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   h->nsm = nsm;
   // shared-memory feasibility of the per-sweep passes
   if (((size_t)((h->px.p.tw_total + 1) & ~1) + 2 * 2 * (size_t)h->px.p.n) * csize > smem_limit() ||
-      ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)col_line_stride(h->py.p.n, csize)) * csize > smem_limit() ||
-      ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)col_line_stride(h->pz.p.n, csize)) * csize > smem_limit() ||
+      ((size_t)((h->py.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)col_line_stride(h->py.p, csize)) * csize > smem_limit() ||
+      ((size_t)((h->pz.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)col_line_stride(h->pz.p, csize)) * csize > smem_limit() ||
       ((size_t)((h->px.p.tw_total + 1) & ~1) + 2 * 3 * (size_t)h->px.p.n) * 16 > smem_limit())
     return bail(fail(MMC_ERR_UNSUPPORTED, "padded lattice dimension too large for the shared-memory FFT"));
   auto alloc = [&](void** p, size_t bytes) -> int {
@@ -1558,11 +1562,15 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     for (int r : {1, 2, 4, 8, 16}) {
       if (r > rows || x_pass_smem(h->px.p, r, cs) > smem_limit()) continue;
       for (int tx : {1, 2, 4, 8}) {
-        if (tx > g.hx || col_pass_smem(h->py.p, tx, cs) > smem_limit()) continue;
+        // a tile the copying form cannot hold is tried in place
+        const bool fits = col_pass_smem(h->py.p, tx, cs, base.col_lean != 0) <= smem_limit();
+        const bool fits_lean = col_pass_smem(h->py.p, tx, cs, true) <= smem_limit();
+        if (tx > g.hx || !(fits || fits_lean)) continue;
         if (r == base.x_rows_per_cta && tx == base.col_tx) continue;
         DemagTuning t = base;
         t.x_rows_per_cta = r;
         t.col_tx = tx;
+        if (!fits) t.col_lean = 1;
         t.col_threads = col_threads_for(g, h->py.p, h->pz.p, tx, t.col_tx_z);
         trial({0, t});
       }
@@ -1581,7 +1589,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
           if (flip) d.tun.col_lean = 1 - cur.tun.col_lean;
           if (half) d.tun.col_threads = std::max(64, cur.tun.col_threads / 2);
           if (half && d.tun.col_threads == cur.tun.col_threads) continue;
-          if (!d.tun.col_lean && col_pass_smem(h->py.p, d.tun.col_tx, cs) > smem_limit()) continue;
+          if (col_pass_smem(h->py.p, d.tun.col_tx, cs, d.tun.col_lean != 0) > smem_limit()) continue;
           trial(d);
         }
     }
@@ -2215,8 +2223,9 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
   const int band = shape[5];
   auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
   if (!pow2(t.x_rows_per_cta) || t.x_rows_per_cta > 16 || x_pass_smem(h->px.p, t.x_rows_per_cta, cs) > smem_limit() ||
-      !pow2(t.col_tx) || t.col_tx > 64 || col_pass_smem(h->py.p, t.col_tx, cs) > smem_limit() || !pow2(t.col_tx_z) ||
-      t.col_tx_z > 64 || col_pass_smem(h->pz.p, t.col_tx_z, cs) > smem_limit() || t.col_threads % t.col_tx != 0 ||
+      !pow2(t.col_tx) || t.col_tx > 64 || col_pass_smem(h->py.p, t.col_tx, cs, t.col_lean != 0) > smem_limit() ||
+      !pow2(t.col_tx_z) || t.col_tx_z > 64 || col_pass_smem(h->pz.p, t.col_tx_z, cs, t.col_lean != 0) > smem_limit() ||
+      t.col_threads % t.col_tx != 0 ||
       t.col_threads % t.col_tx_z != 0 ||
       (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
       t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_BAND ||
