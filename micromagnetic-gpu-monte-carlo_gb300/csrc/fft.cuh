@@ -366,6 +366,117 @@ __device__ __noinline__ void fft_lines_warp(C<T>* buf, int nlines, int stride, c
   fft_lines_warp_body<T, INV, A, B, PAD>(buf, nlines, stride, roots);
 }
 
+// ------------------------------------------------------ per-thread DFT
+// A whole short line (N <= 16) in one thread's registers, by mixed-radix
+// decimation in time with every index known at compile time: N = F M with F
+// the smallest prime factor, X[k1 + M k2] = DFT_F over f of
+// W_N^(f k1) Y_f[k1], Y_f = DFT_M(x[F m + f]).  Radix 2, 3, 4 and 5
+// butterflies are written out; other primes are direct DFTs.  Roots:
+// rt[j * RS] = exp(-2 pi i j / N) (a table of N * RS roots in shared memory).
+template <int N>
+struct SmallFactor {
+  static constexpr int value = N % 4 == 0 ? 4 : N % 2 == 0 ? 2 : N % 3 == 0 ? 3 : N % 5 == 0 ? 5 : N % 7 == 0 ? 7 : N;
+};
+
+template <typename T, bool INV, int N, int RS>
+struct ThreadDft {
+  __device__ __forceinline__ static void run(C<T>* v, const C<T>* rt) {
+    using V = C<T>;
+    constexpr int F = SmallFactor<N>::value, M = N / F;
+    if constexpr (M == 1) {
+      butterfly(v, rt);
+    } else {
+      V sub[F][M];
+#pragma unroll
+      for (int f = 0; f < F; ++f)
+#pragma unroll
+        for (int m = 0; m < M; ++m) sub[f][m] = v[F * m + f];
+#pragma unroll
+      for (int f = 0; f < F; ++f) ThreadDft<T, INV, M, RS * F>::run(sub[f], rt);
+#pragma unroll
+      for (int k1 = 0; k1 < M; ++k1) {
+        V z[F];
+#pragma unroll
+        for (int f = 0; f < F; ++f) {
+          const int e = (f * k1) % N;
+          if (e == 0) {
+            z[f] = sub[f][k1];
+          } else {
+            const V w = rt[e * RS];
+            z[f] = INV ? cmulc(sub[f][k1], w) : cmul(sub[f][k1], w);
+          }
+        }
+        ThreadDft<T, INV, F, RS * M>::run(z, rt);
+#pragma unroll
+        for (int k2 = 0; k2 < F; ++k2) v[k1 + M * k2] = z[k2];
+      }
+    }
+  }
+  // N prime or 4: the butterfly on v[0..N)
+  __device__ __forceinline__ static void butterfly(C<T>* v, const C<T>* rt) {
+    using V = C<T>;
+    if constexpr (N == 2) {
+      const V a = v[0], b = v[1];
+      v[0] = cadd(a, b);
+      v[1] = csub(a, b);
+    } else if constexpr (N == 4) {
+      const V a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]), a2 = cadd(v[1], v[3]), a3 = csub(v[1], v[3]);
+      const V r3 = INV ? cmk<V>(-a3.y, a3.x) : cmk<V>(a3.y, -a3.x);
+      v[0] = cadd(a0, a2);
+      v[1] = cadd(a1, r3);
+      v[2] = csub(a0, a2);
+      v[3] = csub(a1, r3);
+    } else if constexpr (N == 3) {
+      const T s3 = (T)0.86602540378443864676;  // sin(2 pi / 3)
+      const V v0 = v[0], t1 = cadd(v[1], v[2]), t3 = csub(v[1], v[2]);
+      const V t2 = cmk<V>(v0.x - (T)0.5 * t1.x, v0.y - (T)0.5 * t1.y);
+      const V r = INV ? cmk<V>(-s3 * t3.y, s3 * t3.x) : cmk<V>(s3 * t3.y, -s3 * t3.x);
+      v[0] = cadd(v0, t1);
+      v[1] = cadd(t2, r);
+      v[2] = csub(t2, r);
+    } else if constexpr (N == 5) {
+      const T c1 = (T)0.30901699437494742410, c2 = (T)-0.80901699437494742410;
+      const T s1 = (T)0.95105651629515357212, s2 = (T)0.58778525229247312917;
+      const V v0 = v[0];
+      const V t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]), t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+      const V a1 = cmk<V>(v0.x + c1 * t1.x + c2 * t2.x, v0.y + c1 * t1.y + c2 * t2.y);
+      const V a2 = cmk<V>(v0.x + c2 * t1.x + c1 * t2.x, v0.y + c2 * t1.y + c1 * t2.y);
+      const V b1 = cmk<V>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+      const V b2 = cmk<V>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+      const V mb1 = INV ? cmk<V>(-b1.y, b1.x) : cmk<V>(b1.y, -b1.x);
+      const V mb2 = INV ? cmk<V>(-b2.y, b2.x) : cmk<V>(b2.y, -b2.x);
+      v[0] = cadd(v0, cadd(t1, t2));
+      v[1] = cadd(a1, mb1);
+      v[2] = cadd(a2, mb2);
+      v[3] = csub(a2, mb2);
+      v[4] = csub(a1, mb1);
+    } else {  // other primes: direct DFT
+      V x[N];
+#pragma unroll
+      for (int j = 0; j < N; ++j) x[j] = v[j];
+#pragma unroll
+      for (int k = 0; k < N; ++k) {
+        V acc = x[0];
+#pragma unroll
+        for (int j = 1; j < N; ++j) {
+          const int e = (j * k) % N;
+          if (e == 0) {
+            acc = cadd(acc, x[j]);
+          } else {
+            const V w = rt[e * RS];
+            acc = cadd(acc, INV ? cmulc(x[j], w) : cmul(x[j], w));
+          }
+        }
+        v[k] = acc;
+      }
+    }
+  }
+};
+template <typename T, bool INV, int RS>
+struct ThreadDft<T, INV, 1, RS> {
+  __device__ __forceinline__ static void run(C<T>*, const C<T>*) {}
+};
+
 // Transform dispatcher: the warp-level path for the lengths the plan marks,
 // the Stockham stages otherwise.  Returns the buffer holding the result; all
 // threads of the block must call it after the input is complete

@@ -436,6 +436,84 @@ __global__ void __launch_bounds__(256) k_col_pass_wide(FftPlan p, int ncomp, C<T
                               inv_n, tx, s_rstride, lean);
 }
 
+// Column pass for short lines (n <= 16: the padded z axis of thin 3-D
+// lattices, short y axes): one thread per column (kx, plane) holding the three
+// component lines in registers, transformed by ThreadDft -- no shared-memory
+// staging, no barriers, and loads and stores coalesced across the threads'
+// consecutive kx.  Same flags, product and tensor layout as k_col_pass.
+template <typename T, int N>
+__global__ void __launch_bounds__(128) k_col_short(FftPlan p, C<T>* __restrict__ S, long long nspec,
+                                                   const C<T>* __restrict__ khat, int hx, long long plane_stride,
+                                                   long long pos_stride, int load_lim, int store_lim, int flags,
+                                                   T inv_n, long long s_rstride) {
+  using V = C<T>;
+  __shared__ V rt[N];
+  S += blockIdx.z * s_rstride;
+  {
+    const V* src = plan_tw<T>(p) + p.full_off;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) rt[i] = src[i];
+  }
+  __syncthreads();
+  const int kx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (kx >= hx) return;
+  const long long base = (long long)blockIdx.y * plane_stride + kx;
+  V v[3][N];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int z = 0; z < N; ++z) v[c][z] = z < load_lim ? S[c * nspec + base + z * pos_stride] : cmk<V>(0, 0);
+  if (flags & PASS_FWD) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) ThreadDft<T, false, N, 1>::run(v[c], rt);
+  }
+  if (flags & PASS_MUL) {
+#pragma unroll
+    for (int z = 0; z < N; ++z) {
+      const V* kk = khat + base + z * pos_stride;
+      V kxx = kk[0], kxy = kk[nspec], kxz = kk[2 * nspec];
+      V kyy = kk[3 * nspec], kyz = kk[4 * nspec], kzz = kk[5 * nspec];
+      if (flags & PASS_SYM) kxx.y = kxy.y = kxz.y = kyy.y = kyz.y = kzz.y = (T)0;
+      const V mx = v[0][z], my = v[1][z], mz = v[2][z];
+      T hxr = (mx.x * kxx.x - mx.y * kxx.y) + (my.x * kxy.x - my.y * kxy.y) + (mz.x * kxz.x - mz.y * kxz.y);
+      T hxi = (mx.x * kxx.y + mx.y * kxx.x) + (my.x * kxy.y + my.y * kxy.x) + (mz.x * kxz.y + mz.y * kxz.x);
+      T hyr = (mx.x * kxy.x - mx.y * kxy.y) + (my.x * kyy.x - my.y * kyy.y) + (mz.x * kyz.x - mz.y * kyz.y);
+      T hyi = (mx.x * kxy.y + mx.y * kxy.x) + (my.x * kyy.y + my.y * kyy.x) + (mz.x * kyz.y + mz.y * kyz.x);
+      T hzr = (mx.x * kxz.x - mx.y * kxz.y) + (my.x * kyz.x - my.y * kyz.y) + (mz.x * kzz.x - mz.y * kzz.y);
+      T hzi = (mx.x * kxz.y + mx.y * kxz.x) + (my.x * kyz.y + my.y * kyz.x) + (mz.x * kzz.y + mz.y * kzz.x);
+      v[0][z] = cmk<V>(hxr * inv_n, hxi * inv_n);
+      v[1][z] = cmk<V>(hyr * inv_n, hyi * inv_n);
+      v[2][z] = cmk<V>(hzr * inv_n, hzi * inv_n);
+    }
+  }
+  if (flags & PASS_INV) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) ThreadDft<T, true, N, 1>::run(v[c], rt);
+  }
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int z = 0; z < N; ++z)
+      if (z < store_lim) S[c * nspec + base + z * pos_stride] = v[c][z];
+}
+
+// The short-line kernel for length n, or null.
+template <typename T>
+using ColShortFn = void (*)(FftPlan, C<T>*, long long, const C<T>*, int, long long, long long, int, int, int, T,
+                            long long);
+template <typename T>
+ColShortFn<T> col_short_kernel(int n) {
+  switch (n) {
+#define MMC_CS(N_) \
+  case N_:         \
+    return k_col_short<T, N_>;
+    MMC_CS(2) MMC_CS(3) MMC_CS(4) MMC_CS(5) MMC_CS(6) MMC_CS(7) MMC_CS(8) MMC_CS(9) MMC_CS(10) MMC_CS(11)
+    MMC_CS(12) MMC_CS(13) MMC_CS(14) MMC_CS(15) MMC_CS(16)
+#undef MMC_CS
+    default:
+      return nullptr;
+  }
+}
+
 // =========================================================== lattice helpers
 // Neighbour index along an axis, or -1 when the bond does not exist (open
 // edge, or a periodic axis of length 1 where the neighbour is the cell itself).
@@ -1462,6 +1540,15 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
                          int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
                          int flags, T inv_n, int tx, int threads, cudaStream_t st, int nrep = 1,
                          long long s_rstride = 0, bool inl = false, bool lean = false) {
+  if (ncomp == 3 && p.n <= 16 && p.full_off > 0) {  // short lines: one thread per column
+    const ColShortFn<T> ks = col_short_kernel<T>(p.n);
+    if (ks) {
+      dim3 grid((hx + 127) / 128, planes, nrep);
+      ks<<<grid, 128, 0, st>>>(p, S, nspec, khat, hx, plane_stride, pos_stride, load_lim, store_lim, flags, inv_n,
+                               s_rstride);
+      return cudaGetLastError();
+    }
+  }
   if (tx < 1 || (tx & (tx - 1)) != 0 || threads % tx != 0) return cudaErrorInvalidValue;  // see k_col_pass
   lean = lean && p.warp_a != 0;  // in-place transforms exist for the warp path only
   size_t sm = lean ? col_pass_smem_lean(p, ncomp, tx, sizeof(C<T>))

@@ -12,14 +12,14 @@ namespace mmc {
 // 0 <= n < 2^31.  The kernels' index arithmetic divides by lattice and
 // transform sizes that are only known at run time.
 #ifdef __CUDACC__
-#define MMC_HD __host__ __device__
+#define MMC_HDI __host__ __device__
 #else
-#define MMC_HD
+#define MMC_HDI
 #endif
 struct FastDiv {
   uint32_t d = 1, m = 1, l = 0;
   FastDiv() = default;
-  MMC_HD explicit FastDiv(uint32_t dd) : d(dd ? dd : 1) {
+  MMC_HDI explicit FastDiv(uint32_t dd) : d(dd ? dd : 1) {
     l = 0;
     while ((1ull << l) < d) ++l;
     m = (uint32_t)(((1ull << 32) * ((1ull << l) - d)) / d + 1);
@@ -120,7 +120,7 @@ constexpr int NQ = 9;
 // the tile's 8 columns over the banks (+2 for 8-byte FP32 complex values,
 // whose 16-lane wavefronts then touch distinct banks; +1 for 16-byte FP64
 // ones).
-MMC_HD inline int col_line_stride(const FftPlan& p, size_t csize) {
+MMC_HDI inline int col_line_stride(const FftPlan& p, size_t csize) {
   return p.n + p.warp_a + (csize == 8 ? 2 : 1);
 }
 

@@ -113,14 +113,18 @@ int make_plan(int n, PlanHost* ph) {
     if (n == w[0]) {
       p.warp_a = w[1];
       p.warp_b = w[2];
-      p.full_off = (int)(tw.size() / 2);
-      for (int j = 0; j < n; ++j) {
-        double c, sn;
-        unit_root(j, n, &c, &sn);
-        tw.push_back(c);
-        tw.push_back(sn);
-      }
     }
+  // all n roots exp(-2 pi i j / n) for the warp-level transforms and for the
+  // per-thread transforms of short lines (n <= 16)
+  if (p.warp_a || n <= 16) {
+    p.full_off = (int)(tw.size() / 2);
+    for (int j = 0; j < n; ++j) {
+      double c, sn;
+      unit_root(j, n, &c, &sn);
+      tw.push_back(c);
+      tw.push_back(sn);
+    }
+  }
   p.tw_total = (int)(tw.size() / 2);
   size_t cnt = tw.size() / 2;
   if (cnt == 0) cnt = 1, tw.push_back(1.0), tw.push_back(0.0);
