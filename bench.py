@@ -252,6 +252,19 @@ SLAB = dict(nx=512, ny=512, nz=8, dx=2e-9, dy=2e-9, dz=1e-9, ms=1.1e6, Aex=15e-1
             cal_demag_flag=1, randomseed=7, use_random_init=1)
 
 
+def launches_per_step(S, shape, R, graph_sweeps=32):
+    """Kernel launches of one timed step of S sweeps with a launch shape: per
+    sweep the row kernel and the column pass (row path), or the x, column and
+    inverse x passes and the Metropolis launches (one tile launch, or one per
+    colour), once per replica part inside the 32-sweep graphs and on one stream
+    for the sweeps left over; one counter advance per graph and after the
+    left-over sweeps."""
+    per = 2 if shape[5] > 0 else 4 if shape[6] == 1 else 5
+    parts = 1 if shape[5] > 0 else min(shape[9], R)
+    graphs, rem = divmod(S, graph_sweeps)
+    return graphs * graph_sweeps * per * parts + rem * per + graphs + (1 if rem else 0)
+
+
 def slab_line(M, local, sweeps):
     """The 3-D slab in FP32: 512x512x8 cells, PBC 10 images in x and y, open
     in z (padded to 15 layers), seed 7, one lattice on the pass kernels.  The
@@ -489,7 +502,7 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": R * 3 * n * 8, "d2h_bytes_per_step": R * 3 * n * 8},
         "roofline": roofline,
         "clocks": clk.summary(),
-        "gpu_launches": args.steps * S * (3 if shape[5] > 0 else 5 if shape[6] == 1 else 6),
+        "gpu_launches": args.steps * launches_per_step(S, shape, R),
         "single_lattice_fp32": {"value": single_v, "unit": UNIT, "engine": single_engine,
                                 "film_engine_phase_us": phases},
         "fp64_plain": fp64_line,
