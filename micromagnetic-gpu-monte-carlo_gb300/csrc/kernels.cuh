@@ -833,13 +833,17 @@ __device__ __forceinline__ void st4(T* p, const Vec4<T>& r) {
 
 // The decisions of the two cells at offsets P0 and P0 + 2 of a segment.
 // ALLB: every x and y bond exists (both axes periodic, ny > 1), so the
-// availability flags are compile-time true.
-template <typename T, int P0, bool ALLB>
+// availability flags are compile-time true.  Z3: a 3-D lattice, with the
+// segments of the layers below (zd) and above (zu) and their flags; films
+// pass anything there.
+template <typename T, int P0, bool ALLB, bool Z3 = false>
 __device__ __forceinline__ bool quad_cells(const McCoef<T>& c, Vec4<T> (&own)[3], const Vec4<T> (&up)[3],
                                            const Vec4<T> (&dn)[3], const T (&lft)[3], const T (&rgt)[3],
                                            const Vec4<T> (&hh)[3], bool hl, bool hr, bool hd, bool hu,
-                                           uint32_t cell0, uint32_t stage, uint32_t sweep, unsigned int& mine) {
+                                           uint32_t cell0, uint32_t stage, uint32_t sweep, unsigned int& mine,
+                                           const Vec4<T> (&zd)[3], const Vec4<T> (&zu)[3], bool hzd, bool hzu) {
   if constexpr (ALLB) hl = hr = hd = hu = true;
+  if constexpr (!Z3) hzd = hzu = false;
   bool changed = false;
 #pragma unroll
   for (int q = 0; q < 2; ++q) {
@@ -850,7 +854,8 @@ __device__ __forceinline__ bool quad_cells(const McCoef<T>& c, Vec4<T> (&own)[3]
     nb.has[0][1] = rin || hr;
     nb.has[1][0] = hd;
     nb.has[1][1] = hu;
-    nb.has[2][0] = nb.has[2][1] = false;
+    nb.has[2][0] = hzd;
+    nb.has[2][1] = hzu;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const T ov = own[k].v[o];
@@ -858,7 +863,8 @@ __device__ __forceinline__ bool quad_cells(const McCoef<T>& c, Vec4<T> (&own)[3]
       nb.v[0][1][k] = rin ? own[k].v[(o + 1) & 3] : (hr ? rgt[k] : ov);
       nb.v[1][0][k] = hd ? dn[k].v[o] : ov;
       nb.v[1][1][k] = hu ? up[k].v[o] : ov;
-      nb.v[2][0][k] = nb.v[2][1][k] = ov;
+      nb.v[2][0][k] = hzd ? zd[k].v[o] : ov;
+      nb.v[2][1][k] = hzu ? zu[k].v[o] : ov;
     }
     const Proposal<T> pr = mc_propose<T>(c, cell0 + (uint32_t)o, stage, sweep);
     if (mc_accept<T>(c, nb, own[0].v[o], own[1].v[o], own[2].v[o], hh[0].v[o], hh[1].v[o], hh[2].v[o], pr)) {
@@ -872,15 +878,16 @@ __device__ __forceinline__ bool quad_cells(const McCoef<T>& c, Vec4<T> (&own)[3]
   return changed;
 }
 
-__host__ __device__ inline bool mc_quad_ok(const Geom& g) { return g.nz == 1 && g.ncolors == 2 && g.nx % 4 == 0; }
+__host__ __device__ inline bool mc_quad_ok(const Geom& g) { return g.ncolors == 2 && g.nx % 4 == 0; }
 // every x and y bond of a film exists
 __host__ __device__ inline bool mc_all_bonds(const Geom& g) { return g.per[0] && g.per[1] && g.nx > 1 && g.ny > 1; }
 // the staged form (k_mc_band) for the same lattices, up to 1024 cells per row
 // (a band of one row then fits in 96 KB of shared memory in FP64)
 constexpr size_t MC_BAND_SMEM_MAX = 96 * 1024;
-__host__ __device__ inline bool mc_band_ok(const Geom& g) { return mc_quad_ok(g) && g.nx <= 1024; }
+__host__ __device__ inline bool mc_band_ok(const Geom& g) { return g.nz == 1 && mc_quad_ok(g) && g.nx <= 1024; }
 
-template <typename T, bool ALLB>
+// Z3: 3-D lattices (nz > 1), with the segments of the layers below and above.
+template <typename T, bool ALLB, bool Z3>
 __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m,
                                                  const T* __restrict__ h, const SweepCounters* __restrict__ ctr,
                                                  int color, unsigned long long* acc) {
@@ -892,10 +899,16 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
   const int nseg = g.nx >> 2;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned int mine = 0;
-  if (t < nseg * g.ny) {
-    const int y = t / nseg, s = t - y * nseg;  // nseg is a power of two for the usual sizes; cheap either way
+  if (t < nseg * g.ny * g.nz) {
+    const int row = t / nseg, s = t - row * nseg;  // nseg is a power of two for the usual sizes; cheap either way
+    int z = 0, y = row;
+    if constexpr (Z3) {
+      z = g.dny.div(row);
+      y = row - z * g.ny;
+    }
     const int x0 = 4 * s;
-    const long long rowb = (long long)y * g.nx;
+    const long long rowb = (long long)row * g.nx;
+    const long long plane = (long long)g.nx * g.ny;
     // neighbour rows: wrapped on a periodic axis, missing at an open edge or
     // when the axis has length 1
     int yu = y + 1, yd = y - 1;
@@ -903,6 +916,12 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
     if (yu >= g.ny) { if (g.per[1]) yu -= g.ny; else hu = false; }
     if (yd < 0) { if (g.per[1]) yd += g.ny; else hd = false; }
     if (g.ny == 1) hu = hd = false;
+    int zu = z + 1, zd = z - 1;
+    bool hzu = Z3, hzd = Z3;
+    if constexpr (Z3) {
+      if (zu >= g.nz) { if (g.per[2]) zu -= g.nz; else hzu = false; }
+      if (zd < 0) { if (g.per[2]) zd += g.nz; else hzd = false; }
+    }
     // side cells
     int xl = x0 - 1, xr = x0 + 4;
     bool hl = true, hr = true;
@@ -912,15 +931,22 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
     // this colour's cells sit at offsets p0 and p0 + 2 (x0 is even), so only
     // one side cell is a neighbour: the left one for p0 = 0, the right one
     // for p0 = 1
-    const int p0 = (color + y) & 1;
-    Vec4<T> own[3], up[3], dn[3];
+    const int p0 = (color + y + z) & 1;
+    const long long zbase = (long long)z * plane;
+    Vec4<T> own[3], up[3], dn[3], zup[3], zdn[3];
     T lft[3], rgt[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const T* base = m + k * n;
       own[k] = ld4<T>(base + rowb + x0);
-      up[k] = hu ? ld4<T>(base + (long long)yu * g.nx + x0) : own[k];
-      dn[k] = hd ? ld4<T>(base + (long long)yd * g.nx + x0) : own[k];
+      up[k] = hu ? ld4<T>(base + zbase + (long long)yu * g.nx + x0) : own[k];
+      dn[k] = hd ? ld4<T>(base + zbase + (long long)yd * g.nx + x0) : own[k];
+      if constexpr (Z3) {
+        zup[k] = hzu ? ld4<T>(base + (long long)zu * plane + (long long)y * g.nx + x0) : own[k];
+        zdn[k] = hzd ? ld4<T>(base + (long long)zd * plane + (long long)y * g.nx + x0) : own[k];
+      } else {
+        zup[k] = zdn[k] = own[k];
+      }
       lft[k] = (hl && p0 == 0) ? base[rowb + xl] : (T)0;
       rgt[k] = (hr && p0 == 1) ? base[rowb + xr] : (T)0;
     }
@@ -935,11 +961,11 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
     // registers
     bool changed;
     if (p0 == 0)
-      changed = quad_cells<T, 0, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
-                                 ctr->sweep, mine);
+      changed = quad_cells<T, 0, ALLB, Z3>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0),
+                                           ctr->stage, ctr->sweep, mine, zdn, zup, hzd, hzu);
     else
-      changed = quad_cells<T, 1, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
-                                 ctr->sweep, mine);
+      changed = quad_cells<T, 1, ALLB, Z3>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0),
+                                           ctr->stage, ctr->sweep, mine, zdn, zup, hzd, hzu);
     if (changed) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) st4<T>(m + k * n + rowb + x0, own[k]);
@@ -951,7 +977,7 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, (unsigned long long)v);
 }
 
-// One colour of a two-colour film sweep (the k_mc_quad cases) with the rows
+// One colour of a two-colour film sweep (the k_mc_quad film cases) with the rows
 // a CTA needs staged in shared memory first: the CTA owns a band of `band`
 // rows of one replica, copies m rows y0-1 .. y0+band (wrapped on a periodic
 // axis) and h rows y0 .. y0+band-1 with 16-byte asynchronous copies, which
@@ -1053,10 +1079,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_mc_band(Geom g,
     bool changed;
     if (p0 == 0)
       changed = quad_cells<T, 0, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
-                                 ctr->sweep, mine);
+                                 ctr->sweep, mine, own, own, false, false);
     else
       changed = quad_cells<T, 1, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
-                                 ctr->sweep, mine);
+                                 ctr->sweep, mine, own, own, false, false);
     if (changed) {
 #pragma unroll
       for (int k = 0; k < 3; ++k) st4<T>(m + k * n + rowb + x0, own[k]);
@@ -1644,9 +1670,10 @@ cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const S
     return cudaGetLastError();
   }
   if (form == MC_FORM_QUAD && mc_quad_ok(g)) {
-    const long long total = (long long)g.ny * (g.nx >> 2);
+    const long long total = (long long)g.ny * g.nz * (g.nx >> 2);
     dim3 grid((unsigned)((total + threads - 1) / threads), 1, nrep);
-    auto kern = mc_all_bonds(g) ? k_mc_quad<T, true> : k_mc_quad<T, false>;
+    auto kern = g.nz > 1 ? (mc_all_bonds(g) ? k_mc_quad<T, true, true> : k_mc_quad<T, false, true>)
+                         : (mc_all_bonds(g) ? k_mc_quad<T, true, false> : k_mc_quad<T, false, false>);
     kern<<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);
     return cudaGetLastError();
   }

@@ -204,10 +204,12 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   t.col_tx = pick(py, g.nzp == 1 ? 1 : g.nz, g.nzp == 1);
   t.col_tx_z = pick(pz, g.nyp, true);
   t.col_threads = col_threads_for(g, py, pz, t.col_tx, t.col_tx_z);
-  // FP32 film batches: the vectorised per-colour sweep, measured faster from
-  // about 8 replicas; single lattices and FP64 keep the scalar form (the
-  // autotuner tries every form)
-  t.mc_form = csize == 8 && nrep >= 8 && mc_quad_eligible(g) ? MC_FORM_QUAD : MC_FORM_SCALAR;
+  // FP32 with at least 8 x 256^2 trials per launch (batches of 8 films, a
+  // 512x512x8 slab): the vectorised per-colour sweep, measured faster there;
+  // smaller lattices and FP64 keep the scalar form (the autotuner tries every
+  // form)
+  t.mc_form = csize == 8 && (long long)nrep * g.n >= 8LL * 65536 && mc_quad_eligible(g) ? MC_FORM_QUAD
+                                                                                      : MC_FORM_SCALAR;
   t.fft_inline = 0;
   return t;
 }

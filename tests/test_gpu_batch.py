@@ -118,6 +118,41 @@ def test_mc_forms_bitwise_equal_scalar_kernels(M, prec, geom, form):
         assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
 
 
+QUAD3D_GEOMS = [dict(nx=8, ny=6, nz=4, pbc_x=1, pbc_y=1, pbc_z=0), dict(nx=12, ny=5, nz=4, pbc_x=2, pbc_y=0, pbc_z=1),
+                dict(nx=16, ny=8, nz=2, pbc_x=1, pbc_y=1, pbc_z=1)]
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("geom", QUAD3D_GEOMS)
+def test_vector_form_on_3d_lattices(M, O, prec, geom):
+    """The vectorised per-colour form with neighbour layers (3-D lattices)
+    against the scalar form, and in FP64 against the oracle's decisions."""
+    cfgs = cfgs_for(M, 2, prec, sweep_engine=1, **geom)
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        sa, sb = list(a.launch_shape()), list(b.launch_shape())
+        sa[6], sb[6] = 0, 2
+        a.set_launch_shape(sa)
+        b.set_launch_shape(sb)
+        m0 = b.get_m(0)
+        for s0, n in ((0, 21), (21, 32)):
+            a.run_sweeps(3, s0, n)
+            b.run_sweeps(3, s0, n)
+        for r in range(2):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        ob = b.energy()  # the accept counters are read once
+        assert [o.accepted for o in a.energy()] == [o.accepted for o in ob]
+        got = b.get_m(0)
+        acc = ob[0].accepted
+    if prec == 64:
+        c = cfgs[0]
+        with M.Lattice(c) as lat:
+            k6 = lat.tensor()
+        m = m0.copy()
+        want = O.sweeps(c, k6, c.Temperature_start, 3, 0, 53, m, demag_mode=1)
+        assert acc == want
+        assert np.array_equal(got, m)
+
+
 @pytest.mark.parametrize("form", [1, 2, 3])
 def test_mc_forms_fp64_decisions_match_oracle(M, O, form):
     c = cfgs_for(M, 1, 64, sweep_engine=1, nx=64, ny=64, pbc_x=1, pbc_y=1)[0]
