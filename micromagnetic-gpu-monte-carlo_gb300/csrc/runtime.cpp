@@ -148,6 +148,21 @@ void free_plan(PlanHost* ph) {
 
 size_t smem_limit() { return 220 * 1024; }  // below the 227 KB opt-in limit of a CTA
 
+// Shared memory of an x pass with r rows per CTA, of a column pass with tx
+// columns per CTA (bytes).
+size_t x_pass_smem(const FftPlan& px, int r, size_t csize) {
+  if (px.warp_a)  // k_x_forward_w / k_x_inverse_w: the roots and 2 r padded lines
+    return ((size_t)px.n + 2 * (size_t)r * (px.n + px.warp_a)) * csize;
+  return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize;
+}
+// (lean: the in-place form, which exists for warp-shaped lengths only and
+// holds the tile once without a K^ tile)
+size_t col_pass_smem(const FftPlan& p, int tx, size_t csize, bool lean = false) {
+  const size_t tw = (size_t)((p.tw_total + 1) & ~1), lines = (size_t)3 * tx * col_line_stride(p, csize);
+  if (lean && p.warp_a) return (tw + lines) * csize;
+  return (tw + 2 * lines + 6 * (size_t)p.n * tx) * csize;
+}
+
 // Launch shapes for `nrep` replicas.  The warp-level FFT gives each warp
 // 32 / B lines, so a CTA takes enough rows / columns to keep all its warps
 // busy, and column tiles are widened to whole 32-byte sectors when there are
@@ -169,7 +184,7 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   DemagTuning t;
   const long long rows = (long long)g.ny * g.nz;
   const long long want = 2LL * nsm;
-  auto xsm = [&](int r) { return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize; };
+  auto xsm = [&](int r) { return x_pass_smem(px, r, csize); };
   t.x_threads = px.n >= 512 ? 256 : 128;
   int r = 1;
   if (px.warp_a) {
@@ -214,18 +229,6 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   return t;
 }
 
-// Shared memory of an x pass with r rows per CTA, of a column pass with tx
-// columns per CTA (bytes).
-size_t x_pass_smem(const FftPlan& px, int r, size_t csize) {
-  return ((size_t)((px.tw_total + 1) & ~1) + 2 * (size_t)r * 2 * px.n) * csize;
-}
-// (lean: the in-place form, which exists for warp-shaped lengths only and
-// holds the tile once without a K^ tile)
-size_t col_pass_smem(const FftPlan& p, int tx, size_t csize, bool lean = false) {
-  const size_t tw = (size_t)((p.tw_total + 1) & ~1), lines = (size_t)3 * tx * col_line_stride(p, csize);
-  if (lean && p.warp_a) return (tw + lines) * csize;
-  return (tw + 2 * lines + 6 * (size_t)p.n * tx) * csize;
-}
 
 }  // namespace
 
