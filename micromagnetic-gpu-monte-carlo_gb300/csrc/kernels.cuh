@@ -15,6 +15,34 @@
 
 namespace mmc {
 
+// =========================================================== launch helpers
+// Programmatic dependent launch: a kernel launched by launch_pdl may be
+// scheduled before the previous kernel of its stream (or graph branch) has
+// retired, and calls pdl_wait() before it reads anything a previous kernel
+// writes or writes anything one reads; before the wait it touches only
+// constant tables (transform roots and twiddles).  The previous kernels
+// trigger implicitly when their CTAs exit: an explicit early trigger let the
+// next grid's waiting CTAs take SM slots during the tail and cost 4 us per
+// batched sweep.  The wait returns at once for a kernel launched without the
+// attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                       Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, args...);
+}
+
 // =========================================================== demag passes
 //
 // The reference computes H^ = K^ . M^ / N with three cuFFT R2C transforms and
@@ -184,6 +212,7 @@ __global__ void __launch_bounds__(256, x_w_min_blocks<T, A>()) k_x_forward_w(Fft
   V* roots = reinterpret_cast<V*>(smem_raw);
   V* buf = roots + L;  // line pr * nr + rr: row rr, pair pr (mx + i my, mz + 0 i)
   load_roots<T>(p, roots);
+  pdl_wait();
   __syncthreads();
   const int row0 = blockIdx.x * rows_per_cta;
   const int nr = min(rows_per_cta, nrows - row0);
@@ -238,6 +267,7 @@ __global__ void __launch_bounds__(256, x_w_min_blocks<T, A>()) k_x_inverse_w(Fft
   V* roots = reinterpret_cast<V*>(smem_raw);
   V* buf = roots + L;  // line rr: hx + i hy of row rr; line nr + rr: hz
   load_roots<T>(p, roots);
+  pdl_wait();
   __syncthreads();
   const int row0 = blockIdx.x * rows_per_cta;
   const int nr = min(rows_per_cta, nrows - row0);
@@ -343,6 +373,7 @@ __device__ __forceinline__ void col_pass_body(const FftPlan& p, int ncomp, C<T>*
       }
     }
   }
+  pdl_wait();  // the spectrum is the previous pass's output
   // thread -> (column t, first position pos0); positions advance by pstep, so
   // the loops below need no division (tx is a power of two)
   const int lg = __ffs(tx) - 1;
@@ -453,6 +484,7 @@ __global__ void __launch_bounds__(128) k_col_short(FftPlan p, C<T>* __restrict__
     const V* src = plan_tw<T>(p) + p.full_off;
     for (int i = threadIdx.x; i < N; i += blockDim.x) rt[i] = src[i];
   }
+  pdl_wait();
   __syncthreads();
   const int kx = blockIdx.x * blockDim.x + threadIdx.x;
   if (kx >= hx) return;
@@ -761,6 +793,7 @@ __device__ __forceinline__ void count_accepts(bool acc, unsigned long long* coun
 template <typename T>
 __global__ void __launch_bounds__(256, 4) k_mc_checker(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
                              const SweepCounters* __restrict__ ctr, int color, unsigned long long* acc) {
+  pdl_wait();
   // replica blockIdx.z of a batch: its own coefficients, state and counter
   const McCoef<T> c = cp[blockIdx.z];
   m += blockIdx.z * 3 * g.n;
@@ -891,6 +924,7 @@ template <typename T, bool ALLB, bool Z3>
 __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m,
                                                  const T* __restrict__ h, const SweepCounters* __restrict__ ctr,
                                                  int color, unsigned long long* acc) {
+  pdl_wait();
   const McCoef<T> c = cp[blockIdx.z];
   const long long n = g.n;
   m += blockIdx.z * 3 * n;
@@ -1543,10 +1577,9 @@ cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int
     const XPassW<T> w = x_pass_w<T>(p);
     if (w.fwd) {
       dim3 grid((nrows + rpc - 1) / rpc, 1, nrep);
-      w.fwd<<<grid, threads, x_pass_w_smem(p, rpc, sizeof(C<T>)), st>>>(
-          p, xdata, FastDiv((uint32_t)ydata), nrows, in, in_cstride, S, nspec, nyp, hx, pitch, rpc, in_rstride,
-          s_rstride);
-      return cudaGetLastError();
+      return launch_pdl(w.fwd, grid, dim3(threads), x_pass_w_smem(p, rpc, sizeof(C<T>)), st, p, xdata,
+                        FastDiv((uint32_t)ydata), nrows, in, in_cstride, S, nspec, nyp, hx, pitch, rpc, in_rstride,
+                        s_rstride);
     }
   }
   if (ncomp == 3 && p.warp_a == 32) return cudaErrorInvalidValue;  // handled by k_x_forward_w above
@@ -1570,9 +1603,8 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
     const ColShortFn<T> ks = col_short_kernel<T>(p.n);
     if (ks) {
       dim3 grid((hx + 127) / 128, planes, nrep);
-      ks<<<grid, 128, 0, st>>>(p, S, nspec, khat, hx, plane_stride, pos_stride, load_lim, store_lim, flags, inv_n,
-                               s_rstride);
-      return cudaGetLastError();
+      return launch_pdl(ks, grid, dim3(128), 0, st, p, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
+                        store_lim, flags, inv_n, s_rstride);
     }
   }
   if (tx < 1 || (tx & (tx - 1)) != 0 || threads % tx != 0) return cudaErrorInvalidValue;  // see k_col_pass
@@ -1589,9 +1621,8 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
   threads = std::min(threads, fa.maxThreadsPerBlock & ~31);
   threads -= threads % std::max(tx, 32);
   if (threads < 32) return cudaErrorInvalidValue;
-  kern<<<grid, threads, sm, st>>>(p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
-                                           store_lim, flags, inv_n, tx, s_rstride, lean ? 1 : 0);
-  return cudaGetLastError();
+  return launch_pdl(kern, grid, dim3(threads), sm, st, p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride,
+                    load_lim, store_lim, flags, inv_n, tx, s_rstride, lean ? 1 : 0);
 }
 
 #define MMC_TRY(x)                       \
@@ -1633,8 +1664,8 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
   dim3 grid((rows + rpc - 1) / rpc, 1, nrep);
   const XPassW<T> w = x_pass_w<T>(px);
   if (w.inv) {
-    w.inv<<<grid, tun.x_threads, x_pass_w_smem(px, rpc, sizeof(C<T>)), st>>>(px, S, ns, g.nyp, g.hx, g.hxp, g.dnx,
-                                                                           g.dny, rows, h, g.n, rpc, sr, mr);
+    MMC_TRY(launch_pdl(w.inv, grid, dim3(tun.x_threads), x_pass_w_smem(px, rpc, sizeof(C<T>)), st, px,
+                       (const C<T>*)S, ns, g.nyp, g.hx, g.hxp, g.dnx, g.dny, rows, h, g.n, rpc, sr, mr));
   } else {
     if (px.warp_a == 32) return cudaErrorInvalidValue;  // the wide shapes have warp-shaped x passes
     size_t sm = x_pass_smem(px, 2, rpc, sizeof(C<T>));
@@ -1674,13 +1705,12 @@ cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const S
     dim3 grid((unsigned)((total + threads - 1) / threads), 1, nrep);
     auto kern = g.nz > 1 ? (mc_all_bonds(g) ? k_mc_quad<T, true, true> : k_mc_quad<T, false, true>)
                          : (mc_all_bonds(g) ? k_mc_quad<T, true, false> : k_mc_quad<T, false, false>);
-    kern<<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);
-    return cudaGetLastError();
+    return launch_pdl(kern, grid, dim3(threads), 0, st, g, c, m, h, ctr, color, acc);
   }
   if (g.ncolors == 2) {
     const long long total = (long long)g.ny * g.nz * ((g.nx + 1) / 2);
     dim3 grid((unsigned)((total + threads - 1) / threads), 1, nrep);
-    k_mc_checker<T><<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);
+    MMC_TRY(launch_pdl(k_mc_checker<T>, grid, dim3(threads), 0, st, g, c, m, h, ctr, color, acc));
   } else {
     dim3 grid((unsigned)((g.n + threads - 1) / threads), 1, nrep);
     k_mc_general<T><<<grid, threads, 0, st>>>(g, c, m, h, ctr, color, acc);

@@ -60,13 +60,13 @@ cudaError_t launch_tensor_fft(const Geom& g, const FftPlan& px, const FftPlan& p
 }
 
 __global__ void k_advance(SweepCounters* ctr, uint32_t delta, int count) {
+  pdl_wait();  // the previous kernels read the counters
   if ((int)threadIdx.x < count) ctr[threadIdx.x].sweep += delta;
 }
 
 cudaError_t launch_advance(SweepCounters* ctr, uint32_t delta, cudaStream_t st, int count) {
   if (count < 1 || count > 32) return cudaErrorInvalidValue;
-  k_advance<<<1, 32, 0, st>>>(ctr, delta, count);
-  return cudaGetLastError();
+  return launch_pdl(k_advance, dim3(1), dim3(32), 0, st, ctr, delta, count);
 }
 
 // One parallel-tempering pass: in each ladder, the temperature pairs (k, k+1)
