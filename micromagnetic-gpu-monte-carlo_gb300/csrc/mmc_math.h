@@ -318,7 +318,9 @@ MMC_HD u32x4 philox_round(u32x4 c, uint32_t k0, uint32_t k1) {
 // Ten rounds, key bumped by the Weyl constants between rounds.
 MMC_HD u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
   const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#if defined(__CUDA_ARCH__)
 #pragma unroll
+#endif
   for (int i = 0; i < 9; ++i) {
     c = philox_round(c, k0, k1);
     k0 += W0;

@@ -118,7 +118,7 @@ __device__ __forceinline__ void row_load(const RowPhase<T>& R, const McCoef<T>& 
   using V = C<T>;
   const int nx = R.g.nx, hxp = R.g.hxp;
   const long long n = R.g.n, nspec = R.g.nspec;
-  const int nslots = R.nb + 4, nwork = R.nb + 2, half = (nx + 1) >> 1;
+  const int nslots = R.nb + 4, nwork = R.nb + 2;
   const size_t mstride = 3 * (size_t)nx;
   const int elems = 16 / (int)sizeof(T), per_m = nx / elems;
   const int ve = 16 / (int)sizeof(V), per_s = hxp / ve;

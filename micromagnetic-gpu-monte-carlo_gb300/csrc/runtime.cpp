@@ -65,7 +65,7 @@ void unit_root(long long j, long long N, double* c, double* s) {
 
 int make_plan(int n, PlanHost* ph) {
   FftPlan& p = ph->p;
-  std::memset(&p, 0, sizeof p);
+  p = FftPlan{};
   p.n = n;
   std::vector<int> rad;
   int m = n;
