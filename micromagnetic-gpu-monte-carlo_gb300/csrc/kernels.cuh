@@ -1701,11 +1701,14 @@ cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const S
     return cudaGetLastError();
   }
   if (form == MC_FORM_QUAD && mc_quad_ok(g)) {
+    // 128-thread CTAs: the same warps per SM as 256 (the registers limit
+    // them), in finer pieces, measured 2 us faster per batched sweep
+    const int qthreads = 128;
     const long long total = (long long)g.ny * g.nz * (g.nx >> 2);
-    dim3 grid((unsigned)((total + threads - 1) / threads), 1, nrep);
+    dim3 grid((unsigned)((total + qthreads - 1) / qthreads), 1, nrep);
     auto kern = g.nz > 1 ? (mc_all_bonds(g) ? k_mc_quad<T, true, true> : k_mc_quad<T, false, true>)
                          : (mc_all_bonds(g) ? k_mc_quad<T, true, false> : k_mc_quad<T, false, false>);
-    return launch_pdl(kern, grid, dim3(threads), 0, st, g, c, m, h, ctr, color, acc);
+    return launch_pdl(kern, grid, dim3(qthreads), 0, st, g, c, m, h, ctr, color, acc);
   }
   if (g.ncolors == 2) {
     const long long total = (long long)g.ny * g.nz * ((g.nx + 1) / 2);
