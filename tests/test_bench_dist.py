@@ -53,3 +53,20 @@ def test_two_gloo_ranks():
     assert t0 == t1 == 2.0
     assert not set(s0) & set(s1) and s0[0] == 256
     assert ref1 is True
+
+
+def test_launch_count_of_a_step():
+    """bench.py's gpu_launches: per sweep the 5 pass kernels once per replica
+    part inside the 32-sweep graphs and on one stream for the left-over
+    sweeps, 2 for the row path, 4 with the tile form; one counter advance per
+    graph and after the left-over sweeps."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    shape = [4, 128, 8, 64, 384, 0, 2, 1, 1, 2]
+    assert bench.launches_per_step(10000, shape, 32) == 312 * 32 * 5 * 2 + 16 * 5 + 312 + 1
+    assert bench.launches_per_step(64, shape, 1) == 64 * 5 + 2  # one replica: one part
+    rows = [4, 128, 8, 8, 384, 4, 2, 1, 1, 3]
+    assert bench.launches_per_step(40, rows, 32) == 40 * 2 + 2
+    tile = [4, 128, 8, 8, 384, 0, 1, 1, 1, 1]
+    assert bench.launches_per_step(32, tile, 8) == 32 * 4 + 1
