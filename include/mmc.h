@@ -357,8 +357,12 @@ int mmc_batch_launch_shape(mmc_batch* b, int out[10]);
  * (src/main.cu:275-286). */
 int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int* candidates);
 /* Sets the launch shape (the ten values of mmc_batch_launch_shape), e.g. one
- * an earlier autotune chose.  Values outside the ranges the autotuner tries,
- * or a row-kernel band that does not fit this batch, are rejected.  Results do
+ * an earlier autotune chose.  Accepted: 1-16 rows per x-pass CTA (a power of
+ * two) with 128 or 256 threads, 1-64 kx columns per y- and z-pass tile (powers
+ * of two dividing the column-pass thread count, 32-512 threads), tiles whose
+ * shared memory fits 220 KB in the chosen column-pass form, a row-kernel band
+ * this batch offers, a Metropolis form the lattice qualifies for, 0/1 for the
+ * two transform flags and 1-4 streams; anything else is rejected.  Results do
  * not depend on the shape.  No counterpart in the reference. */
 int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]);
 
