@@ -931,78 +931,86 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
   h += blockIdx.z * 3 * n;
   acc += blockIdx.z;
   const int nseg = g.nx >> 2;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  // two segments per thread, a grid-stride apart: the coefficients and the
+  // set-up are shared by both, and the second segment's loads overlap the
+  // first one's work (measured 4 us faster per batched sweep than one segment)
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tstride = gridDim.x * blockDim.x;
   unsigned int mine = 0;
-  if (t < nseg * g.ny * g.nz) {
-    const int row = t / nseg, s = t - row * nseg;  // nseg is a power of two for the usual sizes; cheap either way
-    int z = 0, y = row;
-    if constexpr (Z3) {
-      z = g.dny.div(row);
-      y = row - z * g.ny;
-    }
-    const int x0 = 4 * s;
-    const long long rowb = (long long)row * g.nx;
-    const long long plane = (long long)g.nx * g.ny;
-    // neighbour rows: wrapped on a periodic axis, missing at an open edge or
-    // when the axis has length 1
-    int yu = y + 1, yd = y - 1;
-    bool hu = true, hd = true;
-    if (yu >= g.ny) { if (g.per[1]) yu -= g.ny; else hu = false; }
-    if (yd < 0) { if (g.per[1]) yd += g.ny; else hd = false; }
-    if (g.ny == 1) hu = hd = false;
-    int zu = z + 1, zd = z - 1;
-    bool hzu = Z3, hzd = Z3;
-    if constexpr (Z3) {
-      if (zu >= g.nz) { if (g.per[2]) zu -= g.nz; else hzu = false; }
-      if (zd < 0) { if (g.per[2]) zd += g.nz; else hzd = false; }
-    }
-    // side cells
-    int xl = x0 - 1, xr = x0 + 4;
-    bool hl = true, hr = true;
-    if (xl < 0) { if (g.per[0]) xl += g.nx; else hl = false; }
-    if (xr >= g.nx) { if (g.per[0]) xr -= g.nx; else hr = false; }
-    if constexpr (ALLB) hu = hd = hl = hr = true;
-    // this colour's cells sit at offsets p0 and p0 + 2 (x0 is even), so only
-    // one side cell is a neighbour: the left one for p0 = 0, the right one
-    // for p0 = 1
-    const int p0 = (color + y + z) & 1;
-    const long long zbase = (long long)z * plane;
-    Vec4<T> own[3], up[3], dn[3], zup[3], zdn[3];
-    T lft[3], rgt[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const T* base = m + k * n;
-      own[k] = ld4<T>(base + rowb + x0);
-      up[k] = hu ? ld4<T>(base + zbase + (long long)yu * g.nx + x0) : own[k];
-      dn[k] = hd ? ld4<T>(base + zbase + (long long)yd * g.nx + x0) : own[k];
+  for (int u = 0; u < 2; ++u) {
+    const int t = t0 + u * tstride;
+    if (t < nseg * g.ny * g.nz) {
+      const int row = t / nseg, s = t - row * nseg;  // nseg is a power of two for the usual sizes; cheap either way
+      int z = 0, y = row;
       if constexpr (Z3) {
-        zup[k] = hzu ? ld4<T>(base + (long long)zu * plane + (long long)y * g.nx + x0) : own[k];
-        zdn[k] = hzd ? ld4<T>(base + (long long)zd * plane + (long long)y * g.nx + x0) : own[k];
-      } else {
-        zup[k] = zdn[k] = own[k];
+        z = g.dny.div(row);
+        y = row - z * g.ny;
       }
-      lft[k] = (hl && p0 == 0) ? base[rowb + xl] : (T)0;
-      rgt[k] = (hr && p0 == 1) ? base[rowb + xr] : (T)0;
-    }
-    Vec4<T> hh[3];
-    const bool dm = c.cd != (T)0;
+      const int x0 = 4 * s;
+      const long long rowb = (long long)row * g.nx;
+      const long long plane = (long long)g.nx * g.ny;
+      // neighbour rows: wrapped on a periodic axis, missing at an open edge or
+      // when the axis has length 1
+      int yu = y + 1, yd = y - 1;
+      bool hu = true, hd = true;
+      if (yu >= g.ny) { if (g.per[1]) yu -= g.ny; else hu = false; }
+      if (yd < 0) { if (g.per[1]) yd += g.ny; else hd = false; }
+      if (g.ny == 1) hu = hd = false;
+      int zu = z + 1, zd = z - 1;
+      bool hzu = Z3, hzd = Z3;
+      if constexpr (Z3) {
+        if (zu >= g.nz) { if (g.per[2]) zu -= g.nz; else hzu = false; }
+        if (zd < 0) { if (g.per[2]) zd += g.nz; else hzd = false; }
+      }
+      // side cells
+      int xl = x0 - 1, xr = x0 + 4;
+      bool hl = true, hr = true;
+      if (xl < 0) { if (g.per[0]) xl += g.nx; else hl = false; }
+      if (xr >= g.nx) { if (g.per[0]) xr -= g.nx; else hr = false; }
+      if constexpr (ALLB) hu = hd = hl = hr = true;
+      // this colour's cells sit at offsets p0 and p0 + 2 (x0 is even), so only
+      // one side cell is a neighbour: the left one for p0 = 0, the right one
+      // for p0 = 1
+      const int p0 = (color + y + z) & 1;
+      const long long zbase = (long long)z * plane;
+      Vec4<T> own[3], up[3], dn[3], zup[3], zdn[3];
+      T lft[3], rgt[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      if (dm) hh[k] = ld4<T>(h + k * n + rowb + x0);
-      else hh[k].v[0] = hh[k].v[1] = hh[k].v[2] = hh[k].v[3] = (T)0;
-    }
-    // the offsets are compile-time inside quad_cells so the vectors stay in
-    // registers
-    bool changed;
-    if (p0 == 0)
-      changed = quad_cells<T, 0, ALLB, Z3>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0),
-                                           ctr->stage, ctr->sweep, mine, zdn, zup, hzd, hzu);
-    else
-      changed = quad_cells<T, 1, ALLB, Z3>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0),
-                                           ctr->stage, ctr->sweep, mine, zdn, zup, hzd, hzu);
-    if (changed) {
+      for (int k = 0; k < 3; ++k) {
+        const T* base = m + k * n;
+        own[k] = ld4<T>(base + rowb + x0);
+        up[k] = hu ? ld4<T>(base + zbase + (long long)yu * g.nx + x0) : own[k];
+        dn[k] = hd ? ld4<T>(base + zbase + (long long)yd * g.nx + x0) : own[k];
+        if constexpr (Z3) {
+          zup[k] = hzu ? ld4<T>(base + (long long)zu * plane + (long long)y * g.nx + x0) : own[k];
+          zdn[k] = hzd ? ld4<T>(base + (long long)zd * plane + (long long)y * g.nx + x0) : own[k];
+        } else {
+          zup[k] = zdn[k] = own[k];
+        }
+        lft[k] = (hl && p0 == 0) ? base[rowb + xl] : (T)0;
+        rgt[k] = (hr && p0 == 1) ? base[rowb + xr] : (T)0;
+      }
+      Vec4<T> hh[3];
+      const bool dm = c.cd != (T)0;
 #pragma unroll
-      for (int k = 0; k < 3; ++k) st4<T>(m + k * n + rowb + x0, own[k]);
+      for (int k = 0; k < 3; ++k) {
+        if (dm) hh[k] = ld4<T>(h + k * n + rowb + x0);
+        else hh[k].v[0] = hh[k].v[1] = hh[k].v[2] = hh[k].v[3] = (T)0;
+      }
+      // the offsets are compile-time inside quad_cells so the vectors stay in
+      // registers
+      bool changed;
+      if (p0 == 0)
+        changed = quad_cells<T, 0, ALLB, Z3>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0),
+                                             ctr->stage, ctr->sweep, mine, zdn, zup, hzd, hzu);
+      else
+        changed = quad_cells<T, 1, ALLB, Z3>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0),
+                                             ctr->stage, ctr->sweep, mine, zdn, zup, hzd, hzu);
+      if (changed) {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) st4<T>(m + k * n + rowb + x0, own[k]);
+      }
     }
   }
   unsigned int v = mine;
@@ -1704,8 +1712,8 @@ cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const S
     // 128-thread CTAs: the same warps per SM as 256 (the registers limit
     // them), in finer pieces, measured 2 us faster per batched sweep
     const int qthreads = 128;
-    const long long total = (long long)g.ny * g.nz * (g.nx >> 2);
-    dim3 grid((unsigned)((total + qthreads - 1) / qthreads), 1, nrep);
+    const long long total = (long long)g.ny * g.nz * (g.nx >> 2);  // segments, two per thread
+    dim3 grid((unsigned)((total + 2 * qthreads - 1) / (2 * qthreads)), 1, nrep);
     auto kern = g.nz > 1 ? (mc_all_bonds(g) ? k_mc_quad<T, true, true> : k_mc_quad<T, false, true>)
                          : (mc_all_bonds(g) ? k_mc_quad<T, true, false> : k_mc_quad<T, false, false>);
     return launch_pdl(kern, grid, dim3(qthreads), 0, st, g, c, m, h, ctr, color, acc);
