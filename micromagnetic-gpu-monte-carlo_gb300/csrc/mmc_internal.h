@@ -58,20 +58,25 @@ struct FftPlan {
   const float2* tw32;
 };
 
-// Lattice geometry.  Cell i = x + nx*(y + ny*z).  The padded grid (nxp, nyp,
-// nzp) follows src/main.cu:254-263 of the reference.  The spectrum keeps the
+// Lattice geometry.  Cell i = x + nx*(y + ny*z).  The tensor grid (txp, typ,
+// tzp) follows src/main.cu:254-263 of the reference (open axis n -> 2n - 1,
+// periodic n); the transform grid (nxp, nyp, nzp) equals it except that an
+// open axis of 2n - 1 > 16 is padded further to the next power of two up to
+// 1024, where the warp-level transforms apply.  The spectrum keeps the
 // kx half-axis: hx = nxp/2 + 1 columns stored with an even row pitch hxp (so
 // that pairs of FP32 columns are 16-byte aligned), layout [comp][kz][ky][kx],
 // nspec = hxp*nyp*nzp.  Pad columns hold zeros.
 struct Geom {
   int nx, ny, nz;
-  int nxp, nyp, nzp;
+  int nxp, nyp, nzp;  // the transform grid (the tensor grid, open axes possibly padded further)
+  int txp, typ, tzp;  // the tensor grid: the reference's padded dims
   int hx;
   int hxp;
   int per[3];      // periodic neighbours on this axis (pbc != 0)
   int ncolors;     // 2, or 3 when a periodic axis has odd length
   long long n;     // nx*ny*nz
   long long np;    // nxp*nyp*nzp
+  long long tnp;   // txp*typ*tzp
   long long nspec; // hxp*nyp*nzp
   FastDiv dnx, dny, dhx, dhxc;  // nx, ny, hx, (nx + 1) / 2
 };
@@ -207,6 +212,10 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
 cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz,
                           double pi, double* k6, int px0, int px1, int finalize, cudaStream_t st,
                           double far_r2 = 0.0);
+// The tensor on the tensor grid -> the transform grid: offsets |o| <= n - 1
+// copied, the offsets an open axis gains by the extra padding set to 0 (the
+// convolution of n cells never reaches them).
+cudaError_t launch_tensor_rewrap(const Geom& g, const double* k6t, double* k6f, cudaStream_t st);
 cudaError_t launch_tensor_fft(const Geom& g, const FftPlan& px, const FftPlan& py, const FftPlan& pz,
                               const DemagTuning& tun, const double* k6, double2* spec64, cudaStream_t st);
 // Advances the sweep counter of `count` (<= 32) consecutive SweepCounters.

@@ -138,8 +138,37 @@ __global__ void __launch_bounds__(128) k_newell(int nxp, int nyp, int nzp, doubl
 cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz, double pi,
                           double* k6, int px0, int px1, int finalize, cudaStream_t st, double far_r2) {
   const int threads = 128;
-  k_newell<<<(unsigned)((g.np + threads - 1) / threads), threads, 0, st>>>(
-      g.nxp, g.nyp, g.nzp, dx, dy, dz, Px, Py, Pz, px0, px1, finalize, pi, far_r2, k6, g.np);
+  k_newell<<<(unsigned)((g.tnp + threads - 1) / threads), threads, 0, st>>>(
+      g.txp, g.typ, g.tzp, dx, dy, dz, Px, Py, Pz, px0, px1, finalize, pi, far_r2, k6, g.tnp);
+  return cudaGetLastError();
+}
+
+namespace {
+// Index on the tensor grid (extent t) of transform-grid index j (extent f) of
+// an axis with n cells, or -1 where the transform grid holds no offset of the
+// tensor.
+__device__ __forceinline__ int rewrap_index(int j, int f, int t, int n) {
+  if (f == t || j <= n - 1) return j;
+  if (j >= f - (n - 1)) return j - f + t;
+  return -1;
+}
+
+__global__ void k_tensor_rewrap(const double* __restrict__ k6t, long long tnp, int tx, int ty, int tz, int nx,
+                                int ny, int nz, double* __restrict__ k6f, int fx, int fy, int fz, long long fnp) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= fnp) return;
+  const int jx = (int)(i % fx), jy = (int)((i / fx) % fy), jz = (int)(i / ((long long)fx * fy));
+  const int ix = rewrap_index(jx, fx, tx, nx), iy = rewrap_index(jy, fy, ty, ny), iz = rewrap_index(jz, fz, tz, nz);
+  const bool ok = ix >= 0 && iy >= 0 && iz >= 0;
+  const long long src = ok ? ix + (long long)tx * (iy + (long long)ty * iz) : 0;
+  for (int c = 0; c < 6; ++c) k6f[c * fnp + i] = ok ? k6t[c * tnp + src] : 0.0;
+}
+}  // namespace
+
+cudaError_t launch_tensor_rewrap(const Geom& g, const double* k6t, double* k6f, cudaStream_t st) {
+  const int threads = 256;
+  k_tensor_rewrap<<<(unsigned)((g.np + threads - 1) / threads), threads, 0, st>>>(
+      k6t, g.tnp, g.txp, g.typ, g.tzp, g.nx, g.ny, g.nz, k6f, g.nxp, g.nyp, g.nzp, g.np);
   return cudaGetLastError();
 }
 

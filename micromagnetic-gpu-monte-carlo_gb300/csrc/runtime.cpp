@@ -613,7 +613,7 @@ double far_r2(const mmc_config& c) {
 
 std::string cache_name(const mmc_handle* h) {
   char b[256];
-  std::snprintf(b, sizeof b, "cache_%d_%d_%d-%g_%g_%g-%d_%d_%d", h->g.nxp, h->g.nyp, h->g.nzp, h->cfg.dx,
+  std::snprintf(b, sizeof b, "cache_%d_%d_%d-%g_%g_%g-%d_%d_%d", h->g.txp, h->g.typ, h->g.tzp, h->cfg.dx,
                 h->cfg.dy, h->cfg.dz, h->cfg.pbc_x, h->cfg.pbc_y, h->cfg.pbc_z);
   std::string name = b;
   // a tensor with far-field terms is not the reference's: keep it apart
@@ -637,28 +637,28 @@ bool cache_load(mmc_handle* h, const std::string& path) {
   std::ifstream in(path, std::ios::binary);
   if (!in) return false;
   const Geom& g = h->g;
-  std::vector<double> raw(6 * (size_t)g.np);
+  std::vector<double> raw(6 * (size_t)g.tnp);
   in.read(reinterpret_cast<char*>(raw.data()), (std::streamsize)(raw.size() * sizeof(double)));
   if (!in || in.gcount() != (std::streamsize)(raw.size() * sizeof(double))) return false;
-  h->tensor.assign(6 * (size_t)g.np, 0.0);
+  h->tensor.assign(6 * (size_t)g.tnp, 0.0);
   for (int c = 0; c < 6; ++c)
-    for (int x = 0; x < g.nxp; ++x)
-      for (int y = 0; y < g.nyp; ++y)
-        for (int z = 0; z < g.nzp; ++z)
-          h->tensor[c * g.np + x + (long long)g.nxp * (y + (long long)g.nyp * z)] =
-              raw[c * g.np + z + (long long)g.nzp * (y + (long long)g.nyp * x)];
+    for (int x = 0; x < g.txp; ++x)
+      for (int y = 0; y < g.typ; ++y)
+        for (int z = 0; z < g.tzp; ++z)
+          h->tensor[c * g.tnp + x + (long long)g.txp * (y + (long long)g.typ * z)] =
+              raw[c * g.tnp + z + (long long)g.tzp * (y + (long long)g.typ * x)];
   return true;
 }
 
 bool cache_save(const mmc_handle* h, const std::string& path) {
   const Geom& g = h->g;
-  std::vector<double> raw(6 * (size_t)g.np);
+  std::vector<double> raw(6 * (size_t)g.tnp);
   for (int c = 0; c < 6; ++c)
-    for (int x = 0; x < g.nxp; ++x)
-      for (int y = 0; y < g.nyp; ++y)
-        for (int z = 0; z < g.nzp; ++z)
-          raw[c * g.np + z + (long long)g.nzp * (y + (long long)g.nyp * x)] =
-              h->tensor[c * g.np + x + (long long)g.nxp * (y + (long long)g.nyp * z)];
+    for (int x = 0; x < g.txp; ++x)
+      for (int y = 0; y < g.typ; ++y)
+        for (int z = 0; z < g.tzp; ++z)
+          raw[c * g.tnp + z + (long long)g.tzp * (y + (long long)g.typ * x)] =
+              h->tensor[c * g.tnp + x + (long long)g.txp * (y + (long long)g.typ * z)];
   std::ofstream out(path, std::ios::binary | std::ios::trunc);
   if (!out) return false;
   out.write(reinterpret_cast<const char*>(raw.data()), (std::streamsize)(raw.size() * sizeof(double)));
@@ -672,13 +672,14 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
   std::string dir = cache_dir ? cache_dir : "";
   std::string path = dir.empty() ? "" : join(dir, cache_name(h));
   bool loaded = !path.empty() && cache_load(h, path);
-  double* k6 = nullptr;
+  double* k6 = nullptr;   // the tensor grid
+  double* k6f = nullptr;  // the transform grid, when it differs
   double2* spec64 = nullptr;
-  CU(cudaMalloc(&k6, 6 * (size_t)g.np * sizeof(double)));
+  CU(cudaMalloc(&k6, 6 * (size_t)g.tnp * sizeof(double)));
   int status = MMC_OK;
   do {
     if (loaded) {
-      cudaError_t e = cudaMemcpy(k6, h->tensor.data(), 6 * (size_t)g.np * sizeof(double), cudaMemcpyHostToDevice);
+      cudaError_t e = cudaMemcpy(k6, h->tensor.data(), 6 * (size_t)g.tnp * sizeof(double), cudaMemcpyHostToDevice);
       if (e != cudaSuccess) {
         status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
         break;
@@ -687,7 +688,7 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
       const int Px = std::max(c.pbc_x, 0), Py = std::max(c.pbc_y, 0), Pz = std::max(c.pbc_z, 0);
       // Each launch adds a slab of x images to every point's running sum; about
       // 1e9 f/g evaluations per launch keeps launches near a second.
-      const double per_px = (double)g.np * (2.0 * Py + 1) * (2.0 * Pz + 1) * 384.0;
+      const double per_px = (double)g.tnp * (2.0 * Py + 1) * (2.0 * Pz + 1) * 384.0;
       const int slab = std::max(1, (int)(1e9 / per_px));
       for (int px0 = -Px; px0 <= Px; px0 += slab) {
         if (h->stop.load()) {
@@ -704,16 +705,25 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
         }
       }
       if (status != MMC_OK) break;
-      h->tensor.assign(6 * (size_t)g.np, 0.0);
-      cudaError_t e = cudaMemcpy(h->tensor.data(), k6, 6 * (size_t)g.np * sizeof(double), cudaMemcpyDeviceToHost);
+      h->tensor.assign(6 * (size_t)g.tnp, 0.0);
+      cudaError_t e = cudaMemcpy(h->tensor.data(), k6, 6 * (size_t)g.tnp * sizeof(double), cudaMemcpyDeviceToHost);
       if (e != cudaSuccess) {
         status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
         break;
       }
       if (!path.empty() && dir_exists(dir)) cache_save(h, path);
     }
-    for (int q = 0; q < 6; ++q) h->k0[q] = h->tensor[(size_t)q * g.np];
-    cudaError_t e = cudaMalloc(&spec64, 6 * (size_t)g.nspec * sizeof(double2));
+    for (int q = 0; q < 6; ++q) h->k0[q] = h->tensor[(size_t)q * g.tnp];
+    cudaError_t e = cudaSuccess;
+    if (g.np != g.tnp) {  // the tensor on the transform grid
+      e = cudaMalloc(&k6f, 6 * (size_t)g.np * sizeof(double));
+      if (e == cudaSuccess) e = launch_tensor_rewrap(g, k6, k6f, h->st);
+      if (e != cudaSuccess) {
+        status = fail(MMC_ERR_CUDA, std::string("tensor re-wrap: ") + cudaGetErrorString(e));
+        break;
+      }
+    }
+    e = cudaMalloc(&spec64, 6 * (size_t)g.nspec * sizeof(double2));
     if (e != cudaSuccess) {
       status = fail(MMC_ERR_OOM, "tensor spectrum allocation");
       break;
@@ -728,7 +738,7 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
       tt.col_tx_z /= 2;
     tt.col_tx = std::min(tt.col_tx, tt.col_tx_z);
     tt.col_tx_z = tt.col_tx;
-    e = launch_tensor_fft(g, h->px.p, h->py.p, h->pz.p, tt, k6, spec64, h->st);
+    e = launch_tensor_fft(g, h->px.p, h->py.p, h->pz.p, tt, k6f ? k6f : k6, spec64, h->st);
     if (e == cudaSuccess) {
       if (h->prec == 32) e = launch_khat_store<float>(6 * g.nspec, spec64, h->khat, h->st);
       else e = launch_khat_store<double>(6 * g.nspec, spec64, h->khat, h->st);
@@ -741,6 +751,7 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
     h->demag_built = true;
   } while (0);
   if (spec64) cudaFree(spec64);
+  if (k6f) cudaFree(k6f);
   if (k6) cudaFree(k6);
   return status;
 }
@@ -941,10 +952,22 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   g.nx = cfg->nx;
   g.ny = cfg->ny;
   g.nz = cfg->nz;
-  // src/main.cu:254-263
-  g.nxp = cfg->pbc_x == 0 ? 2 * cfg->nx - 1 : cfg->nx;
-  g.nyp = cfg->pbc_y == 0 ? 2 * cfg->ny - 1 : cfg->ny;
-  g.nzp = cfg->pbc_z == 0 ? 2 * cfg->nz - 1 : cfg->nz;
+  // the tensor grid, src/main.cu:254-263
+  g.txp = cfg->pbc_x == 0 ? 2 * cfg->nx - 1 : cfg->nx;
+  g.typ = cfg->pbc_y == 0 ? 2 * cfg->ny - 1 : cfg->ny;
+  g.tzp = cfg->pbc_z == 0 ? 2 * cfg->nz - 1 : cfg->nz;
+  // the transform grid: an open axis of 2n - 1 > 16 is padded on to the next
+  // power of two when that has a warp-level transform (32 .. 1024); lines of
+  // up to 16 take the per-thread transforms as they are
+  auto fft_len = [](int t, bool open) {
+    if (!open || t <= 16) return t;
+    int p = 1;
+    while (p < t) p *= 2;
+    return p <= 1024 ? p : t;
+  };
+  g.nxp = fft_len(g.txp, cfg->pbc_x == 0);
+  g.nyp = fft_len(g.typ, cfg->pbc_y == 0);
+  g.nzp = fft_len(g.tzp, cfg->pbc_z == 0);
   g.hx = g.nxp / 2 + 1;
   g.hxp = g.hx + (g.hx & 1);
   g.per[0] = cfg->pbc_x != 0;
@@ -956,6 +979,7 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
     if (g.per[a] && (dims[a] & 1) && dims[a] > 1) g.ncolors = 3;
   g.n = (long long)g.nx * g.ny * g.nz;
   g.np = (long long)g.nxp * g.nyp * g.nzp;
+  g.tnp = (long long)g.txp * g.typ * g.tzp;
   g.nspec = (long long)g.hxp * g.nyp * g.nzp;
   g.dnx = FastDiv((uint32_t)g.nx);
   g.dny = FastDiv((uint32_t)g.ny);
