@@ -480,3 +480,28 @@ def test_wide_transforms_match_oracle(M, O, geom, prec):
         acc = O.sweeps(c, k, 150.0, 2, 0, 20, m, demag_mode=1)
         assert acc_gpu == acc
         assert np.array_equal(m_gpu, m)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_open_axis_with_large_prime_padding(M, O, prec):
+    """An open x axis of 40 cells: the reference's padded length 79 is a prime
+    above the mixed-radix transforms' largest radix, so the transform grid is
+    padded on to 128 and the tensor re-wrapped onto it.  Field against the
+    oracle's direct sum on the 79-cell tensor grid; FP64 decisions bit for bit."""
+    c = cfg(M, nx=40, ny=8, nz=1, pbc_x=0, pbc_y=1, precision=prec)
+    assert M.padded_dims(c) == (79, 8, 1)
+    with M.Lattice(c) as lat:
+        lat.build_demag()
+        m0 = lat.get_m()
+        lat.compute_demag()
+        H = lat.field(M.TERM_DEMAG)
+        k = lat.tensor()
+        lat.run_sweeps(150.0, 1, 0, 30)
+        m_gpu = lat.get_m()
+        acc_gpu = lat.energy().accepted
+    assert rel(H, c.ms * O.demag_direct(c, k, m0)) <= (FP64_REL if prec == 64 else FP32_REL)
+    if prec == 64:
+        m = m0.copy()
+        acc = O.sweeps(c, k, 150.0, 1, 0, 30, m, demag_mode=1)
+        assert acc_gpu == acc
+        assert np.array_equal(m_gpu, m)
