@@ -132,7 +132,10 @@ int mmc_config_load_ini(const char* path, mmc_config* cfg);
  * "key: value" echo into buf (NUL-terminated, truncated to len). */
 int mmc_config_format(const mmc_config* cfg, char* buf, size_t len);
 
-/* Padded FFT dimensions (src/main.cu:254-263): n -> 2n-1 on open axes. */
+/* Padded dimensions of the tensor grid (src/main.cu:254-263): n -> 2n-1 on
+ * open axes, n on periodic ones -- the grid of mmc_get_tensor and of the
+ * tensor cache.  The transforms may pad an open axis further (to the next
+ * power of two up to 1024); that grid is internal. */
 int mmc_padded_dims(const mmc_config* cfg, int out[3]);
 
 /* Allocates the device state for one lattice on CUDA device `device`
