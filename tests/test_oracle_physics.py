@@ -206,3 +206,52 @@ def test_even_periodic_kernel_asymmetry_is_the_far_image(M, O):
     assert vals[0] > vals[1] > vals[2] > 0
     # dipole scaling r^-3 with r = (P + 1/2) n
     assert 0.3 < vals[0] / vals[1] / ((2.5 / 1.5) ** 3) < 3
+
+
+def _rewrap_axis(f, t, n):
+    """Tensor-grid index of each transform-grid index of an axis (-1: none):
+    the rule the library applies when it pads an open axis past 2n - 1."""
+    out = np.full(f, -1)
+    for j in range(f):
+        if f == t or j <= n - 1:
+            out[j] = j
+        elif j >= f - (n - 1):
+            out[j] = j - f + t
+    return out
+
+
+@pytest.mark.parametrize("kw", [dict(nx=6, ny=5, nz=1, pbc_x=0, pbc_y=1), dict(nx=5, ny=4, nz=3, pbc_x=0, pbc_y=0),
+                                dict(nx=7, ny=3, nz=1, pbc_x=0, pbc_y=-1)])
+def test_padded_transform_grid_is_the_same_convolution(M, O, kw):
+    """The transform grid of an open axis may be longer than the reference's
+    2n - 1 (the next power of two): the tensor re-wrapped onto it (offsets
+    |o| <= n - 1 kept, the rest 0) gives, by circular convolution, the direct
+    sum of the reference's tensor."""
+    cfg = cfg_small(M, **kw)
+    k = O.tensor(cfg)
+    t = O.padded_dims(cfg)
+    n = (cfg.nx, cfg.ny, cfg.nz)
+    f = tuple(1 << (ti - 1).bit_length() if (p == 0 and ti > 1) else ti
+              for ti, p in zip(t, (cfg.pbc_x, cfg.pbc_y, cfg.pbc_z)))
+    maps = [_rewrap_axis(fi, ti, ni) for fi, ti, ni in zip(f, t, n)]
+    kt = k.reshape(6, t[2], t[1], t[0])  # x fastest
+    kf = np.zeros((6, f[2], f[1], f[0]))
+    for jz in range(f[2]):
+        for jy in range(f[1]):
+            for jx in range(f[0]):
+                iz, iy, ix = maps[2][jz], maps[1][jy], maps[0][jx]
+                if min(ix, iy, iz) >= 0:
+                    kf[:, jz, jy, jx] = kt[:, iz, iy, ix]
+    m = O.init_random(cfg, 3)
+    mg = np.zeros((3, f[2], f[1], f[0]))
+    mg[:, :n[2], :n[1], :n[0]] = m.reshape(3, n[2], n[1], n[0])
+    K = np.fft.fftn(kf, axes=(1, 2, 3))
+    Mh = np.fft.fftn(mg, axes=(1, 2, 3))
+    ab = {(0, 0): 0, (0, 1): 1, (0, 2): 2, (1, 1): 3, (1, 2): 4, (2, 2): 5}
+    h = np.zeros_like(mg)
+    for a in range(3):
+        acc = sum(K[ab[tuple(sorted((a, b)))]] * Mh[b] for b in range(3))
+        h[a] = np.fft.ifftn(acc, axes=(0, 1, 2)).real
+    got = h[:, :n[2], :n[1], :n[0]].reshape(3, -1)
+    want = O.demag_direct(cfg, k, m)
+    np.testing.assert_allclose(got, want, rtol=0, atol=1e-13)
