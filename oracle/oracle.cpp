@@ -37,8 +37,55 @@
 #endif
 
 #include "../include/mmc.h"
+
+#ifdef ORACLE_LIBM
+// Independent build (liboracle_libm.so): the C library's elementary functions
+// and a Philox4x32-10 written here from Salmon, Moraes, Dror, Shaw, "Parallel
+// random numbers: as easy as 1, 2, 3" (SC'11), so that nothing of the
+// product's csrc/mmc_math.h enters.  Its tensor equals the reference's own
+// ktensorCPU bit for bit (same libm, same expression and loop order); the
+// default build is checked against it to the rounding of one ulp per
+// elementary function.  The far-field tensor form is not offered here.
+namespace om {
+inline double dsqrt(double x) { return std::sqrt(x); }
+inline double asinh(double x) { return std::asinh(x); }
+inline double atan(double x) { return std::atan(x); }
+inline double exp(double x) { return std::exp(x); }
+inline double log(double x) { return std::log(x); }
+inline void sincospi(double t, double* s, double* c) {
+  const double a = 3.14159265358979323846 * t;
+  *s = std::sin(a);
+  *c = std::cos(a);
+}
+struct u32x4 {
+  uint32_t x, y, z, w;
+};
+// Counter word 3 of the keying contract: sweeps use 0, the initial state 1.
+enum : uint32_t { STREAM_SWEEP = 0u, STREAM_INIT = 1u };
+inline u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+  for (int round = 0; round < 10; ++round) {
+    if (round > 0) {
+      k0 += 0x9E3779B9u;  // Weyl increments of the key
+      k1 += 0xBB67AE85u;
+    }
+    const uint64_t a = (uint64_t)0xD2511F53u * (uint64_t)c.x;
+    const uint64_t b = (uint64_t)0xCD9E8D57u * (uint64_t)c.z;
+    u32x4 n;
+    n.x = (uint32_t)(b >> 32) ^ c.y ^ k0;
+    n.y = (uint32_t)b;
+    n.z = (uint32_t)(a >> 32) ^ c.w ^ k1;
+    n.w = (uint32_t)a;
+    c = n;
+  }
+  return c;
+}
+inline double u01_f64(uint32_t r) { return ((double)r + 0.5) * 0x1p-32; }
+}  // namespace om
+#else
 #include "../micromagnetic-gpu-monte-carlo_gb300/csrc/mmc_math.h"
 #include "../micromagnetic-gpu-monte-carlo_gb300/csrc/newell_far.h"
+namespace om = mmcm;
+#endif
 
 namespace {
 
@@ -78,10 +125,10 @@ double newell_f(double x, double y, double z) {
   x = ABSV(x);
   y = ABSV(y);
   z = ABSV(z);
-  double R = mmcm::dsqrt(x * x + y * y + z * z);
-  double t1 = y / 2.0 * (z * z - x * x) * mmcm::asinh(y / (mmcm::dsqrt(x * x + z * z) + EPS));
-  double t2 = z / 2.0 * (y * y - x * x) * mmcm::asinh(z / (mmcm::dsqrt(x * x + y * y) + EPS));
-  double t3 = x * y * z * mmcm::atan(y * z / (x * R + EPS));
+  double R = om::dsqrt(x * x + y * y + z * z);
+  double t1 = y / 2.0 * (z * z - x * x) * om::asinh(y / (om::dsqrt(x * x + z * z) + EPS));
+  double t2 = z / 2.0 * (y * y - x * x) * om::asinh(z / (om::dsqrt(x * x + y * y) + EPS));
+  double t3 = x * y * z * om::atan(y * z / (x * R + EPS));
   double t4 = 1.0 / 6.0 * (2 * x * x - y * y - z * z) * R;
   return t1 + t2 - t3 + t4;
 }
@@ -90,13 +137,13 @@ double newell_f(double x, double y, double z) {
 double newell_g(double x, double y, double z) {
   const double EPS = 1e-200;
   z = ABSV(z);
-  double R = mmcm::dsqrt(x * x + y * y + z * z);
-  double t1 = x * y * z * mmcm::asinh(z / (mmcm::dsqrt(x * x + y * y) + EPS));
-  double t2 = y / 6.0 * (3.0 * z * z - y * y) * mmcm::asinh(x / (mmcm::dsqrt(y * y + z * z) + EPS));
-  double t3 = x / 6.0 * (3.0 * z * z - x * x) * mmcm::asinh(y / (mmcm::dsqrt(x * x + z * z) + EPS));
-  double t4 = z * z * z / 6.0 * mmcm::atan(x * y / (z * R + EPS));
-  double t5 = z * y * y / 2.0 * mmcm::atan(x * z / (y * R + EPS));
-  double t6 = z * x * x / 2.0 * mmcm::atan(y * z / (x * R + EPS));
+  double R = om::dsqrt(x * x + y * y + z * z);
+  double t1 = x * y * z * om::asinh(z / (om::dsqrt(x * x + y * y) + EPS));
+  double t2 = y / 6.0 * (3.0 * z * z - y * y) * om::asinh(x / (om::dsqrt(y * y + z * z) + EPS));
+  double t3 = x / 6.0 * (3.0 * z * z - x * x) * om::asinh(y / (om::dsqrt(x * x + z * z) + EPS));
+  double t4 = z * z * z / 6.0 * om::atan(x * y / (z * R + EPS));
+  double t5 = z * y * y / 2.0 * om::atan(x * z / (y * R + EPS));
+  double t6 = z * x * x / 2.0 * om::atan(y * z / (x * R + EPS));
   double t7 = x * y * R / 3.0;
   return t1 + t2 + t3 - t4 - t5 - t6 - t7;
 }
@@ -113,6 +160,7 @@ void newell_point(const Lat& L, double dx, double dy, double dz, double pi, int 
     for (int py = -L.P[1]; py <= L.P[1]; py++)
       for (int pz = -L.P[2]; pz <= L.P[2]; pz++) {
         int ix = idx_x + px * L.nxp, iy = idx_y + py * L.nyp, iz = idx_z + pz * L.nzp;
+#ifndef ORACLE_LIBM
         if (far_r2 > 0.0) {  // far-field form of this image's 64 terms (newell_far.h)
           const double X = ix * dx, Y = iy * dy, Z = iz * dz;
           if (X * X + Y * Y + Z * Z >= far_r2) {
@@ -127,6 +175,9 @@ void newell_point(const Lat& L, double dx, double dy, double dz, double pi, int 
             continue;
           }
         }
+#else
+        (void)far_r2;
+#endif
         for (int ikx = 0; ikx < 2; ikx++)
           for (int iky = 0; iky < 2; iky++)
             for (int ikz = 0; ikz < 2; ikz++)
@@ -250,6 +301,22 @@ void demag_fft_prepare(DemagFFT& D, const Lat& L, const double* k6) {
   }
 }
 
+// src/demag_cu.cu:68-116 (calHexchangeKernel): H^ = K^ . M^ / N for one
+// frequency, K^ symmetric (xx, xy, xz, yy, yz, zz); each complex product is
+// (a.x b.x - a.y b.y, a.x b.y + a.y b.x) and the three are summed left to right
+// before the division, as there.
+inline cd cmul(cd a, cd b) {
+  return cd(a.real() * b.real() - a.imag() * b.imag(), a.real() * b.imag() + a.imag() * b.real());
+}
+inline void demag_product(cd mx, cd my, cd mz, const cd k[6], double N, cd h[3]) {
+  const cd ax = cmul(mx, k[0]) + cmul(my, k[1]) + cmul(mz, k[2]);
+  const cd ay = cmul(mx, k[1]) + cmul(my, k[3]) + cmul(mz, k[4]);
+  const cd az = cmul(mx, k[2]) + cmul(my, k[4]) + cmul(mz, k[5]);
+  h[0] = cd(ax.real() / N, ax.imag() / N);
+  h[1] = cd(ay.real() / N, ay.imag() / N);
+  h[2] = cd(az.real() / N, az.imag() / N);
+}
+
 // h = K * m (circular convolution on the padded grid, cropped), via full complex FFTs.
 void demag_fft_apply(const DemagFFT& D, const double* m, double* h) {
   const Lat& L = D.L;
@@ -263,18 +330,15 @@ void demag_fft_apply(const DemagFFT& D, const double* m, double* h) {
           M[c][x + (long)L.nxp * (y + (long)L.nyp * z)] = m[c * n + x + (long)L.nx * (y + (long)L.ny * z)];
     fft3(M[c], L, -1);
   }
-  // src/demag_cu.cu:68-116: H^ = K^ . M^ / N (symmetric 3x3).
   const double N = (double)np;
 #pragma omp parallel for schedule(static)
   for (long i = 0; i < np; ++i) {
-    cd mx = M[0][i], my = M[1][i], mz = M[2][i];
-    cd xx = D.K[0][i], xy = D.K[1][i], xz = D.K[2][i], yy = D.K[3][i], yz = D.K[4][i], zz = D.K[5][i];
-    cd hx = (mx * xx + my * xy + mz * xz) / N;
-    cd hy = (mx * xy + my * yy + mz * yz) / N;
-    cd hz = (mx * xz + my * yz + mz * zz) / N;
-    M[0][i] = hx;
-    M[1][i] = hy;
-    M[2][i] = hz;
+    const cd k[6] = {D.K[0][i], D.K[1][i], D.K[2][i], D.K[3][i], D.K[4][i], D.K[5][i]};
+    cd h[3];
+    demag_product(M[0][i], M[1][i], M[2][i], k, N, h);
+    M[0][i] = h[0];
+    M[1][i] = h[1];
+    M[2][i] = h[2];
   }
   for (int c = 0; c < 3; ++c) {
     fft3(M[c], L, +1);
@@ -350,7 +414,12 @@ int orc_padded_dims(const mmc_config* c, int out[3]) {
 double orc_newell_f(double x, double y, double z) { return newell_f(x, y, z); }
 // Far-field form of the six 64-term sums of one image offset (newell_far.h).
 void orc_newell_far(double X, double Y, double Z, double dx, double dy, double dz, double out[6]) {
+#ifndef ORACLE_LIBM
   mmcm::newell_far_raw(X, Y, Z, dx, dy, dz, out);
+#else
+  (void)X, (void)Y, (void)Z, (void)dx, (void)dy, (void)dz;
+  for (int k = 0; k < 6; ++k) out[k] = std::nan("");
+#endif
 }
 // The exact six 64-term sums of one offset given in cells (before the -4 pi V division).
 void orc_newell_raw(int ix, int iy, int iz, double dx, double dy, double dz, double out[6]) {
@@ -372,28 +441,72 @@ void orc_math(int fn, const double* x, double* y, long n) {
   for (long i = 0; i < n; ++i) {
     double s, c;
     switch (fn) {
-      case 0: y[i] = mmcm::log(x[i]); break;
-      case 1: y[i] = mmcm::asinh(x[i]); break;
-      case 2: y[i] = mmcm::atan(x[i]); break;
-      case 3: y[i] = mmcm::exp(x[i]); break;
-      case 4: mmcm::sincospi(x[i], &s, &c); y[i] = s; break;
-      case 5: mmcm::sincospi(x[i], &s, &c); y[i] = c; break;
+      case 0: y[i] = om::log(x[i]); break;
+      case 1: y[i] = om::asinh(x[i]); break;
+      case 2: y[i] = om::atan(x[i]); break;
+      case 3: y[i] = om::exp(x[i]); break;
+      case 4: om::sincospi(x[i], &s, &c); y[i] = s; break;
+      case 5: om::sincospi(x[i], &s, &c); y[i] = c; break;
       default: y[i] = 0; break;
     }
   }
 }
 
 void orc_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
-  mmcm::u32x4 c = {ctr[0], ctr[1], ctr[2], ctr[3]};
-  mmcm::u32x4 r = mmcm::philox4x32_10(c, key[0], key[1]);
+  om::u32x4 c = {ctr[0], ctr[1], ctr[2], ctr[3]};
+  om::u32x4 r = om::philox4x32_10(c, key[0], key[1]);
   out[0] = r.x;
   out[1] = r.y;
   out[2] = r.z;
   out[3] = r.w;
 }
 
+// The frequency-domain product of demag_fft_apply on caller arrays: m3 holds
+// three spectra of np complex values (interleaved re, im), k6 six, h3 three.
+void orc_demag_product(long np, const double* m3, const double* k6, double* h3) {
+  const cd* M = reinterpret_cast<const cd*>(m3);
+  const cd* K = reinterpret_cast<const cd*>(k6);
+  cd* H = reinterpret_cast<cd*>(h3);
+  for (long i = 0; i < np; ++i) {
+    const cd k[6] = {K[i], K[np + i], K[2 * np + i], K[3 * np + i], K[4 * np + i], K[5 * np + i]};
+    cd h[3];
+    demag_product(M[i], M[np + i], M[2 * np + i], k, (double)np, h);
+    H[i] = h[0];
+    H[np + i] = h[1];
+    H[2 * np + i] = h[2];
+  }
+}
+
+// The tensor at selected points of the padded grid (flat index x + nxp (y +
+// nyp z)); out holds 6 blocks of `count` values.  The same per-point code as
+// orc_newell_tensor, for checks of large lattices on a few points.
+int orc_newell_points(const mmc_config* c, const long* idx, long count, double* out) {
+#ifdef ORACLE_LIBM
+  if (c->tensor_far_radius > 0) return -1;
+#endif
+  Lat L = lat_of(c);
+  double pi = pi_of(c);
+  double fr2 = 0.0;
+  if (c->tensor_far_radius > 0) {
+    const double d = std::max(c->dx, std::max(c->dy, c->dz)) * (double)c->tensor_far_radius;
+    fr2 = d * d;
+  }
+#pragma omp parallel for schedule(dynamic)
+  for (long j = 0; j < count; ++j) {
+    const long i = idx[j];
+    int x = (int)(i % L.nxp), y = (int)((i / L.nxp) % L.nyp), z = (int)(i / ((long)L.nxp * L.nyp));
+    double o[6];
+    newell_point(L, c->dx, c->dy, c->dz, pi, x, y, z, o, fr2);
+    for (int k = 0; k < 6; ++k) out[k * count + j] = o[k];
+  }
+  return 0;
+}
+
 // Full tensor, 6 blocks of nxp*nyp*nzp doubles (x fastest).
 int orc_newell_tensor(const mmc_config* c, double* k6) {
+#ifdef ORACLE_LIBM
+  if (c->tensor_far_radius > 0) return -1;  // the far-field form is not in the independent build
+#endif
   Lat L = lat_of(c);
   long np = L.np();
   double pi = pi_of(c);
@@ -418,13 +531,13 @@ void orc_init_random(const mmc_config* c, long long seed, double* m) {
   long n = L.n();
   uint32_t k0 = (uint32_t)((uint64_t)seed & 0xffffffffu), k1 = (uint32_t)((uint64_t)seed >> 32);
   for (long i = 0; i < n; ++i) {
-    mmcm::u32x4 ctr = {(uint32_t)i, 0u, 0u, mmcm::STREAM_INIT};
-    mmcm::u32x4 r = mmcm::philox4x32_10(ctr, k0, k1);
-    double z = 2.0 * mmcm::u01_f64(r.x) - 1.0;
+    om::u32x4 ctr = {(uint32_t)i, 0u, 0u, om::STREAM_INIT};
+    om::u32x4 r = om::philox4x32_10(ctr, k0, k1);
+    double z = 2.0 * om::u01_f64(r.x) - 1.0;
     double t = 1.0 - z * z;
     if (t < 0) t = 0;
-    double s = mmcm::dsqrt(t), sn, cs;
-    mmcm::sincospi(2.0 * mmcm::u01_f64(r.y), &sn, &cs);
+    double s = om::dsqrt(t), sn, cs;
+    om::sincospi(2.0 * om::u01_f64(r.y), &sn, &cs);
     m[i] = s * cs;
     m[n + i] = s * sn;
     m[2 * n + i] = z;
@@ -669,13 +782,13 @@ int orc_sweeps(const mmc_config* c, const double* k6, double T, long long stage,
           Fy = Fy + cd * (h[n + i] - sy);
           Fz = Fz + cd * (h[2 * n + i] - sz);
         }
-        mmcm::u32x4 ctr = {(uint32_t)i, sweep, (uint32_t)stage, mmcm::STREAM_SWEEP};
-        mmcm::u32x4 r = mmcm::philox4x32_10(ctr, key0, key1);
-        double pz = 2.0 * mmcm::u01_f64(r.x) - 1.0;
+        om::u32x4 ctr = {(uint32_t)i, sweep, (uint32_t)stage, om::STREAM_SWEEP};
+        om::u32x4 r = om::philox4x32_10(ctr, key0, key1);
+        double pz = 2.0 * om::u01_f64(r.x) - 1.0;
         double t = 1.0 - pz * pz;
         if (t < 0) t = 0;
-        double st = mmcm::dsqrt(t), sn, cs;
-        mmcm::sincospi(2.0 * mmcm::u01_f64(r.y), &sn, &cs);
+        double st = om::dsqrt(t), sn, cs;
+        om::sincospi(2.0 * om::u01_f64(r.y), &sn, &cs);
         double px = st * cs, py = st * sn;
         double ddx = px - ox, ddy = py - oy, ddz = pz - oz;
         double dE = -(ddx * Fx + ddy * Fy + ddz * Fz);
@@ -689,8 +802,8 @@ int orc_sweeps(const mmc_config* c, const double* k6, double T, long long stage,
                       oz * (k0[2] * ox + k0[4] * oy + k0[5] * oz);
           dE = dE - 0.5 * cd * (qn - qo);
         }
-        double u2 = mmcm::u01_f64(r.z);
-        if (dE <= 0.0 || u2 < mmcm::exp(-dE)) {
+        double u2 = om::u01_f64(r.z);
+        if (dE <= 0.0 || u2 < om::exp(-dE)) {
           mx[i] = px;
           my[i] = py;
           mz[i] = pz;

@@ -6,6 +6,7 @@ Arrays are numpy float64, SoA: m has shape (3, n), n = nx*ny*nz, x fastest.
 import ctypes
 import importlib.util
 import os
+import sys
 
 import numpy as np
 
@@ -24,6 +25,10 @@ def _load_module(name, path):
 _build = _load_module("oracle_build", os.path.join(HERE, "build.py"))
 
 _LIB = None
+# "shared": liboracle.so (the product's elementary functions, for bit-level
+# comparison with the GPU); "libm": liboracle_libm.so (see independent()).
+_VARIANT = "shared"
+_INDEP = None
 _dp = ctypes.POINTER(ctypes.c_double)
 _u32p = ctypes.POINTER(ctypes.c_uint32)
 
@@ -40,7 +45,7 @@ def lib():
     global _LIB
     if _LIB is not None:
         return _LIB
-    path = _build.build()
+    path = _build.build(variant=_VARIANT)
     L = ctypes.CDLL(path)
     C = ctypes.c_void_p  # pointer to mmc_config
     sig = {
@@ -62,6 +67,8 @@ def lib():
                                       ctypes.c_longlong, _dp, ctypes.POINTER(ctypes.c_ulonglong), ctypes.c_int,
                                       ctypes.c_int]),
         "orc_energy_total": (ctypes.c_double, [C, _dp, _dp]),
+        "orc_demag_product": (None, [ctypes.c_long, _dp, _dp, _dp]),
+        "orc_newell_points": (ctypes.c_int, [C, ctypes.POINTER(ctypes.c_long), ctypes.c_long, _dp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -69,6 +76,21 @@ def lib():
         fn.argtypes = args
     _LIB = L
     return L
+
+
+def independent():
+    """This API bound to liboracle_libm.so: the oracle built with the C
+    library's elementary functions and its own Philox, sharing no code with
+    the product (no far-field tensor form)."""
+    global _INDEP
+    if _VARIANT == "libm":
+        return sys.modules[__name__]
+    if _INDEP is None:
+        mod = _load_module("oracle_ctypes_libm", os.path.abspath(__file__))
+        mod._VARIANT = "libm"
+        sys.modules["oracle_ctypes_libm"] = mod
+        _INDEP = mod
+    return _INDEP
 
 
 def _c(cfg):
@@ -116,6 +138,25 @@ def tensor(cfg):
     k = np.zeros((6, nxp * nyp * nzp))
     lib().orc_newell_tensor(_c(cfg), _p(k))
     return k
+
+
+def tensor_points(cfg, idx):
+    """The tensor at flat padded-grid indices idx (x fastest): shape (6, len(idx))."""
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    out = np.zeros((6, idx.size))
+    rc = lib().orc_newell_points(_c(cfg), idx.ctypes.data_as(ctypes.POINTER(ctypes.c_long)), idx.size, _p(out))
+    assert rc == 0, rc
+    return out
+
+
+def demag_product(mhat, khat):
+    """H^ = K^ . M^ / N per frequency: mhat complex (3, np), khat complex (6, np)."""
+    m = np.ascontiguousarray(mhat, dtype=np.complex128)
+    k = np.ascontiguousarray(khat, dtype=np.complex128)
+    h = np.zeros_like(m)
+    np_ = m.shape[1]
+    lib().orc_demag_product(np_, m.ctypes.data_as(_dp), k.ctypes.data_as(_dp), h.ctypes.data_as(_dp))
+    return h
 
 
 def init_random(cfg, seed):
