@@ -188,9 +188,9 @@ def barrier(dist):
         dist.barrier()
 
 
-def cpu_sample(M, O, k6, seconds=12.0, threads=0):
+def cpu_sample(O, k6, seconds=12.0, threads=0):
     """FP64 oracle sweeps of the same lattice on the host cores."""
-    cfg = M.Config.defaults(precision=64, **WORKLOAD)
+    cfg = O.config(precision=64, **WORKLOAD)
     m = O.init_random(cfg, 256)
     n = m.shape[1]
     t0 = time.perf_counter()
@@ -319,18 +319,17 @@ def run_reference(args):
     dist, rank, local, world = dist_setup()
     if rank != 0:
         return
-    import mmc_ctypes as M
-    import oracle_ctypes as O
+    import oracle_ctypes as O  # the product library is not loaded on this arm
     cores = os.cpu_count() or 1
     # The sweep cost does not depend on the tensor values, so the sample uses the
     # 256x256 tensor with 2 images (20 images take ~40 core-minutes to build on
     # the CPU).
-    tcfg = M.Config.defaults(precision=64, **dict(WORKLOAD, pbc_x=2, pbc_y=2))
+    tcfg = O.config(precision=64, **dict(WORKLOAD, pbc_x=2, pbc_y=2))
     k6 = O.tensor(tcfg)
     vals = []
     n_sw = 0
     for i in range(args.warmup + args.steps):
-        v, ns = cpu_sample(M, O, k6, seconds=args.ref_seconds, threads=cores)
+        v, ns = cpu_sample(O, k6, seconds=args.ref_seconds, threads=cores)
         if i >= args.warmup:
             vals.append(v)
             n_sw += ns
@@ -458,6 +457,10 @@ def run_ours(args):
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic, "traffic_shape": tshape,
                 "algorithmic_bytes_per_launch": bytes_launch, "avg_ms_per_launch": per_launch_ms,
                 "kernel_ms_per_batch_sweep": fam, "launch_shape": shape,
+                "timing": "per-kernel CUDA events on the batch's stream over 200 sweeps launched on ONE stream "
+                          "(mmc_batch_profile_sweeps): serialised launches, an upper bound on each kernel's time "
+                          "in the timed run, whose graphs overlap the kernels of the replica parts on "
+                          f"{shape[9]} streams",
                 "bytes_model": "per replica: x passes 3*4*N real + 3*8*N_h complex; column pass 2*3*8*N_h "
                                "(+ 6*8*N_h shared tensor once); Metropolis 36 B per trial (both colours); row "
                                "kernel m in/out 2*3*4*N + spectrum rows in/out 2*3*8*N_h; N=65536, N_h=33024"}
@@ -489,6 +492,23 @@ def run_ours(args):
         lat64.close()
         fp64_line = {"value": fp64, "unit": UNIT, "engine": "kernels", "lattices": 1,
                      "batched_fp32_over_fp64": value / world / fp64, "single_fp32_over_fp64": single_v / fp64}
+        # the same batch in FP64: splits "batched FP32 over plain FP64" into its
+        # batching part (FP64 batched / FP64 plain) and its precision part
+        # (FP32 batched / FP64 batched)
+        b64 = M.Batch([M.Config.defaults(precision=64, **dict(WORKLOAD, randomseed=sd)) for sd in seeds],
+                      device=local)
+        b64.build_demag(CACHE_DIR)
+        b64.set_temperatures(np.full(R, stage_temperature(0)))
+        b64.autotune(16)
+        b64.run_sweeps(0, 0, 100)
+        b64.set_temperatures(np.full(R, stage_temperature(1)))
+        b64.run_sweeps(1, 0, 1000)
+        fp64b = R * 1000 * n / (b64.last_run_ms() / 1e3)
+        fp64_line["batched_fp64"] = {"value": fp64b, "unit": UNIT, "replicas": R,
+                                     "launch_shape": list(b64.launch_shape())}
+        fp64_line["batching_part"] = fp64b / fp64
+        fp64_line["precision_part"] = value / world / fp64b
+        b64.close()
 
     farm_line = None if args.no_farm else pt_farm(M, local, 2000)
     slab = None if args.no_slab else slab_line(M, local, 200)
@@ -515,9 +535,9 @@ def run_ours(args):
     }
     if rank == 0 and not args.no_cpu:
         k6 = single.tensor()
-        v1, ns1 = cpu_sample(M, O, k6, seconds=args.cpu_seconds, threads=1)
+        v1, ns1 = cpu_sample(O, k6, seconds=args.cpu_seconds, threads=1)
         cores = os.cpu_count() or 1
-        vN, nsN = cpu_sample(M, O, k6, seconds=args.cpu_seconds, threads=cores)
+        vN, nsN = cpu_sample(O, k6, seconds=args.cpu_seconds, threads=cores)
         line["cpu_baseline"] = {"value": vN, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": f"{nsN} FP64 sweeps of one 256x256x1 lattice (FFT demag), same tensor",
                                 "single_thread": v1}

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define MMC_ABI_VERSION 1
+#define MMC_ABI_VERSION 2
 
 enum mmc_status {
   MMC_OK = 0,
@@ -101,6 +101,9 @@ typedef struct mmc_config {
                                               sum, as the reference; R >= 12: image offsets at least
                                               R cells away by the far-field expansion (more accurate
                                               there, and far cheaper; see mmc_build_demag) */
+  int debug_h_field;                       /* 1: the stage loop writes the per-term field dumps at
+                                              every energy output, as the reference's DEBUG_H_FIELD
+                                              build does (see mmc_run_anneal); default 0 */
 } mmc_config;
 
 typedef struct mmc_observables {
@@ -134,9 +137,18 @@ int mmc_config_format(const mmc_config* cfg, char* buf, size_t len);
 
 /* Padded dimensions of the tensor grid (src/main.cu:254-263): n -> 2n-1 on
  * open axes, n on periodic ones -- the grid of mmc_get_tensor and of the
- * tensor cache.  The transforms may pad an open axis further (to the next
- * power of two up to 1024); that grid is internal. */
+ * tensor cache.  The transforms may pad an open axis further: see
+ * mmc_transform_dims. */
 int mmc_padded_dims(const mmc_config* cfg, int out[3]);
+/* Dimensions of the grid the demag transforms run on (no device needed).
+ * No counterpart in the reference, which transforms on the tensor grid.  An
+ * open axis whose tensor length t = 2n-1 exceeds 16 is padded to the next
+ * power of two when that is at most 256; when it would be 512 or 1024, t is
+ * kept if its prime factors are all at most 31 (the mixed-radix transforms),
+ * else padded.  Periodic axes and t <= 16 are kept.  The tensor is re-wrapped
+ * onto this grid (offsets |o| <= n-1 kept, the rest 0), which gives the same
+ * linear convolution. */
+int mmc_transform_dims(const mmc_config* cfg, int out[3]);
 
 /* Allocates the device state for one lattice on CUDA device `device`
  * (the -gpu= flag, src/GPU_selector.h:35-76).  m starts at +z. */
@@ -193,7 +205,9 @@ int mmc_demag_apply(mmc_handle* h, const void* mdev, void* hdev, void* scratch, 
                     void* stream);
 /* Size of the device array behind mmc_demag_apply_static(): 16 MiB, enough
  * for the spectrum of any lattice with 3 * nspec * 2 * sizeof(real) at most
- * this size (a 1024 x 1024 periodic film in FP32, 512 x 512 open in FP64). */
+ * this size (a 1024 x 1024 periodic film in FP32, a 512 x 512 open film in
+ * FP32 -- transform grid 1023 x 1023, 12.6 MB -- or a 256 x 256 open film in
+ * FP64). */
 #define MMC_DEMAG_STATIC_SCRATCH_BYTES (16u * 1024u * 1024u)
 /* mmc_demag_apply() for callers that cannot allocate device memory at the
  * point of the call: code that runs inside a device-memory budget owned by
@@ -287,7 +301,13 @@ int mmc_profile_fused(mmc_handle* h, double temperature, long long stage, long l
 
 /* The whole temperature-stage loop of src/main.cu:801-1139 with its outputs
  * (energy.txt, %06ld_%.2fK_%ld.ovf snapshots) written into output_dir.
- * verbose != 0 prints progress lines to stdout. */
+ * verbose != 0 prints progress lines to stdout.  With cfg.debug_h_field the
+ * loop also writes, at every energy output and over the same files, the
+ * per-term dumps of the reference's DEBUG_H_FIELD build (src/main.cu:965-1086):
+ * B_demag.ovf, B_anis.ovf, B_exch.ovf, B_dmi.ovf, B_effective.ovf (mu0 H in T,
+ * B_effective including B_ext) and E_density.ovf (J/m^3 in all three columns;
+ * e_i = -(mu0 Ms/2) m_i.(H_ex + H_dm + H_an + H_d) - Ms m_i.B_ext, which sums
+ * times V to the total energy), in cfg.ovf_format. */
 int mmc_run_anneal(mmc_handle* h, const char* output_dir, int verbose);
 
 /* Asks a running call on another thread (or a signal handler) to stop at the

@@ -14,7 +14,8 @@ int ovf_read(const std::string& path, int nx, int ny, int nz, double dx, double 
              double* mx, double* my, double* mz);
 int ovf_write(const std::string& path, int nx, int ny, int nz, double dx, double dy, double dz,
               const double* mx, const double* my, const double* mz, int format,
-              const std::string& title);
+              const std::string& title, const std::string& labels = "m_x m_y m_z",
+              const std::string& units = "1 1 1");
 
 int config_load_ini(const std::string& path, mmc_config* cfg);
 int config_validate(const mmc_config* cfg);

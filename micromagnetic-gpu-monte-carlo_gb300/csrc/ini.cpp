@@ -103,7 +103,7 @@ const KeyDef kKeys[] = {
     KD(rand_block_size, K_INT, true), KD(cal_demag_flag, K_BOOL, true),
     // optional keys of this library
     KD(use_reference_pi, K_BOOL, false), KD(tensor_cache, K_STR, false), KD(fused_band, K_INT, false),
-    KD(tensor_far_radius, K_INT, false),
+    KD(tensor_far_radius, K_INT, false), KD(debug_h_field, K_BOOL, false),
 };
 #undef KD
 

@@ -9,7 +9,10 @@
 // triples, x index fastest, then y, then z.
 //
 // Formats read: OVF 2.0 ("Data Text", "Data Binary 4", "Data Binary 8",
-// little-endian) and OVF 1.0 rectangular meshes (binary data big-endian).
+// little-endian) and OVF 1.0 rectangular meshes (binary data big-endian; the
+// stored values times "valuemultiplier" are the field).  Header keys other
+// than the node counts, step sizes, valuedim, meshtype and valuemultiplier
+// (Title, Desc, units, extents, boundary, "##" comments) are skipped.
 // Format written: OVF 2.0, binary 4 / binary 8 / text.
 #include <cctype>
 #include <cmath>
@@ -111,6 +114,7 @@ int ovf_read(const std::string& path, int nx, int ny, int nz, double dx, double 
   long long xn = -1, yn = -1, zn = -1;
   double xs = -1, ys = -1, zs = -1;
   int valuedim = 3;
+  double multiplier = 1.0;  // OVF 1.0: stored values times valuemultiplier are the field
   std::string meshtype = "rectangular";
   std::string data_kind;
   while (next_line(&line)) {
@@ -126,6 +130,7 @@ int ovf_read(const std::string& path, int nx, int ny, int nz, double dx, double 
     else if (k == "ystepsize") ys = std::atof(v.c_str());
     else if (k == "zstepsize") zs = std::atof(v.c_str());
     else if (k == "valuedim") valuedim = std::atoi(v.c_str());
+    else if (k == "valuemultiplier" && version == 1) multiplier = std::atof(v.c_str());
     else if (k == "meshtype") meshtype = v;
     else if (k == "begin" && v.rfind("data", 0) == 0) {
       data_kind = v;
@@ -162,9 +167,9 @@ int ovf_read(const std::string& path, int nx, int ny, int nz, double dx, double 
     }
     if (got != 3 * n) return fail(MMC_ERR_IO, path + ": truncated text data");
     for (size_t i = 0; i < n; ++i) {
-      mx[i] = vals[3 * i];
-      my[i] = vals[3 * i + 1];
-      mz[i] = vals[3 * i + 2];
+      mx[i] = multiplier * vals[3 * i];
+      my[i] = multiplier * vals[3 * i + 1];
+      mz[i] = multiplier * vals[3 * i + 2];
     }
     return MMC_OK;
   }
@@ -188,7 +193,6 @@ int ovf_read(const std::string& path, int nx, int ny, int nz, double dx, double 
     else if (as_f64(load_u64(p, true)) == 123456789012345.0) big = true;
     else return fail(MMC_ERR_IO, path + ": bad binary-8 check value");
   }
-  (void)version;
   p += width;
   for (size_t i = 0; i < n; ++i) {
     double v[3];
@@ -196,16 +200,16 @@ int ovf_read(const std::string& path, int nx, int ny, int nz, double dx, double 
       const unsigned char* q = p + (3 * i + c) * (size_t)width;
       v[c] = width == 4 ? (double)as_f32(load_u32(q, big)) : as_f64(load_u64(q, big));
     }
-    mx[i] = v[0];
-    my[i] = v[1];
-    mz[i] = v[2];
+    mx[i] = multiplier * v[0];
+    my[i] = multiplier * v[1];
+    mz[i] = multiplier * v[2];
   }
   return MMC_OK;
 }
 
 int ovf_write(const std::string& path, int nx, int ny, int nz, double dx, double dy, double dz,
               const double* mx, const double* my, const double* mz, int format,
-              const std::string& title) {
+              const std::string& title, const std::string& labels, const std::string& units) {
   if (format < 0 || format > 2) return fail(MMC_ERR_INVALID, "bad OVF format");
   std::ofstream out(path, std::ios::binary | std::ios::trunc);
   if (!out) return fail(MMC_ERR_IO, "cannot write OVF file: " + path);
@@ -217,7 +221,7 @@ int ovf_write(const std::string& path, int nx, int ny, int nz, double dx, double
   h << "# meshtype: rectangular\n# meshunit: m\n";
   h << "# xmin: 0\n# ymin: 0\n# zmin: 0\n";
   h << "# xmax: " << nx * dx << "\n# ymax: " << ny * dy << "\n# zmax: " << nz * dz << "\n";
-  h << "# valuedim: 3\n# valuelabels: m_x m_y m_z\n# valueunits: 1 1 1\n";
+  h << "# valuedim: 3\n# valuelabels: " << labels << "\n# valueunits: " << units << "\n";
   h << "# xbase: " << 0.5 * dx << "\n# ybase: " << 0.5 * dy << "\n# zbase: " << 0.5 * dz << "\n";
   h << "# xnodes: " << nx << "\n# ynodes: " << ny << "\n# znodes: " << nz << "\n";
   h << "# xstepsize: " << dx << "\n# ystepsize: " << dy << "\n# zstepsize: " << dz << "\n";

@@ -63,6 +63,54 @@ void unit_root(long long j, long long N, double* c, double* s) {
   *s = (double)-sinl(a);
 }
 
+// An initial state read from an OVF file as unit vectors: files that store
+// the magnetisation M in A/m (OOMMF's usual output) or slightly unnormalised
+// m are scaled to |m| = 1; vectors already of unit length to 1e-6 are kept
+// as they are (bit for bit).  A zero vector (a vacuum cell) has no direction
+// and is an error: every cell of this model is magnetic.
+int unit_vectors(double* m3, long long n, const char* path) {
+  for (long long i = 0; i < n; ++i) {
+    double& x = m3[i];
+    double& y = m3[n + i];
+    double& z = m3[2 * n + i];
+    const double r = std::sqrt(x * x + y * y + z * z);
+    if (!(r > 0) || !std::isfinite(r))
+      return fail(MMC_ERR_IO, std::string(path) + ": cell " + std::to_string(i) +
+                                  " has no magnetisation direction (zero or non-finite vector)");
+    if (std::fabs(r - 1.0) > 1e-6) {
+      x /= r;
+      y /= r;
+      z /= r;
+    }
+  }
+  return MMC_OK;
+}
+
+// The transform grid's length for a tensor-grid length t: an open axis of
+// 2n - 1 > 16 is padded on to the next power of two when that has a
+// warp-level transform that every engine takes (32 .. 256); lines of up to 16
+// take the per-thread transforms as they are.  Lengths whose power of two
+// would be 512 or 1024 (served by the pass kernels' wide transforms only, not
+// by the film engine or the batched row kernel) stay as they are when the
+// mixed-radix transforms have a plan for them, and are padded only when they
+// have a prime factor above FFT_MAX_RADIX or too many factors.
+bool has_mixed_radix_plan(int t) {
+  int m = t, stages = 0;
+  while (m % 2 == 0) m /= 2, ++stages;
+  for (int f = 3; m > 1 && f <= FFT_MAX_RADIX; f += 2)
+    while (m % f == 0) m /= f, ++stages;
+  return m == 1 && stages <= FFT_MAX_STAGES;
+}
+
+int transform_len(int t, bool open) {
+  if (!open || t <= 16) return t;
+  int p = 1;
+  while (p < t) p *= 2;
+  if (p > 1024) return t;
+  if (p <= 256) return p;
+  return has_mixed_radix_plan(t) ? t : p;
+}
+
 int make_plan(int n, PlanHost* ph) {
   FftPlan& p = ph->p;
   p = FftPlan{};
@@ -258,7 +306,7 @@ struct mmc_handle {
   double* field64 = nullptr;  // 3n doubles, device
   bool demag_built = false;
   double k0[6] = {0, 0, 0, 0, 0, 0};
-  std::vector<double> tensor;  // 6*np, x fastest
+  std::vector<double> tensor;  // 6*tnp on the tensor grid (txp, typ, tzp), x fastest
   std::atomic<int> stop{0};
   unsigned long long proposed = 0;
   unsigned long long acc_base = 0;
@@ -632,7 +680,7 @@ std::string join(const std::string& d, const std::string& f) {
 }
 
 // Tensor cache in the reference's raw format (src/main.cu:427-455, 548-572):
-// 6 blocks xx,xy,xz,yy,yz,zz of nxp*nyp*nzp doubles, z fastest / x slowest.
+// 6 blocks xx,xy,xz,yy,yz,zz of txp*typ*tzp doubles (the tensor grid), z fastest / x slowest.
 bool cache_load(mmc_handle* h, const std::string& path) {
   std::ifstream in(path, std::ios::binary);
   if (!in) return false;
@@ -956,18 +1004,9 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   g.txp = cfg->pbc_x == 0 ? 2 * cfg->nx - 1 : cfg->nx;
   g.typ = cfg->pbc_y == 0 ? 2 * cfg->ny - 1 : cfg->ny;
   g.tzp = cfg->pbc_z == 0 ? 2 * cfg->nz - 1 : cfg->nz;
-  // the transform grid: an open axis of 2n - 1 > 16 is padded on to the next
-  // power of two when that has a warp-level transform (32 .. 1024); lines of
-  // up to 16 take the per-thread transforms as they are
-  auto fft_len = [](int t, bool open) {
-    if (!open || t <= 16) return t;
-    int p = 1;
-    while (p < t) p *= 2;
-    return p <= 1024 ? p : t;
-  };
-  g.nxp = fft_len(g.txp, cfg->pbc_x == 0);
-  g.nyp = fft_len(g.typ, cfg->pbc_y == 0);
-  g.nzp = fft_len(g.tzp, cfg->pbc_z == 0);
+  g.nxp = transform_len(g.txp, cfg->pbc_x == 0);
+  g.nyp = transform_len(g.typ, cfg->pbc_y == 0);
+  g.nzp = transform_len(g.tzp, cfg->pbc_z == 0);
   g.hx = g.nxp / 2 + 1;
   g.hxp = g.hx + (g.hx & 1);
   g.per[0] = cfg->pbc_x != 0;
@@ -1046,6 +1085,7 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
     if ((st = ovf_read(cfg->ovf_filename, g.nx, g.ny, g.nz, cfg->dx, cfg->dy, cfg->dz, mm.data(), mm.data() + g.n,
                        mm.data() + 2 * g.n)) != MMC_OK)
       return bail(st);
+    if ((st = unit_vectors(mm.data(), g.n, cfg->ovf_filename)) != MMC_OK) return bail(st);
     if ((st = set_m_impl(h, mm.data(), mm.data() + g.n, mm.data() + 2 * g.n)) != MMC_OK) return bail(st);
   } else {
     std::vector<double> mm(3 * g.n, 0.0);
@@ -1099,6 +1139,59 @@ int snapshot(mmc_handle* h, const std::string& dir, long long count, double T, l
                    mm.data() + n, mm.data() + 2 * n, h->cfg.ovf_format, "m");
 }
 
+// One term of the effective field (enum mmc_term) in A/m, into host arrays.
+int field_to_host(mmc_handle* h, int term, double* out3) {
+  HCoef k = make_h_coef(h);
+  cudaError_t e = h->prec == 32 ? launch_field<float>(h->g, k, term, (const float*)h->m, (const float*)h->h,
+                                                      h->field64, h->st)
+                                : launch_field<double>(h->g, k, term, (const double*)h->m, (const double*)h->h,
+                                                       h->field64, h->st);
+  CU(e);
+  CU(cudaMemcpyAsync(out3, h->field64, 3 * h->g.n * sizeof(double), cudaMemcpyDeviceToHost, h->st));
+  return sync_check(h);
+}
+
+// The per-term dumps of the reference's DEBUG_H_FIELD build (src/main.cu:965-1086),
+// written over the same files at every energy output: B_demag, B_anis, B_exch,
+// B_dmi and B_effective (mu0 H in T; B_effective includes B_ext) and
+// E_density (the energy density in J/m^3, in all three columns as there).
+// The demag field is the one the energy evaluation just computed for the
+// current state.  The reference's B_exch kernel body is not published; here
+// exchange and interfacial DMI are written apart.  Its mc_E_density (the
+// Metropolis kernel's per-cell energy, also unpublished) is not written.
+// E_density splits the energy by cells as
+//   e_i = -(mu0 Ms / 2) m_i.(H_ex + H_dm + H_an + H_d)_i - mu0 Ms m_i.H_zeeman,
+// whose sum times the cell volume is the total energy.
+int dump_fields(mmc_handle* h, const std::string& dir) {
+  const mmc_config& c = h->cfg;
+  const long long n = h->g.n;
+  const double mu0 = 4e-7 * pi_of(&c);
+  std::vector<double> m(3 * n), f(3 * n), e(3 * n, 0.0);
+  TRY(get_m_impl(h, m.data(), m.data() + n, m.data() + 2 * n));
+  struct Dump {
+    int term;
+    const char* name;  // file stem, also the OVF title; none for the Zeeman term
+  };
+  const Dump dumps[] = {{MMC_TERM_DEMAG, "B_demag"}, {MMC_TERM_ANISOTROPY, "B_anis"},
+                        {MMC_TERM_EXCHANGE, "B_exch"}, {MMC_TERM_DMI, "B_dmi"},
+                        {MMC_TERM_ZEEMAN, nullptr}, {MMC_TERM_TOTAL, "B_effective"}};
+  for (const Dump& d : dumps) {
+    TRY(field_to_host(h, d.term, f.data()));
+    if (d.term != MMC_TERM_TOTAL) {
+      const double w = d.term == MMC_TERM_ZEEMAN ? -mu0 * c.ms : -0.5 * mu0 * c.ms;
+      for (long long i = 0; i < n; ++i)
+        e[i] += w * (m[i] * f[i] + m[n + i] * f[n + i] + m[2 * n + i] * f[2 * n + i]);
+    }
+    if (!d.name) continue;
+    for (auto& v : f) v *= mu0;
+    TRY(ovf_write(join(dir, std::string(d.name) + ".ovf"), h->g.nx, h->g.ny, h->g.nz, c.dx, c.dy, c.dz, f.data(),
+                  f.data() + n, f.data() + 2 * n, c.ovf_format, d.name, "B_x B_y B_z", "T T T"));
+  }
+  for (long long i = 0; i < n; ++i) e[n + i] = e[2 * n + i] = e[i];
+  return ovf_write(join(dir, "E_density.ovf"), h->g.nx, h->g.ny, h->g.nz, c.dx, c.dy, c.dz, e.data(),
+                   e.data() + n, e.data() + 2 * n, c.ovf_format, "E_density", "E E E", "J/m3 J/m3 J/m3");
+}
+
 // The temperature-stage loop (src/main.cu:801-1139).  T is stepped in the
 // working precision as the reference's FLOAT_ Temperature is.
 template <typename R>
@@ -1140,6 +1233,7 @@ int anneal_loop(mmc_handle* h, const std::string& dir, int verbose) {
         if (!fp) return fail(MMC_ERR_IO, "cannot append to " + efile);
         std::fprintf(fp, "%f %lld %g\n", (double)T, s, o.e_total);
         std::fclose(fp);
+        if (c.debug_h_field) TRY(dump_fields(h, dir));
       }
       long long next = c.circle_per_stage;
       const long long per[3] = {c.terminal_output_period, c.ms_output_period, c.energy_output_period};
@@ -1783,6 +1877,7 @@ int batch_create_impl(const mmc_config* cfgs, int R, int device, mmc_batch** out
       if ((st = ovf_read(cfgs[r].ovf_filename, g.nx, g.ny, g.nz, cfgs[r].dx, cfgs[r].dy, cfgs[r].dz, mm.data(),
                          mm.data() + g.n, mm.data() + 2 * g.n)) != MMC_OK)
         return bail(st);
+      if ((st = unit_vectors(mm.data(), g.n, cfgs[r].ovf_filename)) != MMC_OK) return bail(st);
       if (cudaMemcpy(h->stage64, mm.data(), 3 * g.n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(MMC_ERR_CUDA, "upload failed"));
       cudaError_t e = h->prec == 32 ? launch_from_f64<float>(3 * g.n, h->stage64, (float*)b->m + off, h->st)
@@ -1851,6 +1946,15 @@ int mmc_padded_dims(const mmc_config* cfg, int out[3]) {
   out[0] = cfg->pbc_x == 0 ? 2 * cfg->nx - 1 : cfg->nx;
   out[1] = cfg->pbc_y == 0 ? 2 * cfg->ny - 1 : cfg->ny;
   out[2] = cfg->pbc_z == 0 ? 2 * cfg->nz - 1 : cfg->nz;
+  return MMC_OK;
+}
+
+int mmc_transform_dims(const mmc_config* cfg, int out[3]) {
+  int t[3];
+  TRY(mmc_padded_dims(cfg, t));
+  out[0] = transform_len(t[0], cfg->pbc_x == 0);
+  out[1] = transform_len(t[1], cfg->pbc_y == 0);
+  out[2] = transform_len(t[2], cfg->pbc_z == 0);
   return MMC_OK;
 }
 

@@ -54,6 +54,7 @@ class Config(ctypes.Structure):
         ("sweep_engine", ctypes.c_int),
         ("fused_band", ctypes.c_int),
         ("tensor_far_radius", ctypes.c_int),
+        ("debug_h_field", ctypes.c_int),
     ]
 
     @classmethod
@@ -126,6 +127,7 @@ def lib(path=None):
         "mmc_config_load_ini": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(Config)]),
         "mmc_config_format": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_char_p, ctypes.c_size_t]),
         "mmc_padded_dims": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_int)]),
+        "mmc_transform_dims": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_int)]),
         "mmc_create": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.c_int, ctypes.POINTER(H)]),
         "mmc_destroy": (None, [H]),
         "mmc_init_random": (ctypes.c_int, [H, ctypes.c_longlong]),
@@ -227,6 +229,13 @@ def format_config(cfg):
 def padded_dims(cfg):
     out = (ctypes.c_int * 3)()
     check(lib().mmc_padded_dims(ctypes.byref(cfg), out))
+    return tuple(out)
+
+
+def transform_dims(cfg):
+    """The grid the demag transforms run on (mmc_transform_dims; no device call)."""
+    out = (ctypes.c_int * 3)()
+    check(lib().mmc_transform_dims(ctypes.byref(cfg), out))
     return tuple(out)
 
 

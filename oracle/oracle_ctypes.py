@@ -93,6 +93,16 @@ def independent():
     return _INDEP
 
 
+def config(**kw):
+    """An mmc_config for the oracle alone (zero-initialised, then kw), without
+    loading the product library: the oracle reads only the geometry, the
+    material, the seed, use_reference_pi and tensor_far_radius."""
+    c = _config_type()()
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
 def _c(cfg):
     return ctypes.cast(ctypes.byref(cfg), ctypes.c_void_p)
 

@@ -17,7 +17,7 @@ def test_exports_every_declared_symbol(M):
 
 def test_abi_constants(M):
     L = M.lib()
-    assert L.mmc_abi_version() == 1
+    assert L.mmc_abi_version() == 2
     assert L.mmc_config_size() == ctypes.sizeof(M.Config)
     assert L.mmc_status_string(0) == b"ok"
     assert L.mmc_status_string(7) == b"interrupted"

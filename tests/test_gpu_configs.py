@@ -70,9 +70,9 @@ def test_batched_fp32_vector_form_tracks_fp64_at_256(M, cache):
     with M.Batch(c32) as a, M.Batch(c64) as b:
         a.build_demag(cache)
         b.build_demag(cache)
-        shape = list(a.launch_shape())
-        shape[5], shape[6] = 0, 2  # pass kernels, vectorised Metropolis form
-        a.set_launch_shape(shape)
+        # pass kernels (4-row x passes of 128 threads, 8-column passes of 384
+        # threads), the vectorised Metropolis form, one stream
+        a.set_launch_shape([4, 128, 8, 64, 384, 0, 2, 1, 1, 1])
         assert a.launch_shape()[6] == 2
         for r in range(R):
             b.set_m(r, a.get_m(r))

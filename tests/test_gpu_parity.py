@@ -264,6 +264,75 @@ def test_anneal_outputs(M, tmp_path):
     np.testing.assert_allclose(np.linalg.norm(m, axis=0), 1, atol=1e-6)
 
 
+def test_debug_field_dumps(M, O, tmp_path):
+    """debug_h_field = 1: at every energy output the stage loop writes
+    B_demag / B_anis / B_exch / B_dmi / B_effective (mu0 H, T) and E_density
+    (J/m^3), as the reference's DEBUG_H_FIELD build (src/main.cu:965-1086).
+    Three stages of 20 sweeps with one energy output each: the files left are
+    those of the last stage's start, i.e. of the state after 40 sweeps.  They
+    equal the library's own fields of that state bit for bit (FP64, Binary 8),
+    and the oracle's within 1e-12; E_density sums to the total energy."""
+    kw = dict(nx=12, ny=10, precision=64, Dind=6e-3, debug_h_field=1, ovf_format=M.OVF_BINARY8,
+              Temperature_start=200.0, Temperature_end=150.0, Temperature_step=0.9, circle_per_stage=20,
+              energy_output_period=20, ms_output_period=1000, terminal_output_period=1000)
+    c = cfg(M, **kw)
+    out = tmp_path / "run.output"
+    out.mkdir()
+    with M.Lattice(c) as lat:
+        lat.build_demag()
+        m0 = lat.get_m()
+        k = lat.tensor()
+        lat.run_anneal(out)
+    mu0 = 4e-7 * np.pi
+    files = {t: M.ovf_read(out / (t + ".ovf"), c.nx, c.ny, 1, c.dx, c.dy, c.dz)
+             for t in ("B_demag", "B_anis", "B_exch", "B_dmi", "B_effective", "E_density")}
+    terms = {"B_exch": M.TERM_EXCHANGE, "B_dmi": M.TERM_DMI, "B_anis": M.TERM_ANISOTROPY,
+             "B_demag": M.TERM_DEMAG, "B_effective": M.TERM_TOTAL}
+    with M.Lattice(c.copy(debug_h_field=0)) as lat:
+        lat.set_m(m0)
+        lat.run_sweeps(200.0, 0, 0, 20)
+        lat.run_sweeps(180.0, 1, 0, 20)
+        lat.compute_demag()
+        m40 = lat.get_m()
+        for name, term in terms.items():
+            assert np.array_equal(files[name], mu0 * lat.field(term)), name
+        e_total = lat.energy().e_total
+    m = m0.copy()
+    O.sweeps(c, k, 200.0, 0, 0, 20, m, demag_mode=1)
+    O.sweeps(c, k, 180.0, 1, 0, 20, m, demag_mode=1)
+    assert np.array_equal(m, m40)
+    hd = O.demag_fft(c, k, m)
+    for name, term in terms.items():
+        want = mu0 * O.field(c, term, m, hd)
+        assert rel(files[name], want) <= FP64_REL, name
+    e = files["E_density"]
+    assert np.array_equal(e[0], e[1]) and np.array_equal(e[0], e[2])
+    V = c.dx * c.dy * c.dz
+    assert abs(e[0].sum() * V - e_total) <= 1e-11 * abs(O.energy(c, m, hd)[:5]).sum()
+
+
+@pytest.mark.parametrize("name", ["ovf2_b8_comments.ovf", "ovf1_b4_bigendian.omf", "ovf2_text_spacing.ovf"])
+def test_initial_state_from_interop_ovf(M, name):
+    """ovf_filename with use_random_init = 0: a file of M in A/m (or of m times
+    an OVF 1.0 multiplier) starts the lattice at the unit vectors M / |M|; a
+    file of unit vectors is taken as it is."""
+    import importlib.util
+    p = os.path.join(GOLDEN, "make_ovf_interop.py")
+    spec = importlib.util.spec_from_file_location("make_ovf_interop", p)
+    G = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(G)
+    path = os.path.join(GOLDEN, "ovf_interop", name)
+    c = M.Config.defaults(nx=G.NX, ny=G.NY, nz=G.NZ, dx=G.DX, dy=G.DY, dz=G.DZ, pbc_x=1, pbc_y=1, pbc_z=0,
+                          precision=64, use_random_init=0, ovf_filename=path)
+    with M.Lattice(c) as lat:
+        m = lat.get_m()
+    raw = M.ovf_read(path, G.NX, G.NY, G.NZ, G.DX, G.DY, G.DZ)
+    if name == "ovf2_text_spacing.ovf":
+        assert np.array_equal(m, raw)
+    else:
+        np.testing.assert_allclose(m, raw / np.linalg.norm(raw, axis=0), rtol=0, atol=4e-16)
+
+
 def test_stop_request_interrupts(M):
     import threading
     import time
@@ -356,6 +425,9 @@ FILMS = {
     "rect_x96": dict(nx=96, ny=6, pbc_x=1, pbc_y=-1),
     "tile64": dict(nx=64, ny=64, pbc_x=2, pbc_y=2),
     "tile96x41": dict(nx=96, ny=41, pbc_x=1, pbc_y=0),
+    # open x of 200 cells: transform length 399 = 3 7 19 (kept, not padded to
+    # 512, so the film engine takes it)
+    "open200x24": dict(nx=200, ny=24, pbc_x=0, pbc_y=1),
 }
 
 

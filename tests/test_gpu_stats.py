@@ -5,6 +5,8 @@ The FP64 path makes the oracle's decisions bit for bit (test_gpu_parity), so
 them within statistical error in the final energy density, <m_z> and
 topological charge.  Workload: the 64x64x1 film with PBC 20 images, T from
 1400 K to 40 K by x0.90 per stage, 1000 sweeps per stage, seeds 1..32."""
+import os
+
 import numpy as np
 import pytest
 
@@ -55,6 +57,62 @@ def test_full_anneal_statistics_fp32_vs_fp64(M, tmp_path_factory):
         assert diff <= 4 * se + 1e-12 * abs(b.mean()), name
     # the annealed states are ordered: low energy, skyrmion / stripe mixture
     assert e64.mean() < 0
+
+
+STATS_SWEEPS_256 = int(os.environ.get("MMC_STATS_SWEEPS_256", "1000"))
+SEEDS_256 = list(range(1, 17))
+
+
+def test_full_anneal_statistics_256_fp32_vs_fp64(M, tmp_path_factory):
+    """The 256x256x1 film with PBC 20 images and the same material and
+    schedule (34 stages, 1400 K -> 40 K by x0.90): 16 batched FP32 anneals
+    against 16 batched FP64 anneals (seeds 1..16).  Sweeps per stage: 1000 by
+    default (the FP64 batch takes ~1 ms per sweep on GB300, whose FP64 rate is
+    a small fraction of its FP32 rate); MMC_STATS_SWEEPS_256=10000 runs the
+    benchmark schedule itself (~6 minutes).
+    Checked: (1) final energy density, <m_z> and Q agree within 4 standard
+    errors of the difference of the means; (2) the FP32 path's energy of each
+    final FP32 state is within 1e-4 relative of the FP64 evaluation of the same
+    state (the precision target for the energy density)."""
+    tmp = tmp_path_factory.mktemp("tensor256")
+    W = dict(MATERIAL, nx=256, ny=256, circle_per_stage=STATS_SWEEPS_256)
+    n = 256 * 256
+    V = MATERIAL["dx"] * MATERIAL["dy"] * MATERIAL["dz"]
+    res = {}
+    for prec in (32, 64):
+        cfgs = [M.Config.defaults(precision=prec, randomseed=s, **W) for s in SEEDS_256]
+        with M.Batch(cfgs) as b:
+            b.build_demag(str(tmp))
+            if prec == 32:
+                b.autotune(4)
+            for k, T in enumerate(stage_temperatures()):
+                b.set_temperatures(np.full(len(SEEDS_256), T))
+                b.run_sweeps(k, 0, STATS_SWEEPS_256)
+            obs = b.energy()
+            finals = [b.get_m(r) for r in range(len(SEEDS_256))] if prec == 32 else None
+        res[prec] = (np.array([o.e_total / (n * V) for o in obs]), np.array([o.m[2] for o in obs]),
+                     np.array([o.q for o in obs]), obs)
+        if prec == 32:
+            # the FP32 energies of the FP32 final states against FP64 evaluations of the same states
+            worst = 0.0
+            c64 = M.Config.defaults(precision=64, randomseed=1, **W)
+            with M.Lattice(c64) as lat:
+                lat.build_demag(str(tmp))
+                for r, m in enumerate(finals):
+                    lat.set_m(m)
+                    e64 = lat.energy().e_total
+                    worst = max(worst, abs(obs[r].e_total - e64) / abs(e64))
+            print(f"256^2: FP32 energy of the annealed FP32 states vs FP64 evaluation: max rel {worst:.2e}")
+            assert worst <= 1e-4
+    for i, name in enumerate(("energy density", "<m_z>", "Q")):
+        a, b = res[32][i], res[64][i]
+        se = np.sqrt(a.var(ddof=1) / len(a) + b.var(ddof=1) / len(b))
+        diff = abs(a.mean() - b.mean())
+        print(f"256^2 ({STATS_SWEEPS_256} sweeps/stage) {name}: fp32 {a.mean():.6g} +- {a.std(ddof=1):.3g}, "
+              f"fp64 {b.mean():.6g} +- {b.std(ddof=1):.3g}, |diff| / se = {diff / se if se > 0 else 0:.2f}, "
+              f"se / |mean| = {se / max(abs(b.mean()), 1e-300):.2e}")
+        assert diff <= 4 * se + 1e-12 * abs(b.mean()), name
+    assert res[64][0].mean() < 0
 
 
 def test_fp32_error_report_256(M, tmp_path):

@@ -191,3 +191,28 @@ def test_ovf_truncated_binary(M, tmp_path):
     p.write_bytes(b[: len(b) // 2])
     with pytest.raises(M.MmcError):
         M.ovf_read(p, 2, 2, 2, 1e-9, 1e-9, 1e-9)
+
+
+def _interop():
+    import importlib.util
+    p = os.path.join(os.path.dirname(__file__), "golden", "make_ovf_interop.py")
+    spec = importlib.util.spec_from_file_location("make_ovf_interop", p)
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+@pytest.mark.parametrize("name,kind", [("ovf2_b4_desc.ovf", "m32"), ("ovf2_b8_comments.ovf", "M64"),
+                                       ("ovf1_b4_bigendian.omf", "m32xMS"), ("ovf2_text_spacing.ovf", "m64")])
+def test_ovf_interop_files(M, name, kind):
+    """OVF files laid out as other codes write them (tests/golden/make_ovf_interop.py,
+    from the OVF 2.0 / 1.0 format descriptions): Desc and "##" comment lines,
+    lower-case data tags, OVF 1.0 big-endian data with a value multiplier,
+    irregular text spacing.  Values as stored (times the OVF 1.0 multiplier)."""
+    G = _interop()
+    path = os.path.join(os.path.dirname(__file__), "golden", "ovf_interop", name)
+    got = M.ovf_read(path, G.NX, G.NY, G.NZ, G.DX, G.DY, G.DZ)
+    f = G.field()
+    want = {"m32": f.astype(np.float32).astype(np.float64), "m64": f, "M64": G.MS * f,
+            "m32xMS": G.MS * f.astype(np.float32).astype(np.float64)}[kind]
+    assert np.array_equal(got, want)

@@ -208,6 +208,19 @@ def test_even_periodic_kernel_asymmetry_is_the_far_image(M, O):
     assert 0.3 < vals[0] / vals[1] / ((2.5 / 1.5) ** 3) < 3
 
 
+@pytest.mark.parametrize("n,open_len", [(6, 11), (9, 32), (16, 32), (40, 128), (129, 512), (200, 399),
+                                        (300, 1024), (512, 1023)])
+def test_transform_dims_rule(M, n, open_len):
+    """The library's transform length of an open axis of n cells: 2n - 1 kept up
+    to 16, the next power of two up to 256, beyond that 2n - 1 kept when its
+    prime factors are <= 31 (399 = 3 7 19, 1023 = 3 11 31) and padded when not
+    (257 and 599 are primes); periodic axes are never padded."""
+    c = M.Config.defaults(nx=n, ny=8, nz=1, pbc_x=0, pbc_y=3, pbc_z=0)
+    assert M.padded_dims(c) == (2 * n - 1, 8, 1)
+    assert M.transform_dims(c) == (open_len, 8, 1)
+    assert M.transform_dims(c.copy(pbc_x=2)) == (n, 8, 1)
+
+
 def _rewrap_axis(f, t, n):
     """Tensor-grid index of each transform-grid index of an axis (-1: none):
     the rule the library applies when it pads an open axis past 2n - 1."""
@@ -220,19 +233,27 @@ def _rewrap_axis(f, t, n):
     return out
 
 
-@pytest.mark.parametrize("kw", [dict(nx=6, ny=5, nz=1, pbc_x=0, pbc_y=1), dict(nx=5, ny=4, nz=3, pbc_x=0, pbc_y=0),
-                                dict(nx=7, ny=3, nz=1, pbc_x=0, pbc_y=-1)])
-def test_padded_transform_grid_is_the_same_convolution(M, O, kw):
+@pytest.mark.parametrize("kw,f", [
+    (dict(nx=6, ny=5, nz=1, pbc_x=0, pbc_y=1), (16, 5, 1)),
+    (dict(nx=5, ny=4, nz=3, pbc_x=0, pbc_y=0), (16, 8, 8)),
+    (dict(nx=7, ny=3, nz=1, pbc_x=0, pbc_y=-1), (16, 3, 1)),
+    (dict(nx=9, ny=4, nz=1, pbc_x=0, pbc_y=1), None),  # 17 > 16: the library pads x to 32
+    (dict(nx=11, ny=9, nz=1, pbc_x=0, pbc_y=0), None),  # 21 -> 32, 17 -> 32
+])
+def test_padded_transform_grid_is_the_same_convolution(M, O, kw, f):
     """The transform grid of an open axis may be longer than the reference's
-    2n - 1 (the next power of two): the tensor re-wrapped onto it (offsets
-    |o| <= n - 1 kept, the rest 0) gives, by circular convolution, the direct
-    sum of the reference's tensor."""
+    2n - 1: the tensor re-wrapped onto it (offsets |o| <= n - 1 kept, the rest
+    0) gives, by circular convolution, the direct sum of the reference's
+    tensor.  f = None takes the library's own transform grid
+    (mmc_transform_dims); the other cases pad every open axis to a power of
+    two to exercise the re-wrap where the library would not pad."""
     cfg = cfg_small(M, **kw)
     k = O.tensor(cfg)
     t = O.padded_dims(cfg)
     n = (cfg.nx, cfg.ny, cfg.nz)
-    f = tuple(1 << (ti - 1).bit_length() if (p == 0 and ti > 1) else ti
-              for ti, p in zip(t, (cfg.pbc_x, cfg.pbc_y, cfg.pbc_z)))
+    if f is None:
+        f = M.transform_dims(cfg)
+        assert f != tuple(t)
     maps = [_rewrap_axis(fi, ti, ni) for fi, ti, ni in zip(f, t, n)]
     kt = k.reshape(6, t[2], t[1], t[0])  # x fastest
     kf = np.zeros((6, f[2], f[1], f[0]))

@@ -34,11 +34,16 @@ def test_static_scratch_matches_caller_scratch(M, geom):
         ref = want.cpu().numpy().astype(np.float64)
         scale = np.abs(ref).max()
         assert scale > 0
-        for _ in range(2):  # two calls in a row share the array
-            got = torch.full_like(m, float("nan"))
-            torch.cuda.synchronize()
+        outs = [torch.full_like(m, float("nan")) for _ in range(3)]
+        torch.cuda.synchronize()
+        lat.demag_apply_static(m.data_ptr(), outs[0].data_ptr(), None)  # warm: module and array looked up
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(dev)[0]
+        for got in outs[1:]:  # two calls in a row share the array and allocate nothing
             lat.demag_apply_static(m.data_ptr(), got.data_ptr(), None)
             torch.cuda.synchronize()
+            assert torch.cuda.mem_get_info(dev)[0] == free0
+        for got in outs:
             g = got.cpu().numpy().astype(np.float64)
             assert np.abs(g - ref).max() <= tol * scale
 
@@ -54,6 +59,12 @@ def test_static_scratch_limits(M):
         h = torch.zeros_like(m)
         with pytest.raises(M.MmcError, match="static array"):
             lat.demag_apply_static(m.data_ptr(), h.data_ptr(), None)
+    # the sizes the header names: a 512 x 512 open film fits in FP32 (transform
+    # grid 1023 x 1023), not in FP64; a 256 x 256 open film fits in FP64
+    for side, prec, fits in ((512, 32, True), (512, 64, False), (256, 64, True)):
+        c = M.Config.defaults(nx=side, ny=side, nz=1, pbc_x=0, pbc_y=0, pbc_z=0, precision=prec)
+        with M.Lattice(c) as lat:
+            assert (lat.demag_scratch_bytes() <= 16 * 1024 * 1024) == fits, (side, prec)
     # an unbuilt tensor is reported, not built (building allocates)
     small = M.Config.defaults(nx=16, ny=16, nz=1, precision=32)
     with M.Lattice(small) as lat:
