@@ -1283,6 +1283,212 @@ __global__ void __launch_bounds__(256) k_mc_tile(Geom g, const McCoef<T>* __rest
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, (unsigned long long)v);
 }
 
+// Both colours of a two-colour film sweep (nz = 1, nx a multiple of 4) in one
+// launch, by strips of rows.  A CTA owns `rows` consecutive rows of one
+// replica (the last strip may be shorter) and stages the m rows y0 - 2 ..
+// y0 + rows + 1 in shared memory (slot s holds row y0 - 2 + s, wrapped on a
+// periodic y axis, absent beyond an open edge).  Colour 0 runs on its own
+// rows and on the two rows next to them (y0 - 1 and y0 + rows): the owners of
+// those rows make the same decisions from the same inputs, since the
+// neighbours of a colour-0 cell are colour-1 cells, unchanged until colour 1.
+// Colour 1 then runs on the own rows, reading the colour-0 values just
+// decided.  A thread owns pairs of cells (2k, 2k + 1) of a row, one of each
+// colour, and reads the pair's h once for both decisions.  The strip reads m
+// from `m_in` and writes its own rows to `m_out`, a different buffer: other
+// strips still read the rows it changes.  Each trial is mc_propose /
+// mc_accept on the same inputs as in the per-colour forms, so the decisions
+// are theirs bit for bit.  m is read once and written once per sweep, h is
+// read once, and one launch replaces two.
+constexpr int MCS_THREADS = 256;
+constexpr int MCS_IPT = 4;  // own-row pairs per thread
+__host__ __device__ inline bool mc_strip_ok(const Geom& g) {
+  return g.nz == 1 && g.ncolors == 2 && g.nx % 4 == 0 && g.nx >= 4 && g.nx <= 2048;
+}
+// rows per strip: the own-row pairs of a strip fill the CTA's MCS_IPT pairs
+// per thread, at most 32 rows
+__host__ __device__ inline int mc_strip_rows(const Geom& g) {
+  const int r = MCS_IPT * MCS_THREADS / (g.nx / 2);
+  return r < 1 ? 1 : r > 32 ? 32 : (r > g.ny ? g.ny : r);
+}
+template <typename T>
+__host__ __device__ inline size_t mc_strip_smem(const Geom& g) {
+  return (size_t)(mc_strip_rows(g) + 4) * 3 * g.nx * sizeof(T);
+}
+
+// Lattice row of slot s of the strip starting at y0, or -1 (absent).
+__device__ __forceinline__ int strip_slot_row(const Geom& g, int y0, int s) {
+  int y = y0 - 2 + s;
+  if (y < 0 || y >= g.ny) {
+    if (!g.per[1]) return -1;
+    y %= g.ny;
+    if (y < 0) y += g.ny;
+  }
+  return y;
+}
+
+// One trial at x of slot s (lattice row y) with the given h; neighbours from
+// the staged rows.  ALLB: every x and y bond exists.
+template <typename T, bool ALLB>
+__device__ __forceinline__ bool strip_trial(const Geom& g, const McCoef<T>& c, T* __restrict__ sm, int s, int y,
+                                            int x, bool hdn, bool hup, T hx, T hy, T hz, uint32_t stage,
+                                            uint32_t sweep) {
+  const int nx = g.nx, rs = 3 * nx;
+  T* own = sm + s * rs + x;
+  int xl = x - 1, xr = x + 1;
+  bool hl = true, hr = true;
+  if (xl < 0) {
+    if (g.per[0]) xl += nx;
+    else hl = false;
+  }
+  if (xr >= nx) {
+    if (g.per[0]) xr -= nx;
+    else hr = false;
+  }
+  if constexpr (ALLB) hl = hr = hdn = hup = true;
+  Nbrs<T> nb;
+  nb.has[0][0] = hl;
+  nb.has[0][1] = hr;
+  nb.has[1][0] = hdn;
+  nb.has[1][1] = hup;
+  nb.has[2][0] = nb.has[2][1] = false;
+  const T* row = sm + s * rs;
+  T ov[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    ov[k] = own[k * nx];
+    nb.v[0][0][k] = hl ? row[k * nx + xl] : ov[k];
+    nb.v[0][1][k] = hr ? row[k * nx + xr] : ov[k];
+    nb.v[1][0][k] = hdn ? own[k * nx - rs] : ov[k];
+    nb.v[1][1][k] = hup ? own[k * nx + rs] : ov[k];
+    nb.v[2][0][k] = nb.v[2][1][k] = ov[k];
+  }
+  const Proposal<T> p = mc_propose<T>(c, (uint32_t)(y * nx + x), stage, sweep);
+  if (mc_accept<T>(c, nb, ov[0], ov[1], ov[2], hx, hy, hz, p)) {
+    own[0] = p.x;
+    own[nx] = p.y;
+    own[2 * nx] = p.z;
+    return true;
+  }
+  return false;
+}
+
+template <typename T>
+struct Pair2 {
+  T a, b;
+};
+template <typename T>
+__device__ __forceinline__ Pair2<T> ld2(const T* p) {
+  if constexpr (sizeof(T) == 4) {
+    const float2 v = *reinterpret_cast<const float2*>(p);
+    return {v.x, v.y};
+  } else {
+    const double2 v = *reinterpret_cast<const double2*>(p);
+    return {v.x, v.y};
+  }
+}
+
+template <typename T, bool ALLB>
+__global__ void __launch_bounds__(MCS_THREADS) k_mc_strip(Geom g, const McCoef<T>* __restrict__ cp,
+                                                          const T* __restrict__ m_in, T* __restrict__ m_out,
+                                                          const T* __restrict__ h,
+                                                          const SweepCounters* __restrict__ ctr, int rows,
+                                                          FastDiv dq, FastDiv dp, unsigned long long* acc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);  // [slot][comp][x]
+  pdl_wait();  // coefficients (tempering swaps), counters, m and h come from earlier kernels
+  const McCoef<T> c = cp[blockIdx.z];
+  const long long n = g.n;
+  const int nx = g.nx, P = nx >> 1, Q = nx >> 2, rs = 3 * nx;
+  const int y0 = blockIdx.x * rows;
+  const int nown = min(rows, g.ny - y0);
+  const int nslots = nown + 4;
+  m_in += blockIdx.z * 3 * n;
+  m_out += blockIdx.z * 3 * n;
+  h += blockIdx.z * 3 * n;
+  acc += blockIdx.z;
+  const bool dm = c.cd != (T)0;
+  const bool ybonds = g.ny > 1;
+  const uint32_t stage = ctr->stage, sweep = ctr->sweep;
+  // stage the slots (16-byte loads and stores, x fastest)
+  for (int idx = threadIdx.x; idx < nslots * 3 * Q; idx += blockDim.x) {
+    const int sk = dq.div(idx), q = idx - sk * Q;
+    const int sl = sk / 3, k = sk - 3 * sl;
+    const int y = strip_slot_row(g, y0, sl);
+    if (y >= 0) st4<T>(sm + sl * rs + k * nx + 4 * q, ld4<T>(m_in + k * n + (long long)y * nx + 4 * q));
+  }
+  __syncthreads();
+  // colour 0 on the own rows (slots 2 .. nown + 1), keeping the colour-1
+  // cells' h for the second phase
+  T h1[MCS_IPT][3];
+  unsigned int mine = 0;
+#pragma unroll
+  for (int i = 0; i < MCS_IPT; ++i) {
+    const int item = threadIdx.x + i * MCS_THREADS;
+    if (item < nown * P) {
+      const int r = dp.div(item), k = item - r * P;
+      const int sl = 2 + r, y = y0 + r;
+      const int p0 = y & 1;
+      T hc[3] = {(T)0, (T)0, (T)0};
+      if (dm) {
+#pragma unroll
+        for (int cc = 0; cc < 3; ++cc) {
+          const Pair2<T> hv = ld2<T>(h + cc * n + (long long)y * nx + 2 * k);
+          hc[cc] = p0 ? hv.b : hv.a;
+          h1[i][cc] = p0 ? hv.a : hv.b;
+        }
+      } else {
+        h1[i][0] = h1[i][1] = h1[i][2] = (T)0;
+      }
+      const bool hdn = ybonds && (ALLB || strip_slot_row(g, y0, sl - 1) >= 0);
+      const bool hup = ybonds && (ALLB || strip_slot_row(g, y0, sl + 1) >= 0);
+      if (strip_trial<T, ALLB>(g, c, sm, sl, y, 2 * k + p0, hdn, hup, hc[0], hc[1], hc[2], stage, sweep)) ++mine;
+    }
+  }
+  // colour 0 on the rows next to the strip (slots 1 and nown + 2): the
+  // neighbouring strips' decisions, recomputed, not counted
+  for (int item = threadIdx.x; item < 2 * P; item += blockDim.x) {
+    const int side = item >= P, k = item - side * P;
+    const int sl = side ? nown + 2 : 1;
+    const int y = strip_slot_row(g, y0, sl);
+    if (y < 0) continue;
+    const int x = 2 * k + (y & 1);
+    T hc[3] = {(T)0, (T)0, (T)0};
+    if (dm) {
+#pragma unroll
+      for (int cc = 0; cc < 3; ++cc) hc[cc] = h[cc * n + (long long)y * nx + x];
+    }
+    const bool hdn = ybonds && (ALLB || strip_slot_row(g, y0, sl - 1) >= 0);
+    const bool hup = ybonds && (ALLB || strip_slot_row(g, y0, sl + 1) >= 0);
+    strip_trial<T, ALLB>(g, c, sm, sl, y, x, hdn, hup, hc[0], hc[1], hc[2], stage, sweep);
+  }
+  __syncthreads();
+  // colour 1 on the own rows
+#pragma unroll
+  for (int i = 0; i < MCS_IPT; ++i) {
+    const int item = threadIdx.x + i * MCS_THREADS;
+    if (item < nown * P) {
+      const int r = dp.div(item), k = item - r * P;
+      const int sl = 2 + r, y = y0 + r;
+      const int p1 = (y & 1) ^ 1;
+      const bool hdn = ybonds && (ALLB || strip_slot_row(g, y0, sl - 1) >= 0);
+      const bool hup = ybonds && (ALLB || strip_slot_row(g, y0, sl + 1) >= 0);
+      if (strip_trial<T, ALLB>(g, c, sm, sl, y, 2 * k + p1, hdn, hup, h1[i][0], h1[i][1], h1[i][2], stage, sweep))
+        ++mine;
+    }
+  }
+  __syncthreads();
+  // own rows back, whole
+  for (int idx = threadIdx.x; idx < nown * 3 * Q; idx += blockDim.x) {
+    const int sk = dq.div(idx), q = idx - sk * Q;
+    const int r = sk / 3, k = sk - 3 * r;
+    st4<T>(m_out + k * n + (long long)(y0 + r) * nx + 4 * q, ld4<T>(sm + (r + 2) * rs + k * nx + 4 * q));
+  }
+  unsigned int v = mine;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, (unsigned long long)v);
+}
+
 // =========================================================== energy
 // Per-cell energies in FP64 whatever T is (calEnergyKernel,
 // src/effective_H.h:35-43, + thrust::reduce, src/main.cu:945-948), reduced
@@ -1573,6 +1779,10 @@ cudaError_t prepare_impl(int max_dyn_smem) {
                                     (int)MC_BAND_SMEM_MAX));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_band<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)MC_BAND_SMEM_MAX));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_strip<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    max_dyn_smem));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_strip<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    max_dyn_smem));
   return cudaSuccess;
 }
 
@@ -1775,6 +1985,16 @@ cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const
   return mc_impl<T>(g, c, m, h, ctr, color, acc, st, nrep, form);
 }
 template <typename T>
+cudaError_t launch_mc_strip(const Geom& g, const McCoef<T>* c, const T* m_in, T* m_out, const T* h,
+                            const SweepCounters* ctr, unsigned long long* acc, cudaStream_t st, int nrep) {
+  if (!mc_strip_ok(g) || m_in == m_out) return cudaErrorInvalidValue;
+  const int rows = mc_strip_rows(g);
+  dim3 grid((unsigned)((g.ny + rows - 1) / rows), 1, nrep);
+  auto kern = mc_all_bonds(g) ? k_mc_strip<T, true> : k_mc_strip<T, false>;
+  return launch_pdl(kern, grid, dim3(MCS_THREADS), mc_strip_smem<T>(g), st, g, c, m_in, m_out, h, ctr, rows,
+                    FastDiv((uint32_t)(g.nx / 4)), FastDiv((uint32_t)(g.nx / 2)), acc);
+}
+template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials, int npartials,
                           double* out, cudaStream_t st, int nrep) {
   return energy_impl<T>(g, e, m, h, partials, npartials, out, st, nrep);
@@ -1828,6 +2048,8 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
                                            const DemagTuning&, const T*, T*, void*, const void*, cudaStream_t); \
   template cudaError_t launch_mc<T>(const Geom&, const McCoef<T>*, T*, const T*, const SweepCounters*, int,   \
                                     unsigned long long*, cudaStream_t, int, int);                             \
+  template cudaError_t launch_mc_strip<T>(const Geom&, const McCoef<T>*, const T*, T*, const T*,             \
+                                          const SweepCounters*, unsigned long long*, cudaStream_t, int);       \
   template cudaError_t launch_energy<T>(const Geom&, const EnCoef*, const T*, const T*, double*, int, double*, \
                                         cudaStream_t, int);                                                    \
   template cudaError_t launch_field<T>(const Geom&, const HCoef&, int, const T*, const T*, double*,            \

@@ -15,6 +15,10 @@ static_assert(MCT == MC_TILE_SIDE, "tile side");
 bool mc_tile_eligible(const Geom& g) { return mc_tile_ok(g); }
 bool mc_quad_eligible(const Geom& g) { return mc_quad_ok(g); }
 bool mc_band_eligible(const Geom& g) { return mc_band_ok(g); }
+bool mc_strip_eligible(const Geom& g) { return mc_strip_ok(g); }
+size_t mc_strip_smem_bytes(const Geom& g, size_t real_size) {
+  return real_size == 4 ? mc_strip_smem<float>(g) : mc_strip_smem<double>(g);
+}
 MMC_INSTANTIATE_FUSED(double)
 MMC_INSTANTIATE_GRAD(double)
 

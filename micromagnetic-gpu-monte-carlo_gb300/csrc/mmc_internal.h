@@ -160,8 +160,10 @@ cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, co
 // per colour; both colours of a film in one tile launch; one vectorised launch
 // per colour for films with nx a multiple of 4.
 // (MC_FORM_BAND: the vectorised form with the CTA's rows staged in shared
-// memory by asynchronous copies.)
-enum : int { MC_FORM_SCALAR = 0, MC_FORM_TILE = 1, MC_FORM_QUAD = 2, MC_FORM_BAND = 3 };
+// memory by asynchronous copies.)  MC_FORM_STRIP: both colours of a film in
+// one launch by strips of rows, reading m from one buffer and writing the
+// other (launch_mc_strip; the batch alternates its two copies of m).
+enum : int { MC_FORM_SCALAR = 0, MC_FORM_TILE = 1, MC_FORM_QUAD = 2, MC_FORM_BAND = 3, MC_FORM_STRIP = 4 };
 // color < 0: every colour of the sweep in the given form (falls back to the
 // scalar form where the lattice does not qualify).
 template <typename T>
@@ -171,6 +173,12 @@ cudaError_t launch_mc(const Geom& g, const McCoef<T>* c, T* m, const T* h, const
 bool mc_tile_eligible(const Geom& g);
 bool mc_quad_eligible(const Geom& g);
 bool mc_band_eligible(const Geom& g);
+bool mc_strip_eligible(const Geom& g);
+size_t mc_strip_smem_bytes(const Geom& g, size_t real_size);
+// One sweep (both colours) in the strip form: m_in -> m_out (distinct buffers).
+template <typename T>
+cudaError_t launch_mc_strip(const Geom& g, const McCoef<T>* c, const T* m_in, T* m_out, const T* h,
+                            const SweepCounters* ctr, unsigned long long* acc, cudaStream_t st, int nrep);
 constexpr int MC_TILE_SIDE = 32;
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials,

@@ -1344,13 +1344,31 @@ int batch_upload_coefs(mmc_batch* b) {
   return MMC_OK;
 }
 
-cudaError_t batch_demag(mmc_batch* b, cudaEvent_t* ev = nullptr) {
+// The demag field of every replica from m (default: the batch's m).
+cudaError_t batch_demag(mmc_batch* b, cudaEvent_t* ev = nullptr, const void* m = nullptr) {
   mmc_handle* h = b->base;
+  if (!m) m = b->m;
   if (h->prec == 32)
-    return launch_demag<float>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, (const float*)b->m, (float*)b->h, b->spec,
+    return launch_demag<float>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, (const float*)m, (float*)b->h, b->spec,
                                h->khat, h->st, b->R, ev);
-  return launch_demag<double>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, (const double*)b->m, (double*)b->h, b->spec,
+  return launch_demag<double>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, (const double*)m, (double*)b->h, b->spec,
                               h->khat, h->st, b->R, ev);
+}
+
+// The strip form (both colours in one launch) reads m from one copy and
+// writes the other: sweep q of a run reads m on even q and m2 on odd q.
+bool batch_strip(const mmc_batch* b) {
+  return b->rows_band == 0 && b->tun.mc_form == MC_FORM_STRIP && mc_strip_eligible(b->base->g);
+}
+int batch_alloc_m2(mmc_batch* b) {
+  const mmc_handle* h = b->base;
+  if (!b->m2) CU(cudaMalloc(&b->m2, (size_t)b->R * 3 * h->g.n * h->tsize));
+  return MMC_OK;
+}
+// After an odd number of strip-form sweeps the state sits in m2: move it back.
+cudaError_t batch_strip_settle(mmc_batch* b) {
+  mmc_handle* h = b->base;
+  return cudaMemcpyAsync(b->m, b->m2, (size_t)b->R * 3 * h->g.n * h->tsize, cudaMemcpyDeviceToDevice, h->st);
 }
 
 // The second copies of m and of the spectrum that the row kernel path needs.
@@ -1409,24 +1427,30 @@ int batch_alloc_streams(mmc_batch* b) {
   return MMC_OK;
 }
 
-// One sweep of replicas [r0, r0 + nr) on stream st.
+// One sweep of replicas [r0, r0 + nr) on stream st (parity: see batch_strip).
 template <typename T>
-cudaError_t batch_sweep_part(mmc_batch* b, int r0, int nr, cudaStream_t st, int slot) {
+cudaError_t batch_sweep_part(mmc_batch* b, int r0, int nr, cudaStream_t st, int slot, int parity) {
   mmc_handle* h = b->base;
   const long long ms = 3 * h->g.n, ss = 3 * h->g.nspec;
-  T* m = (T*)b->m + r0 * ms;
+  const bool strip = batch_strip(b);
+  T* m = (T*)(strip && parity ? b->m2 : b->m) + r0 * ms;
   T* hh = (T*)b->h + r0 * ms;
   cudaError_t e = cudaSuccess;
   if (h->cfg.cal_demag_flag)
     e = launch_demag<T>(h->g, h->px.p, h->py.p, h->pz.p, b->tun, m, hh,
                         (char*)b->spec + (size_t)r0 * ss * 2 * sizeof(T), h->khat, st, nr);
   if (e != cudaSuccess) return e;
+  if (strip) {
+    T* mo = (T*)(parity ? b->m : b->m2) + r0 * ms;
+    return launch_mc_strip<T>(h->g, (const McCoef<T>*)b->coef + r0, m, mo, hh, b->ctr + slot, b->acc + r0, st, nr);
+  }
   return launch_mc<T>(h->g, (const McCoef<T>*)b->coef + r0, m, hh, b->ctr + slot, -1, b->acc + r0, st, nr,
                       b->tun.mc_form);
 }
 
-// One sweep reading counter slot `slot` (the caller advances the counters).
-cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev, int slot) {
+// One sweep reading counter slot `slot` (the caller advances the counters);
+// parity: see batch_strip.
+cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev, int slot, int parity) {
   mmc_handle* h = b->base;
   cudaError_t e;
   const int parts = std::min(b->streams, b->R);
@@ -1444,8 +1468,8 @@ cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev, int slot) {
     for (int k = parts - 1; k >= 0; --k) {
       const int r0 = (int)((long long)b->R * k / parts), r1 = (int)((long long)b->R * (k + 1) / parts);
       cudaStream_t st = k == 0 ? h->st : b->sts[k - 1];
-      e = h->prec == 32 ? batch_sweep_part<float>(b, r0, r1 - r0, st, slot)
-                        : batch_sweep_part<double>(b, r0, r1 - r0, st, slot);
+      e = h->prec == 32 ? batch_sweep_part<float>(b, r0, r1 - r0, st, slot, parity)
+                        : batch_sweep_part<double>(b, r0, r1 - r0, st, slot, parity);
       if (e != cudaSuccess) return e;
     }
     for (int k = 1; k < parts; ++k) {
@@ -1454,11 +1478,20 @@ cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev, int slot) {
     }
     return cudaSuccess;
   }
-  if (h->cfg.cal_demag_flag && (e = batch_demag(b, ev)) != cudaSuccess) return e;
-  e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h,
-                                       b->ctr + slot, -1, b->acc, h->st, b->R, b->tun.mc_form)
-                    : launch_mc<double>(h->g, (const McCoef<double>*)b->coef, (double*)b->m, (const double*)b->h,
-                                        b->ctr + slot, -1, b->acc, h->st, b->R, b->tun.mc_form);
+  const bool strip = batch_strip(b);
+  void* mi = strip && parity ? b->m2 : b->m;
+  void* mo = parity ? b->m : b->m2;
+  if (h->cfg.cal_demag_flag && (e = batch_demag(b, ev, mi)) != cudaSuccess) return e;
+  if (strip)
+    e = h->prec == 32 ? launch_mc_strip<float>(h->g, (const McCoef<float>*)b->coef, (const float*)mi, (float*)mo,
+                                               (const float*)b->h, b->ctr + slot, b->acc, h->st, b->R)
+                      : launch_mc_strip<double>(h->g, (const McCoef<double>*)b->coef, (const double*)mi, (double*)mo,
+                                                (const double*)b->h, b->ctr + slot, b->acc, h->st, b->R);
+  else
+    e = h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h,
+                                         b->ctr + slot, -1, b->acc, h->st, b->R, b->tun.mc_form)
+                      : launch_mc<double>(h->g, (const McCoef<double>*)b->coef, (double*)b->m, (const double*)b->h,
+                                          b->ctr + slot, -1, b->acc, h->st, b->R, b->tun.mc_form);
   if (e != cudaSuccess) return e;
   if (ev && (e = cudaEventRecord(ev[4], h->st)) != cudaSuccess) return e;
   return cudaSuccess;
@@ -1473,11 +1506,13 @@ cudaError_t batch_sweeps(mmc_batch* b, long long k) {
   cudaError_t e = cudaSuccess;
   for (long long q = 0; q < k && e == cudaSuccess; ++q) {
     const int slot = (int)(q % CTR_SLOTS);
-    e = b->rows_band > 0 ? batch_sweep_rows(b, (int)(q & 1), nullptr, slot) : batch_sweep(b, nullptr, slot);
+    e = b->rows_band > 0 ? batch_sweep_rows(b, (int)(q & 1), nullptr, slot)
+                         : batch_sweep(b, nullptr, slot, (int)(q & 1));
     if (e == cudaSuccess && (slot == CTR_SLOTS - 1 || q == k - 1))
       e = launch_advance(b->ctr, (uint32_t)(slot + 1), b->base->st, CTR_SLOTS);
   }
   if (e == cudaSuccess && b->rows_band > 0 && (k & 1)) e = batch_rows_settle(b);
+  if (e == cudaSuccess && batch_strip(b) && (k & 1)) e = batch_strip_settle(b);
   return e;
 }
 
@@ -1647,6 +1682,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     if (e != cudaSuccess || status != MMC_OK) return;
     if (cd.rows_band > 0 && (status = batch_alloc_rows(b)) != MMC_OK) return;
     if (cd.streams > 1 && (status = batch_alloc_streams(b)) != MMC_OK) return;
+    if (cd.tun.mc_form == MC_FORM_STRIP && (status = batch_alloc_m2(b)) != MMC_OK) return;
     ++tried;
     b->rows_band = cd.rows_band;
     b->tun = cd.tun;
@@ -1723,6 +1759,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   }
   {
     std::vector<int> forms;
+    if (mc_strip_eligible(g) && mc_strip_smem_bytes(g, h->tsize) <= smem_limit()) forms.push_back(MC_FORM_STRIP);
     if (mc_quad_eligible(g)) forms.push_back(MC_FORM_QUAD);
     if (mc_band_eligible(g)) forms.push_back(MC_FORM_BAND);
     if (mc_tile_eligible(g)) forms.push_back(MC_FORM_TILE);
@@ -2330,7 +2367,7 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
     if (e != cudaSuccess) status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
   }
   for (long long s = 0; b->rows_band == 0 && s < nsweeps && status == MMC_OK; ++s) {
-    cudaError_t e = batch_sweep(b, ev, 0);
+    cudaError_t e = batch_sweep(b, ev, 0, (int)(s & 1));
     if (e == cudaSuccess) e = launch_advance(b->ctr, 1, h->st, CTR_SLOTS);
     if (e == cudaSuccess) e = cudaEventSynchronize(ev[4]);
     for (int k = 0; k < 4 && e == cudaSuccess; ++k) {
@@ -2338,6 +2375,10 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
       e = cudaEventElapsedTime(&ms, ev[k], ev[k + 1]);
       acc[k] += ms;
     }
+    if (e != cudaSuccess) status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (status == MMC_OK && batch_strip(b) && (nsweeps & 1)) {
+    cudaError_t e = batch_strip_settle(b);
     if (e != cudaSuccess) status = fail(MMC_ERR_CUDA, cudaGetErrorString(e));
   }
   for (auto& e : ev) cudaEventDestroy(e);
@@ -2365,9 +2406,11 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
       t.col_threads % t.col_tx != 0 ||
       t.col_threads % t.col_tx_z != 0 ||
       (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
-      t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_BAND ||
+      t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_STRIP ||
       (t.mc_form == MC_FORM_TILE && !mc_tile_eligible(g)) || (t.mc_form == MC_FORM_QUAD && !mc_quad_eligible(g)) ||
       (t.mc_form == MC_FORM_BAND && !mc_band_eligible(g)) ||
+      (t.mc_form == MC_FORM_STRIP && (!mc_strip_eligible(g) || shape[5] != 0 ||
+                                      mc_strip_smem_bytes(g, h->tsize) > smem_limit())) ||
       (t.fft_inline != 0 && t.fft_inline != 1) || (t.col_lean != 0 && t.col_lean != 1))
     return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
   if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())
@@ -2375,6 +2418,7 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
   TRY(set_dev(h));
   if (band > 0) TRY(batch_alloc_rows(b));
   if (streams > 1) TRY(batch_alloc_streams(b));
+  if (t.mc_form == MC_FORM_STRIP) TRY(batch_alloc_m2(b));
   b->tun = t;
   b->rows_band = band;
   b->streams = streams;

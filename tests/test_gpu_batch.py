@@ -83,10 +83,10 @@ TILE_GEOMS = [dict(nx=64, ny=64, pbc_x=1, pbc_y=1), dict(nx=96, ny=41, pbc_x=1, 
 
 
 def form_ok(geom, form):
-    """Eligibility of the tile (1), vector (2) and staged vector (3) forms for a
-    two-colour film."""
+    """Eligibility of the tile (1), vector (2), staged vector (3) and strip (4)
+    forms for a two-colour film."""
     nx, ny = geom["nx"], geom["ny"]
-    if form == 2:
+    if form in (2, 4):
         return nx % 4 == 0
     if form == 3:
         return nx % 4 == 0 and nx <= 1024
@@ -96,11 +96,14 @@ def form_ok(geom, form):
 
 @pytest.mark.parametrize("prec", [32, 64])
 @pytest.mark.parametrize("geom", TILE_GEOMS)
-@pytest.mark.parametrize("form", [1, 2, 3])
+@pytest.mark.parametrize("form", [1, 2, 3, 4])
 def test_mc_forms_bitwise_equal_scalar_kernels(M, prec, geom, form):
     """Both colours in one tile launch (ring of colour-0 cells recomputed), the
-    vectorised per-colour form, or the same with the rows staged in shared
-    memory, against the scalar per-colour form."""
+    vectorised per-colour form, the same with the rows staged in shared
+    memory, or both colours in one launch by strips of rows (the rows next to
+    a strip recomputed; m read from one copy and written to the other), against
+    the scalar per-colour form.  37 + 32 sweeps: the strip form's odd run ends
+    in the second copy and is moved back."""
     if not form_ok(geom, form):
         pytest.skip("form not available for this lattice (checked in test_mc_forms_rejected_where_ineligible)")
     cfgs = cfgs_for(M, 3, prec, sweep_engine=1, **geom)
@@ -322,3 +325,44 @@ def test_streams_with_tempering_and_odd_batch(M, streams):
         for r in range(5):
             assert np.array_equal(a.get_m(r), b.get_m(r)), r
         assert np.array_equal(a.temperatures(), b.temperatures())
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("streams", [1, 3])
+def test_strip_form_with_streams_tempering_and_profile(M, prec, streams):
+    """The strip form (form 4: both colours in one launch, m alternating
+    between two copies) on replica parts on several streams, with
+    parallel-tempering ladders swapping every 7 sweeps (odd graphs end in the
+    second copy), and through the profiling path with an odd sweep count:
+    results equal the scalar one-stream batch."""
+    cfgs = cfgs_for(M, 5, prec, sweep_engine=1, nx=32, ny=32, pbc_x=1, pbc_y=1)
+    temps = np.array([[60.0, 100.0, 170.0, 290.0, 500.0]])
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        sa, sb = list(a.launch_shape()), list(b.launch_shape())
+        sa[6], sa[9] = 0, 1
+        sb[6], sb[9] = 4, streams
+        a.set_launch_shape(sa)
+        b.set_launch_shape(sb)
+        assert b.launch_shape()[6] == 4
+        for x in (a, b):
+            x.set_ladders(np.arange(5).reshape(1, 5), temps, 7, 3)
+            x.run_sweeps(0, 0, 95)
+        for r in range(5):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        assert np.array_equal(a.temperatures(), b.temperatures())
+        a.profile_sweeps(1, 0, 5)
+        b.profile_sweeps(1, 0, 5)
+        for r in range(5):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
+
+
+def test_strip_form_rejected_where_ineligible(M):
+    """The strip form needs a two-colour film with nx a multiple of 4."""
+    for geom in (dict(nx=41, ny=23, pbc_x=0, pbc_y=0), dict(nx=15, ny=8, pbc_x=1, pbc_y=1),
+                 dict(nx=8, ny=6, nz=3, pbc_x=1, pbc_y=1, pbc_z=0)):
+        with M.Batch(cfgs_for(M, 2, 32, sweep_engine=1, **geom)) as b:
+            s = list(b.launch_shape())
+            s[6] = 4
+            with pytest.raises(M.MmcError):
+                b.set_launch_shape(s)
