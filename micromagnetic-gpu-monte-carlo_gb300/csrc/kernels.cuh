@@ -1569,9 +1569,14 @@ __device__ __forceinline__ void block_sum_nq(const double q[NQ], double* __restr
   }
 }
 
+// with_q = 0: the five energies (and m) only, without the solid angles of the
+// topological charge -- FP64 atan2 per plaquette, the dearest part on a GPU
+// whose FP64 rate is a small fraction of its FP32 rate; the energies are the
+// same bit for bit.  Parallel-tempering swaps need only the energies.
 template <typename T>
 __global__ void __launch_bounds__(256) k_energy(Geom g, const EnCoef* __restrict__ ep, const T* __restrict__ m,
-                                                const T* __restrict__ h, double* __restrict__ partials) {
+                                                const T* __restrict__ h, double* __restrict__ partials,
+                                                int with_q) {
   const EnCoef e = ep[blockIdx.z];
   m += blockIdx.z * 3 * g.n;
   if (h) h += blockIdx.z * 3 * g.n;
@@ -1580,7 +1585,7 @@ __global__ void __launch_bounds__(256) k_energy(Geom g, const EnCoef* __restrict
   double q[NQ];
 #pragma unroll
   for (int k = 0; k < NQ; ++k) q[k] = 0;
-  if (i < g.n) energy_terms_at<T>(g, e, m, h, i, true, q);
+  if (i < g.n) energy_terms_at<T>(g, e, m, h, i, with_q != 0, q);
   block_sum_nq(q, partials);
 }
 
@@ -1943,10 +1948,10 @@ inline int energy_blocks(const Geom& g) { return (int)((g.n + 255) / 256); }
 
 template <typename T>
 cudaError_t energy_impl(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials, int npartials,
-                        double* out, cudaStream_t st, int nrep) {
+                        double* out, cudaStream_t st, int nrep, int with_q) {
   const int nb = energy_blocks(g);
   if (nb > npartials) return cudaErrorInvalidValue;
-  k_energy<T><<<dim3(nb, 1, nrep), 256, 0, st>>>(g, e, m, h, partials);
+  k_energy<T><<<dim3(nb, 1, nrep), 256, 0, st>>>(g, e, m, h, partials, with_q);
   MMC_TRY(cudaGetLastError());
   k_reduce_partials<<<nrep, 256, 0, st>>>(partials, nb, out);
   return cudaGetLastError();
@@ -1996,8 +2001,8 @@ cudaError_t launch_mc_strip(const Geom& g, const McCoef<T>* c, const T* m_in, T*
 }
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials, int npartials,
-                          double* out, cudaStream_t st, int nrep) {
-  return energy_impl<T>(g, e, m, h, partials, npartials, out, st, nrep);
+                          double* out, cudaStream_t st, int nrep, int with_q) {
+  return energy_impl<T>(g, e, m, h, partials, npartials, out, st, nrep, with_q);
 }
 template <typename T>
 cudaError_t launch_field(const Geom& g, const HCoef& c, int term, const T* m, const T* h, double* out,
@@ -2051,7 +2056,7 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
   template cudaError_t launch_mc_strip<T>(const Geom&, const McCoef<T>*, const T*, T*, const T*,             \
                                           const SweepCounters*, unsigned long long*, cudaStream_t, int);       \
   template cudaError_t launch_energy<T>(const Geom&, const EnCoef*, const T*, const T*, double*, int, double*, \
-                                        cudaStream_t, int);                                                    \
+                                        cudaStream_t, int, int);                                               \
   template cudaError_t launch_field<T>(const Geom&, const HCoef&, int, const T*, const T*, double*,            \
                                        cudaStream_t);                                                          \
   template cudaError_t launch_init<T>(const Geom&, uint64_t, T*, cudaStream_t);                               \

@@ -182,7 +182,7 @@ cudaError_t launch_mc_strip(const Geom& g, const McCoef<T>* c, const T* m_in, T*
 constexpr int MC_TILE_SIDE = 32;
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials,
-                          int npartials, double* out, cudaStream_t st, int nrep = 1);
+                          int npartials, double* out, cudaStream_t st, int nrep = 1, int with_q = 1);
 template <typename T>
 cudaError_t launch_field(const Geom& g, const HCoef& c, int term, const T* m, const T* h, double* out,
                          cudaStream_t st);

@@ -1522,16 +1522,17 @@ cudaError_t batch_set_counters(mmc_batch* b, long long stage, long long sweep0) 
   return cudaMemcpyAsync(b->ctr, b->ctr_host, sizeof b->ctr_host, cudaMemcpyHostToDevice, b->base->st);
 }
 
-cudaError_t batch_energy_kernels(mmc_batch* b) {
+// Energies (and, with_q, the topological charge) of every replica into b->red.
+cudaError_t batch_energy_kernels(mmc_batch* b, bool with_q = true) {
   mmc_handle* h = b->base;
   cudaError_t e;
   if (h->cfg.cal_demag_flag && (e = batch_demag(b)) != cudaSuccess) return e;
   const bool dm = h->cfg.cal_demag_flag != 0;
   return h->prec == 32 ? launch_energy<float>(h->g, b->ecoef, (const float*)b->m, dm ? (const float*)b->h : nullptr,
-                                              b->partials, h->npartials, b->red, h->st, b->R)
+                                              b->partials, h->npartials, b->red, h->st, b->R, with_q)
                        : launch_energy<double>(h->g, b->ecoef, (const double*)b->m,
                                                dm ? (const double*)b->h : nullptr, b->partials, h->npartials,
-                                               b->red, h->st, b->R);
+                                               b->red, h->st, b->R, with_q);
 }
 
 cudaError_t batch_swap(mmc_batch* b) {
@@ -1550,7 +1551,7 @@ int batch_graph(mmc_batch* b, int len, bool pt) {
   CU(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   e = batch_sweeps(b, len);
-  if (pt && e == cudaSuccess) e = batch_energy_kernels(b);
+  if (pt && e == cudaSuccess) e = batch_energy_kernels(b, false);  // the swap reads the energies only
   if (pt && e == cudaSuccess) e = batch_swap(b);
   cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
   if (e != cudaSuccess || e2 != cudaSuccess) cudaGetLastError();
@@ -1608,7 +1609,7 @@ int batch_run_piece(mmc_batch* b, BatchRun& r, bool* finished) {
         CU(batch_sweeps(b, k));
         r.done += k;
         if (k == to_boundary) {
-          CU(batch_energy_kernels(b));
+          CU(batch_energy_kernels(b, false));
           CU(batch_swap(b));
         }
       }
