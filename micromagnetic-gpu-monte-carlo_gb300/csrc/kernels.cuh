@@ -1589,6 +1589,58 @@ __global__ void __launch_bounds__(256) k_energy(Geom g, const EnCoef* __restrict
   block_sum_nq(q, partials);
 }
 
+// The five energies of FP32 replicas for parallel-tempering swaps: each cell's
+// terms in FP32 (the working precision of the replicas' own updates), summed
+// per thread over ENL_CELLS cells in FP32 and from there in FP64.  Within
+// ~1e-6 relative of the FP64-per-cell evaluation (k_energy) of the same state,
+// far below what a swap decision resolves (kT ~ 1e-3 of these energies), at
+// a small fraction of its cost on a GPU with a low FP64 rate.  q[5..8] are 0.
+constexpr int ENL_CELLS = 8;
+static __global__ void __launch_bounds__(256) k_energy_lean(Geom g, const EnCoef* __restrict__ ep,
+                                                            const float* __restrict__ m, const float* __restrict__ h,
+                                                            double* __restrict__ partials) {
+  const EnCoef e = ep[blockIdx.z];
+  const int n = (int)g.n;
+  m += blockIdx.z * 3 * g.n;
+  if (h) h += blockIdx.z * 3 * g.n;
+  partials += (long long)blockIdx.z * gridDim.x * NQ;
+  const float* mx = m;
+  const float* my = m + n;
+  const float* mz = m + 2 * n;
+  const float aex[3] = {(float)e.aexV_d2[0], (float)e.aexV_d2[1], (float)e.aexV_d2[2]};
+  const float dv0 = (float)e.dV_2d[0], dv1 = (float)e.dV_2d[1], kuv = (float)e.kuV;
+  const float u0 = (float)e.u[0], u1 = (float)e.u[1], u2 = (float)e.u[2];
+  const float b0 = (float)e.msVB[0], b1 = (float)e.msVB[1], b2 = (float)e.msVB[2];
+  const float dmg = (float)e.demag;
+  float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const int row = g.dnx.div(i), x = i - row * g.nx;
+    const int z = g.dny.div(row), y = row - z * g.ny;
+    const float ax = mx[i], ay = my[i], az = mz[i];
+    for (int a = 0; a < 3; ++a) {
+      const long long j = nbr_idx(g, x, y, z, a, 1);
+      if (j < 0) continue;
+      const float ddx = mx[j] - ax, ddy = my[j] - ay, ddz = mz[j] - az;
+      acc[0] += aex[a] * (ddx * ddx + ddy * ddy + ddz * ddz);
+    }
+    const long long xp = nbr_idx(g, x, y, z, 0, 1), xm = nbr_idx(g, x, y, z, 0, -1);
+    const long long yp = nbr_idx(g, x, y, z, 1, 1), ym = nbr_idx(g, x, y, z, 1, -1);
+    const float dxmz = (xp >= 0 ? mz[xp] : 0.f) - (xm >= 0 ? mz[xm] : 0.f);
+    const float dxmx = (xp >= 0 ? mx[xp] : 0.f) - (xm >= 0 ? mx[xm] : 0.f);
+    const float dymz = (yp >= 0 ? mz[yp] : 0.f) - (ym >= 0 ? mz[ym] : 0.f);
+    const float dymy = (yp >= 0 ? my[yp] : 0.f) - (ym >= 0 ? my[ym] : 0.f);
+    acc[1] -= ax * dv0 * dxmz + ay * dv1 * dymz - az * (dv0 * dxmx + dv1 * dymy);
+    const float mu = ax * u0 + ay * u1 + az * u2;
+    acc[2] -= kuv * mu * mu;
+    acc[3] -= ax * b0 + ay * b1 + az * b2;
+    if (h) acc[4] -= dmg * (ax * h[i] + ay * h[n + i] + az * h[2 * n + i]);
+  }
+  double q[NQ];
+#pragma unroll
+  for (int k = 0; k < NQ; ++k) q[k] = k < 5 ? (double)acc[k] : 0.0;
+  block_sum_nq(q, partials);
+}
+
 static __global__ void __launch_bounds__(256) k_reduce_partials(const double* __restrict__ partials, int nblocks,
                                                                 double* __restrict__ out) {
   partials += (long long)blockIdx.x * nblocks * NQ;  // one block per replica
@@ -1957,6 +2009,22 @@ cudaError_t energy_impl(const Geom& g, const EnCoef* e, const T* m, const T* h, 
   return cudaGetLastError();
 }
 
+// with_q < 0: the energies for tempering swaps (k_energy_lean for FP32 replicas).
+template <typename T>
+cudaError_t energy_swap_impl(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials,
+                             int npartials, double* out, cudaStream_t st, int nrep) {
+  if constexpr (sizeof(T) == 4) {
+    const int nb = std::max(1, energy_blocks(g) / ENL_CELLS);
+    if (nb > npartials || g.n >= (1LL << 31)) return cudaErrorInvalidValue;
+    k_energy_lean<<<dim3(nb, 1, nrep), 256, 0, st>>>(g, e, m, h, partials);
+    MMC_TRY(cudaGetLastError());
+    k_reduce_partials<<<nrep, 256, 0, st>>>(partials, nb, out);
+    return cudaGetLastError();
+  } else {
+    return energy_impl<T>(g, e, m, h, partials, npartials, out, st, nrep, 0);
+  }
+}
+
 template <typename T>
 cudaError_t field_impl(const Geom& g, const HCoef& c, int term, const T* m, const T* h, double* out,
                        cudaStream_t st) {
@@ -2002,6 +2070,7 @@ cudaError_t launch_mc_strip(const Geom& g, const McCoef<T>* c, const T* m_in, T*
 template <typename T>
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials, int npartials,
                           double* out, cudaStream_t st, int nrep, int with_q) {
+  if (with_q < 0) return energy_swap_impl<T>(g, e, m, h, partials, npartials, out, st, nrep);
   return energy_impl<T>(g, e, m, h, partials, npartials, out, st, nrep, with_q);
 }
 template <typename T>

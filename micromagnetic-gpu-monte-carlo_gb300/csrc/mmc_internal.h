@@ -181,6 +181,9 @@ cudaError_t launch_mc_strip(const Geom& g, const McCoef<T>* c, const T* m_in, T*
                             const SweepCounters* ctr, unsigned long long* acc, cudaStream_t st, int nrep);
 constexpr int MC_TILE_SIDE = 32;
 template <typename T>
+// with_q: 1 energies, <m> and Q; 0 energies and <m> (FP64 per cell); -1 the
+// energies for tempering swaps (FP32 per cell, FP64 sums, for FP32 replicas;
+// as 0 for FP64 ones).
 cudaError_t launch_energy(const Geom& g, const EnCoef* e, const T* m, const T* h, double* partials,
                           int npartials, double* out, cudaStream_t st, int nrep = 1, int with_q = 1);
 template <typename T>

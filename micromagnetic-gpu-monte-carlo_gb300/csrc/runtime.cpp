@@ -1522,8 +1522,10 @@ cudaError_t batch_set_counters(mmc_batch* b, long long stage, long long sweep0) 
   return cudaMemcpyAsync(b->ctr, b->ctr_host, sizeof b->ctr_host, cudaMemcpyHostToDevice, b->base->st);
 }
 
-// Energies (and, with_q, the topological charge) of every replica into b->red.
-cudaError_t batch_energy_kernels(mmc_batch* b, bool with_q = true) {
+// Energies (and <m> and the topological charge) of every replica into b->red;
+// swap = true: the energies a tempering swap needs (launch_energy, with_q = -1).
+cudaError_t batch_energy_kernels(mmc_batch* b, bool swap = false) {
+  const int with_q = swap ? -1 : 1;
   mmc_handle* h = b->base;
   cudaError_t e;
   if (h->cfg.cal_demag_flag && (e = batch_demag(b)) != cudaSuccess) return e;
@@ -1551,7 +1553,7 @@ int batch_graph(mmc_batch* b, int len, bool pt) {
   CU(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaSuccess;
   e = batch_sweeps(b, len);
-  if (pt && e == cudaSuccess) e = batch_energy_kernels(b, false);  // the swap reads the energies only
+  if (pt && e == cudaSuccess) e = batch_energy_kernels(b, true);  // the swap reads the energies only
   if (pt && e == cudaSuccess) e = batch_swap(b);
   cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
   if (e != cudaSuccess || e2 != cudaSuccess) cudaGetLastError();
@@ -1609,7 +1611,7 @@ int batch_run_piece(mmc_batch* b, BatchRun& r, bool* finished) {
         CU(batch_sweeps(b, k));
         r.done += k;
         if (k == to_boundary) {
-          CU(batch_energy_kernels(b, false));
+          CU(batch_energy_kernels(b, true));
           CU(batch_swap(b));
         }
       }

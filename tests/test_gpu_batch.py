@@ -366,3 +366,39 @@ def test_strip_form_rejected_where_ineligible(M):
             s[6] = 4
             with pytest.raises(M.MmcError):
                 b.set_launch_shape(s)
+
+
+def test_parallel_tempering_fp32_swap_energies(M, O):
+    """FP32 replicas swap on energies summed from FP32 per-cell terms
+    (k_energy_lean): the first round's decisions equal the host rule applied
+    to the FP64-per-cell energies of the same states wherever the decision is
+    not a near-tie (|delta - log u| above the ~1e-6 relative energy difference
+    times |E| / kT)."""
+    K = 8
+    temps = 80.0 * (1.35 ** np.arange(K))
+    cfgs = [M.Config.defaults(nx=64, ny=64, nz=1, pbc_x=2, pbc_y=2, pbc_z=0, precision=32, randomseed=21 + r)
+            for r in range(K)]
+    interval = 10
+    with M.Batch(cfgs) as plain:
+        plain.set_temperatures(temps)
+        plain.run_sweeps(0, 0, interval)
+        E = np.array([o.e_total for o in plain.energy()])
+    with M.Batch(cfgs) as pt:
+        pt.set_ladders(np.arange(K)[None, :], temps[None, :], interval, seed=77)
+        pt.run_sweeps(0, 0, interval)
+        rep, cnt = pt.ladder_state()
+    kB = 1.3806488e-23
+    at = list(range(K))
+    checked = 0
+    for k in range(0, K - 1, 2):
+        a, b = at[k], at[k + 1]
+        delta = (1 / (kB * temps[k]) - 1 / (kB * temps[k + 1])) * (E[a] - E[b])
+        r = O.philox([0, 0, k, 2], [77, 0])[0]
+        u = (r + 0.5) * 2.0 ** -32
+        margin = abs(min(delta, 0.0) - np.log(u))
+        tol = 1e-5 * abs(1 / (kB * temps[k]) - 1 / (kB * temps[k + 1])) * (abs(E[a]) + abs(E[b]))
+        swapped = rep[0][k] == b
+        if margin > tol:
+            assert swapped == (delta >= 0 or u < np.exp(delta)), k
+            checked += 1
+    assert checked >= 3 and int(cnt[0]) == K // 2
