@@ -467,6 +467,127 @@ __global__ void __launch_bounds__(256) k_col_pass_wide(FftPlan p, int ncomp, C<T
                               inv_n, tx, s_rstride, lean);
 }
 
+// Column pass of a film (the y lines, with the K^ product between the forward
+// and the inverse transform) for lengths A x A (64, 256) with the lines held
+// in registers.  A CTA takes CR_TX kx columns; thread (t, b), t = threadIdx.x
+// mod CR_TX, holds the values y = b + A a (a = 0 .. A-1) of the three
+// components of column kx0 + t, loaded straight from the spectrum (CR_TX
+// consecutive kx per row: whole sectors).  The forward transform is the
+// arithmetic of fft_line_regs<T, false, A, A>: an A-point DFT over a in
+// registers, the twiddles W^(b ka), a transpose among the A threads of the
+// column through shared memory, an A-point DFT -- after which thread (t, b)
+// holds the frequencies b + A kb, the layout the inverse starts from, so the
+// K^ product and the inverse (fft_line_regs<T, true, A, A>'s arithmetic) run
+// from the same registers and the results go straight back.  No line is
+// staged in shared memory, and the transform, the product and the loads
+// round exactly as in k_col_pass: the same results bit for bit, with about
+// 40 % fewer instructions (ncu: 9.9 M against 17.0 M warp instructions for 32
+// replicas of 256^2).  Holding three lines per thread takes 255 registers, so
+// 2 CTAs of 128 threads fit per SM (12 % of the warp slots) and the loads'
+// latency is exposed: at 256^2 it runs at k_col_pass's speed (32.2 against
+// 33.0 us per batched sweep).  Capping it at 168 registers (3 CTAs) spilled
+// and took 44.8 us; transforming one component at a time with the others
+// parked in shared memory (126 registers) took 36.3 us.  It is an autotuner
+// candidate (col_lean = 2).
+constexpr int CR_TX = 8;  // kx columns per CTA
+template <int A>
+__host__ __device__ constexpr int col_reg_row() {
+  return A * CR_TX + 8;  // transpose row (complex): conflict-free 8-byte accesses both ways
+}
+template <typename T, int A>
+__host__ __device__ inline size_t col_reg_smem() {
+  return ((size_t)A * A + 3 * (size_t)A * col_reg_row<A>()) * sizeof(C<T>);
+}
+
+// The three components' lines of column t: DFT over the thread's A values,
+// twiddles, transpose (tb: three buffers of A rows), DFT.  first: the
+// buffers are not being read by an earlier transform.
+template <typename T, bool INV, int A>
+__device__ __forceinline__ void col_reg_transform3(C<T> (&v)[3][A], C<T>* tb, const C<T>* roots, int t, int b,
+                                                   bool first) {
+  using V = C<T>;
+  constexpr int RW = col_reg_row<A>();
+#pragma unroll
+  for (int c = 0; c < 3; ++c) RegDft<T, INV, A>::run(v[c]);
+#pragma unroll
+  for (int ka = 1; ka < A; ++ka) {
+    const V w = roots[b * ka];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c][ka] = INV ? cmulc(v[c][ka], w) : cmul(v[c][ka], w);
+  }
+  if (!first) __syncthreads();
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int ka = 0; ka < A; ++ka) tb[(c * A + ka) * RW + b * CR_TX + t] = v[c][ka];
+  __syncthreads();
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int bb = 0; bb < A; ++bb) v[c][bb] = tb[(c * A + b) * RW + bb * CR_TX + t];
+    RegDft<T, INV, A>::run(v[c]);
+  }
+}
+
+template <typename T, int A>
+__global__ void __launch_bounds__(CR_TX * A) k_col_reg(FftPlan p, C<T>* __restrict__ S, long long nspec,
+                                                          const C<T>* __restrict__ khat, int hx, int pitch,
+                                                          int load_lim, int store_lim, int flags, T inv_n,
+                                                          long long s_rstride) {
+  using V = C<T>;
+  constexpr int L = A * A;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* roots = reinterpret_cast<V*>(smem_raw);  // exp(-2 pi i j / L), j < L
+  V* tb = roots + L;
+  S += blockIdx.z * s_rstride;
+  const int t = threadIdx.x % CR_TX, b = threadIdx.x / CR_TX;
+  const int kx = blockIdx.x * CR_TX + t;
+  const bool ok = kx < hx;
+  {
+    const V* src = plan_tw<T>(p) + p.full_off;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) roots[i] = src[i];
+  }
+  pdl_wait();  // the spectrum is the x pass's output
+  V v[3][A];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int a = 0; a < A; ++a) {
+      const int row = b + A * a;
+      v[c][a] = (ok && row < load_lim) ? S[c * nspec + (long long)row * pitch + kx] : cmk<V>(0, 0);
+    }
+  __syncthreads();  // roots
+  col_reg_transform3<T, false, A>(v, tb, roots, t, b, true);
+  // src/demag_cu.cu:98-111: real and imaginary parts of sum_b K_ab M_b, divided by N
+#pragma unroll
+  for (int kb = 0; kb < A; ++kb) {
+    const int pos = b + A * kb;
+    const V* kk = khat + (long long)pos * pitch + (ok ? kx : 0);
+    V kxx = kk[0], kxy = kk[nspec], kxz = kk[2 * nspec];
+    V kyy = kk[3 * nspec], kyz = kk[4 * nspec], kzz = kk[5 * nspec];
+    if (flags & PASS_SYM) kxx.y = kxy.y = kxz.y = kyy.y = kyz.y = kzz.y = (T)0;
+    const V mx = v[0][kb], my = v[1][kb], mz = v[2][kb];
+    T hxr = (mx.x * kxx.x - mx.y * kxx.y) + (my.x * kxy.x - my.y * kxy.y) + (mz.x * kxz.x - mz.y * kxz.y);
+    T hxi = (mx.x * kxx.y + mx.y * kxx.x) + (my.x * kxy.y + my.y * kxy.x) + (mz.x * kxz.y + mz.y * kxz.x);
+    T hyr = (mx.x * kxy.x - mx.y * kxy.y) + (my.x * kyy.x - my.y * kyy.y) + (mz.x * kyz.x - mz.y * kyz.y);
+    T hyi = (mx.x * kxy.y + mx.y * kxy.x) + (my.x * kyy.y + my.y * kyy.x) + (mz.x * kyz.y + mz.y * kyz.x);
+    T hzr = (mx.x * kxz.x - mx.y * kxz.y) + (my.x * kyz.x - my.y * kyz.y) + (mz.x * kzz.x - mz.y * kzz.y);
+    T hzi = (mx.x * kxz.y + mx.y * kxz.x) + (my.x * kyz.y + my.y * kyz.x) + (mz.x * kzz.y + mz.y * kzz.x);
+    v[0][kb] = cmk<V>(hxr * inv_n, hxi * inv_n);
+    v[1][kb] = cmk<V>(hyr * inv_n, hyi * inv_n);
+    v[2][kb] = cmk<V>(hzr * inv_n, hzi * inv_n);
+  }
+  col_reg_transform3<T, true, A>(v, tb, roots, t, b, false);
+  if (!ok) return;
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int kb = 0; kb < A; ++kb) {
+      const int row = b + A * kb;
+      if (row < store_lim) S[c * nspec + (long long)row * pitch + kx] = v[c][kb];
+    }
+}
+
 // Column pass for short lines (n <= 16: the padded z axis of thin 3-D
 // lattices, short y axes): one thread per column (kx, plane) holding the three
 // component lines in registers, transformed by ThreadDft -- no shared-memory
@@ -1836,6 +1957,10 @@ cudaError_t prepare_impl(int max_dyn_smem) {
                                     (int)MC_BAND_SMEM_MAX));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_band<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)MC_BAND_SMEM_MAX));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_col_reg<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)col_reg_smem<T, 16>()));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_col_reg<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)col_reg_smem<T, 8>()));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_strip<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     max_dyn_smem));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_strip<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1873,7 +1998,7 @@ template <typename T>
 cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, const C<T>* khat, int hx,
                          int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
                          int flags, T inv_n, int tx, int threads, cudaStream_t st, int nrep = 1,
-                         long long s_rstride = 0, bool inl = false, bool lean = false) {
+                         long long s_rstride = 0, bool inl = false, bool lean = false, bool regs = false) {
   if (ncomp == 3 && p.n <= 16 && p.full_off > 0) {  // short lines: one thread per column
     const ColShortFn<T> ks = col_short_kernel<T>(p.n);
     if (ks) {
@@ -1881,6 +2006,15 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
       return launch_pdl(ks, grid, dim3(128), 0, st, p, S, nspec, khat, hx, plane_stride, pos_stride, load_lim,
                         store_lim, flags, inv_n, s_rstride);
     }
+  }
+  if (regs && ncomp == 3 && planes == 1 && (flags & ~PASS_SYM) == (PASS_FWD | PASS_MUL | PASS_INV) &&
+      pos_stride < (1LL << 31) && p.warp_a == p.warp_b && (p.warp_a == 16 || p.warp_a == 8)) {
+    dim3 grid((hx + CR_TX - 1) / CR_TX, 1, nrep);
+    if (p.warp_a == 16)
+      return launch_pdl(k_col_reg<T, 16>, grid, dim3(CR_TX * 16), col_reg_smem<T, 16>(), st, p, S, nspec, khat, hx,
+                        (int)pos_stride, load_lim, store_lim, flags, inv_n, s_rstride);
+    return launch_pdl(k_col_reg<T, 8>, grid, dim3(CR_TX * 8), col_reg_smem<T, 8>(), st, p, S, nspec, khat, hx,
+                      (int)pos_stride, load_lim, store_lim, flags, inv_n, s_rstride);
   }
   if (tx < 1 || (tx & (tx - 1)) != 0 || threads % tx != 0) return cudaErrorInvalidValue;  // see k_col_pass
   lean = lean && p.warp_a != 0;  // in-place transforms exist for the warp path only
@@ -1924,7 +2058,7 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
   if (g.nzp == 1) {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny,
                             PASS_FWD | PASS_MUL | PASS_INV | mul_flags, inv_n, tun.col_tx, tun.col_threads, st, nrep,
-                            sr, tun.fft_inline != 0, tun.col_lean != 0));
+                            sr, tun.fft_inline != 0, tun.col_lean != 0, tun.col_lean == 2));
   } else {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.ny, g.nyp, PASS_FWD, inv_n, tun.col_tx,
                             tun.col_threads, st, nrep, sr, tun.fft_inline != 0, tun.col_lean != 0));
@@ -2089,7 +2223,7 @@ cudaError_t launch_col_pass_2d(const Geom& g, const FftPlan& py, const DemagTuni
   return run_col_pass<T>(py, 3, reinterpret_cast<C<T>*>(spec), g.nspec, reinterpret_cast<const C<T>*>(khat), g.hx, 1,
                          (long long)g.nyp * g.hxp, g.hxp, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV, inv_n,
                          tun.col_tx, tun.col_threads, st, nrep, 3 * g.nspec, tun.fft_inline != 0,
-                         tun.col_lean != 0);
+                         tun.col_lean != 0, tun.col_lean == 2);
 }
 template <typename T>
 cudaError_t launch_prepare(int max_dyn_smem) {

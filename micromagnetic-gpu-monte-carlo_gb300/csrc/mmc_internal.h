@@ -138,7 +138,8 @@ struct DemagTuning {
   int col_threads;
   int mc_form;     // MC_FORM_*
   int fft_inline;  // 1: the pass kernels expand the warp-level transforms in line
-  int col_lean;    // 1: column passes transform in place and read K^ from global memory
+  int col_lean;    // 1: column passes transform in place and read K^ from global memory; 2: as 1, and
+                   // film y passes of length 64 or 256 hold their lines in registers (k_col_reg)
 };
 
 // Device counters read by the sweep kernels: [stage, sweep].

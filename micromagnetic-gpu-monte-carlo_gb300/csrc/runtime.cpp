@@ -1760,6 +1760,13 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
         }
     }
   }
+  // the column pass held in registers (col_lean = 2; films with y lengths 64 and 256)
+  if (h->cfg.cal_demag_flag && g.nzp == 1 && h->py.p.warp_a == h->py.p.warp_b &&
+      (h->py.p.warp_a == 8 || h->py.p.warp_a == 16)) {
+    Cand c = best;
+    c.tun.col_lean = 2;
+    trial(c);
+  }
   {
     std::vector<int> forms;
     if (mc_strip_eligible(g) && mc_strip_smem_bytes(g, h->tsize) <= smem_limit()) forms.push_back(MC_FORM_STRIP);
@@ -2414,7 +2421,7 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
       (t.mc_form == MC_FORM_BAND && !mc_band_eligible(g)) ||
       (t.mc_form == MC_FORM_STRIP && (!mc_strip_eligible(g) || shape[5] != 0 ||
                                       mc_strip_smem_bytes(g, h->tsize) > smem_limit())) ||
-      (t.fft_inline != 0 && t.fft_inline != 1) || (t.col_lean != 0 && t.col_lean != 1))
+      (t.fft_inline != 0 && t.fft_inline != 1) || t.col_lean < 0 || t.col_lean > 2)
     return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
   if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())
     return fail(MMC_ERR_UNSUPPORTED, "row-kernel band not available for this batch");
