@@ -103,7 +103,7 @@ const KeyDef kKeys[] = {
     KD(rand_block_size, K_INT, true), KD(cal_demag_flag, K_BOOL, true),
     // optional keys of this library
     KD(use_reference_pi, K_BOOL, false), KD(tensor_cache, K_STR, false), KD(fused_band, K_INT, false),
-    KD(tensor_far_radius, K_INT, false), KD(debug_h_field, K_BOOL, false),
+    KD(tensor_far_radius, K_INT, false), KD(debug_h_field, K_BOOL, false), KD(tensor_sum, K_INT, false),
 };
 #undef KD
 
@@ -137,6 +137,7 @@ void config_defaults(mmc_config* c) {
   c->precision = 32;
   c->ovf_format = MMC_OVF_BINARY4;
   c->use_reference_pi = 0;
+  c->tensor_sum = 1;
 }
 
 int config_validate(const mmc_config* c) {
@@ -154,6 +155,7 @@ int config_validate(const mmc_config* c) {
   if (c->fused_band < 0 || c->fused_band > 60) return fail(MMC_ERR_CONFIG, "fused_band must be in [0, 60]");
   if (c->tensor_far_radius != 0 && (c->tensor_far_radius < 12 || c->tensor_far_radius > 1000000))
     return fail(MMC_ERR_CONFIG, "tensor_far_radius must be 0 (off) or in [12, 1e6] cells");
+  if (c->tensor_sum != 0 && c->tensor_sum != 1) return fail(MMC_ERR_CONFIG, "tensor_sum must be 0 or 1");
   if (c->circle_per_stage < 0) return fail(MMC_ERR_CONFIG, "circle_per_stage must be >= 0");
   if (c->terminal_output_period < 1 || c->energy_output_period < 1 || c->ms_output_period < 1)
     return fail(MMC_ERR_CONFIG, "output periods must be >= 1");

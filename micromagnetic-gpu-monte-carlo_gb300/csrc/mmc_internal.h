@@ -220,10 +220,11 @@ cudaError_t launch_khat_store(long long count, const double2* spec64, void* khat
 
 // FP64 setup: the Newell tensor (newell.cu) and its forward transform.
 // far_r2 > 0: image offsets with squared distance >= far_r2 (m^2) use the
-// far-field expansion (newell_far.h).
+// far-field expansion (newell_far.h).  nodes: each image's sum as the 27-point
+// stencil of node values (tensor_sum = 1) instead of its 64 terms.
 cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz,
                           double pi, double* k6, int px0, int px1, int finalize, cudaStream_t st,
-                          double far_r2 = 0.0);
+                          double far_r2 = 0.0, int nodes = 0);
 // The tensor on the tensor grid -> the transform grid: offsets |o| <= n - 1
 // copied, the offsets an open axis gains by the extra padding set to 0 (the
 // convolution of n cells never reaches them).

@@ -8,8 +8,9 @@
 // (as the GPU orchestration src/main.cu:475-491 does), the 64 parity-signed
 // evaluations of the f / g potentials of src/demag_cu.h:43-71 with the
 // component argument permutations (:190-210), and the division by
-// -4 pi dx dy dz (:221-228).  One thread owns one grid point and accumulates
-// in the reference's order.  Elementary functions come from mmc_math.h and
+// -4 pi dx dy dz (:221-228).  In the term form (tensor_sum = 0) one thread
+// owns one grid point and accumulates in the reference's order; the node form
+// (k_newell_nodes, the default) groups each image's terms by lattice node.  Elementary functions come from mmc_math.h and
 // this file is compiled with -fmad=false, so the result is bit-identical to
 // the CPU oracle's.
 #include <cuda_runtime.h>
@@ -133,10 +134,106 @@ __global__ void __launch_bounds__(128) k_newell(int nxp, int nyp, int nzp, doubl
   k6[5 * np + i] = kzz;
 }
 
+// The node form (tensor_sum = 1).  Per axis the parity-signed terms over
+// (ik, il) in {0,1}^2 of the 64-term sum are the weights 2 at s = ik - il = 0
+// and -1 at s = +-1, so one image's sum at offset o is
+//   sum over s in {-1,0,1}^3 of w(sx) w(sy) w(sz) F(o + s)
+// (sx outer, sz inner; each w F exact), and the six potentials F at a
+// lattice node serve the 27 offsets around it.  A CTA owns a tile of
+// NT x NT offsets (x, y) at one z offset; per image it evaluates the six
+// potentials on the tile's nodes and one node around it (3 z layers) into
+// shared memory -- 972 nodes against 256 x 64 terms -- and each thread forms
+// its offset's 27-term sum from there and adds it to its running sum.  Image
+// offsets at least the far radius away use the far-field expansion, and a
+// tile whose every offset is that far skips its nodes.  The oracle's
+// newell_point_nodes is the same arithmetic in the same order.
+constexpr int NT = 16;
+__device__ __forceinline__ double box_min_sq(int lo, int hi, double d) {
+  if (lo <= 0 && hi >= 0) return 0.0;
+  const double v = (lo > 0 ? lo : -hi) * d;
+  return v * v;
+}
+
+__global__ void __launch_bounds__(NT * NT) k_newell_nodes(int nxp, int nyp, int nzp, double dx, double dy,
+                                                          double dz, int Px, int Py, int Pz, int px0, int px1,
+                                                          int finalize, double pi, double far_r2,
+                                                          double* __restrict__ k6, long long np) {
+  constexpr int NW = NT + 2;
+  __shared__ double F[6][3][NW][NW];
+  const int tx = threadIdx.x % NT, ty = threadIdx.x / NT;
+  const int omx = 1 - (nxp + 1) / 2, omy = 1 - (nyp + 1) / 2, omz = 1 - (nzp + 1) / 2;  // smallest offsets
+  const int bx = omx + blockIdx.x * NT, by = omy + blockIdx.y * NT;                    // the tile's first
+  const int ox = bx + tx, oy = by + ty, oz = omz + (int)blockIdx.z;
+  const bool inside = ox - omx < nxp && oy - omy < nyp;
+  const long long i = inside ? (long long)((ox + nxp) % nxp) +
+                                   (long long)nxp * ((oy + nyp) % nyp + (long long)nyp * ((oz + nzp) % nzp))
+                             : 0;
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  if (inside && px0 > -Px)
+    for (int c = 0; c < 6; ++c) k[c] = k6[c * np + i];
+  const double w1[3] = {-1.0, 2.0, -1.0};
+  for (int px = px0; px <= px1; px++)
+    for (int py = -Py; py <= Py; py++)
+      for (int pz = -Pz; pz <= Pz; pz++) {
+        const int ix = ox + px * nxp, iy = oy + py * nyp, iz = oz + pz * nzp;
+        const int ex = bx + px * nxp, ey = by + py * nyp;  // the tile's first offsets of this image
+        const bool tile_far = far_r2 > 0.0 && box_min_sq(ex, ex + NT - 1, dx) + box_min_sq(ey, ey + NT - 1, dy) +
+                                                      box_min_sq(iz, iz, dz) >= far_r2;
+        if (!tile_far) {
+          __syncthreads();  // the previous image's stencils have read F
+          for (int n = threadIdx.x; n < 3 * NW * NW; n += blockDim.x) {
+            const int lz = n / (NW * NW), r = n - lz * NW * NW, ly = r / NW, lx = r - ly * NW;
+            const double X = (ex - 1 + lx) * dx, Y = (ey - 1 + ly) * dy, Z = (iz - 1 + lz) * dz;
+            F[0][lz][ly][lx] = newell_f(X, Y, Z);
+            F[1][lz][ly][lx] = newell_g(X, Y, Z);
+            F[2][lz][ly][lx] = newell_g(X, Z, Y);
+            F[3][lz][ly][lx] = newell_f(Y, Z, X);
+            F[4][lz][ly][lx] = newell_g(Y, Z, X);
+            F[5][lz][ly][lx] = newell_f(Z, X, Y);
+          }
+          __syncthreads();
+        }
+        if (!inside) continue;
+        if (far_r2 > 0.0) {
+          const double X = ix * dx, Y = iy * dy, Z = iz * dz;
+          if (X * X + Y * Y + Z * Z >= far_r2) {
+            double r[6];
+            mmcm::newell_far_raw(X, Y, Z, dx, dy, dz, r);
+            for (int c = 0; c < 6; ++c) k[c] += r[c];
+            continue;
+          }
+        }
+        double a[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+        for (int sx = -1; sx <= 1; ++sx)
+#pragma unroll
+          for (int sy = -1; sy <= 1; ++sy)
+#pragma unroll
+            for (int sz = -1; sz <= 1; ++sz) {
+              const double w = w1[sx + 1] * w1[sy + 1] * w1[sz + 1];
+#pragma unroll
+              for (int c = 0; c < 6; ++c) a[c] += w * F[c][1 + sz][1 + ty + sy][1 + tx + sx];
+            }
+        for (int c = 0; c < 6; ++c) k[c] += a[c];
+      }
+  if (!inside) return;
+  if (finalize) {
+    const double d = -pi * 4.0 * dx * dy * dz;
+    for (int c = 0; c < 6; ++c) k[c] = k[c] / d;
+  }
+  for (int c = 0; c < 6; ++c) k6[c * np + i] = k[c];
+}
+
 }  // namespace
 
 cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz, double pi,
-                          double* k6, int px0, int px1, int finalize, cudaStream_t st, double far_r2) {
+                          double* k6, int px0, int px1, int finalize, cudaStream_t st, double far_r2, int nodes) {
+  if (nodes) {
+    dim3 grid((unsigned)((g.txp + NT - 1) / NT), (unsigned)((g.typ + NT - 1) / NT), (unsigned)g.tzp);
+    k_newell_nodes<<<grid, NT * NT, 0, st>>>(g.txp, g.typ, g.tzp, dx, dy, dz, Px, Py, Pz, px0, px1, finalize, pi,
+                                             far_r2, k6, g.tnp);
+    return cudaGetLastError();
+  }
   const int threads = 128;
   k_newell<<<(unsigned)((g.tnp + threads - 1) / threads), threads, 0, st>>>(
       g.txp, g.typ, g.tzp, dx, dy, dz, Px, Py, Pz, px0, px1, finalize, pi, far_r2, k6, g.tnp);

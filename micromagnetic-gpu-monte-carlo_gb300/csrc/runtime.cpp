@@ -735,8 +735,9 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
     } else {
       const int Px = std::max(c.pbc_x, 0), Py = std::max(c.pbc_y, 0), Pz = std::max(c.pbc_z, 0);
       // Each launch adds a slab of x images to every point's running sum; about
-      // 1e9 f/g evaluations per launch keeps launches near a second.
-      const double per_px = (double)g.tnp * (2.0 * Py + 1) * (2.0 * Pz + 1) * 384.0;
+      // 1e9 f/g evaluations per launch keeps launches near a second (384 per
+      // point and image in the term form, 6 x 972 per 256 points in the node form).
+      const double per_px = (double)g.tnp * (2.0 * Py + 1) * (2.0 * Pz + 1) * (c.tensor_sum == 1 ? 23.0 : 384.0);
       const int slab = std::max(1, (int)(1e9 / per_px));
       for (int px0 = -Px; px0 <= Px; px0 += slab) {
         if (h->stop.load()) {
@@ -745,7 +746,7 @@ int build_demag_impl(mmc_handle* h, const char* cache_dir) {
         }
         const int px1 = std::min(Px, px0 + slab - 1);
         cudaError_t e = launch_newell(g, c.dx, c.dy, c.dz, Px, Py, Pz, pi_of(&c), k6, px0, px1, px1 == Px, h->st,
-                                      far_r2(c));
+                                      far_r2(c), c.tensor_sum);
         if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
         if (e != cudaSuccess) {
           status = fail(MMC_ERR_CUDA, std::string("tensor build: ") + cudaGetErrorString(e));

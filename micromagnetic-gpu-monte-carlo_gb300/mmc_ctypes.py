@@ -55,6 +55,7 @@ class Config(ctypes.Structure):
         ("fused_band", ctypes.c_int),
         ("tensor_far_radius", ctypes.c_int),
         ("debug_h_field", ctypes.c_int),
+        ("tensor_sum", ctypes.c_int),
     ]
 
     @classmethod

@@ -211,6 +211,54 @@ void newell_point(const Lat& L, double dx, double dy, double dz, double pi, int 
   out[5] = kzz / d;
 }
 
+// The same point with each image's 64 terms grouped by lattice node: the
+// parity-signed sum over (ik, il) in {0,1}^2 per axis is, per axis, the
+// weights 2 at s = ik - il = 0 and -1 at s = +-1, so an image's sum is
+// sum_s w(sx) w(sy) w(sz) F(offset + s) over the 27 nodes s in {-1,0,1}^3
+// (sx outer, sz inner; each product w F is exact, powers of two), formed per
+// image and then added to the point's sum.  The GPU's node kernel evaluates F
+// once per node and tile; this per-point form is its arithmetic.
+void newell_point_nodes(const Lat& L, double dx, double dy, double dz, double pi, int x, int y, int z,
+                        double out[6], double far_r2 = 0.0) {
+  int idx_x = wrap_offset(x, L.nxp), idx_y = wrap_offset(y, L.nyp), idx_z = wrap_offset(z, L.nzp);
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  const double w1[3] = {-1.0, 2.0, -1.0};
+  for (int px = -L.P[0]; px <= L.P[0]; px++)
+    for (int py = -L.P[1]; py <= L.P[1]; py++)
+      for (int pz = -L.P[2]; pz <= L.P[2]; pz++) {
+        int ix = idx_x + px * L.nxp, iy = idx_y + py * L.nyp, iz = idx_z + pz * L.nzp;
+#ifndef ORACLE_LIBM
+        if (far_r2 > 0.0) {
+          const double X = ix * dx, Y = iy * dy, Z = iz * dz;
+          if (X * X + Y * Y + Z * Z >= far_r2) {
+            double r[6];
+            mmcm::newell_far_raw(X, Y, Z, dx, dy, dz, r);
+            for (int c = 0; c < 6; ++c) k[c] += r[c];
+            continue;
+          }
+        }
+#else
+        (void)far_r2;
+#endif
+        double a[6] = {0, 0, 0, 0, 0, 0};
+        for (int sx = -1; sx <= 1; ++sx)
+          for (int sy = -1; sy <= 1; ++sy)
+            for (int sz = -1; sz <= 1; ++sz) {
+              const double w = w1[sx + 1] * w1[sy + 1] * w1[sz + 1];
+              const double X = (ix + sx) * dx, Y = (iy + sy) * dy, Z = (iz + sz) * dz;
+              a[0] += w * newell_f(X, Y, Z);
+              a[1] += w * newell_g(X, Y, Z);
+              a[2] += w * newell_g(X, Z, Y);
+              a[3] += w * newell_f(Y, Z, X);
+              a[4] += w * newell_g(Y, Z, X);
+              a[5] += w * newell_f(Z, X, Y);
+            }
+        for (int c = 0; c < 6; ++c) k[c] += a[c];
+      }
+  const double d = -pi * 4.0 * dx * dy * dz;
+  for (int c = 0; c < 6; ++c) out[c] = k[c] / d;
+}
+
 // ---------------------------------------------------------------- FFT
 // Recursive mixed-radix decimation-in-time DFT (any length; prime factors
 // handled by a direct sum).  sign = -1 forward, +1 inverse (unnormalised).
@@ -496,7 +544,8 @@ int orc_newell_points(const mmc_config* c, const long* idx, long count, double* 
     const long i = idx[j];
     int x = (int)(i % L.nxp), y = (int)((i / L.nxp) % L.nyp), z = (int)(i / ((long)L.nxp * L.nyp));
     double o[6];
-    newell_point(L, c->dx, c->dy, c->dz, pi, x, y, z, o, fr2);
+    if (c->tensor_sum == 1) newell_point_nodes(L, c->dx, c->dy, c->dz, pi, x, y, z, o, fr2);
+    else newell_point(L, c->dx, c->dy, c->dz, pi, x, y, z, o, fr2);
     for (int k = 0; k < 6; ++k) out[k * count + j] = o[k];
   }
   return 0;
@@ -519,7 +568,8 @@ int orc_newell_tensor(const mmc_config* c, double* k6) {
       const double d = std::max(c->dx, std::max(c->dy, c->dz)) * (double)c->tensor_far_radius;
       fr2 = d * d;
     }
-    newell_point(L, c->dx, c->dy, c->dz, pi, x, y, z, o, fr2);
+    if (c->tensor_sum == 1) newell_point_nodes(L, c->dx, c->dy, c->dz, pi, x, y, z, o, fr2);
+    else newell_point(L, c->dx, c->dy, c->dz, pi, x, y, z, o, fr2);
     for (int k = 0; k < 6; ++k) k6[k * np + i] = o[k];
   }
   return 0;

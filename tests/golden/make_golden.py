@@ -159,7 +159,7 @@ def main():
     import mmc_ctypes as M
     import oracle_ctypes as O
     cfg = M.Config.defaults(nx=8, ny=8, nz=1, pbc_x=2, pbc_y=2, pbc_z=0, precision=64, randomseed=256,
-                            cal_demag_flag=1)
+                            cal_demag_flag=1, tensor_sum=0)
     k6 = O.tensor(cfg)
     m0 = O.init_random(cfg, 256)
     h0 = O.demag_direct(cfg, k6, m0)

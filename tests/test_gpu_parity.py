@@ -78,9 +78,13 @@ def test_tensor_matches_golden(M, case):
     np.testing.assert_allclose(k, np.array(g["K"]), rtol=0, atol=5e-13)
 
 
+@pytest.mark.parametrize("tensor_sum", [0, 1])
 @pytest.mark.parametrize("geom", sorted(GEOMS))
-def test_tensor_bitwise_equals_oracle(M, O, geom):
-    c = cfg(M, **GEOMS[geom])
+def test_tensor_bitwise_equals_oracle(M, O, geom, tensor_sum):
+    """Both forms of the image sums (0: the 64 terms in the reference's order,
+    one thread per point; 1: node values shared in tiles, k_newell_nodes)
+    equal the oracle's same form bit for bit."""
+    c = cfg(M, tensor_sum=tensor_sum, **GEOMS[geom])
     with M.Lattice(c) as lat:
         lat.build_demag()
         k = lat.tensor()
@@ -162,7 +166,7 @@ def test_fp64_decisions_bitwise_100_sweeps(M, O, geom, demag):
 def test_trajectory_fixture(M):
     z = np.load(os.path.join(GOLDEN, "trajectory_fp64.npz"))
     c = M.Config.defaults(nx=8, ny=8, nz=1, pbc_x=2, pbc_y=2, pbc_z=0, precision=64, randomseed=256,
-                          cal_demag_flag=1)
+                          cal_demag_flag=1, tensor_sum=0)
     with M.Lattice(c) as lat:
         lat.build_demag()
         assert np.array_equal(lat.tensor(), z["k6"])

@@ -171,7 +171,7 @@ def test_trajectory_fixture(M, O):
     """Regression pin: the committed oracle trajectory is reproduced."""
     z = np.load(os.path.join(GOLDEN, "trajectory_fp64.npz"))
     cfg = M.Config.defaults(nx=8, ny=8, nz=1, pbc_x=2, pbc_y=2, pbc_z=0, precision=64, randomseed=256,
-                            cal_demag_flag=1)
+                            cal_demag_flag=1, tensor_sum=0)
     k = O.tensor(cfg)
     assert np.array_equal(k, z["k6"])
     m = O.init_random(cfg, 256)

@@ -77,27 +77,31 @@ def test_fixture_records_the_reference_pi(G):
 
 @pytest.mark.parametrize("case", SMALL)
 def test_independent_oracle_tensor_equals_reference_bitwise(M, G, OL, case):
-    k = OL.tensor(_cfg(M, G, case))
+    k = OL.tensor(_cfg(M, G, case, tensor_sum=0))  # the term-by-term sums, ktensorCPU's order
     assert np.array_equal(k, G["K_" + case])
 
 
 def test_independent_oracle_tensor_equals_reference_at_config0(M, G, OL):
     """64x64x1 with 20 images in x and y: probe points, every one bit-exact."""
-    c = _cfg(M, G, "cfg0_64x64x1_pbc20")
+    c = _cfg(M, G, "cfg0_64x64x1_pbc20", tensor_sum=0)
     idx = _probe_points(64, 64, 1, 40, 5)
     got = OL.tensor_points(c, idx)
     assert np.array_equal(got, G["K_cfg0_64x64x1_pbc20"][:, idx])
 
 
+@pytest.mark.parametrize("tensor_sum", [0, 1])
 @pytest.mark.parametrize("case", SMALL)
-def test_shared_oracle_tensor_vs_reference(M, G, O, case):
+def test_shared_oracle_tensor_vs_reference(M, G, O, case, tensor_sum):
+    """The default build, term by term (0) and by lattice nodes (1, the
+    library's default), against ktensorCPU: both within the sums' rounding."""
     want = G["K_" + case]
-    k = O.tensor(_cfg(M, G, case))
+    k = O.tensor(_cfg(M, G, case, tensor_sum=tensor_sum))
     assert np.abs(k - want).max() <= SHARED_TOL[case] * np.abs(want).max()
 
 
-def test_shared_oracle_tensor_vs_reference_at_config0(M, G, O):
-    c = _cfg(M, G, "cfg0_64x64x1_pbc20")
+@pytest.mark.parametrize("tensor_sum", [0, 1])
+def test_shared_oracle_tensor_vs_reference_at_config0(M, G, O, tensor_sum):
+    c = _cfg(M, G, "cfg0_64x64x1_pbc20", tensor_sum=tensor_sum)
     want = G["K_cfg0_64x64x1_pbc20"]
     idx = _probe_points(64, 64, 1, 40, 6)
     got = O.tensor_points(c, idx)
@@ -210,8 +214,9 @@ def test_live_reference_tensor_on_random_lattices(M, OL, O):
         k_ref = R.ktensor(int(n[0]), int(n[1]), int(n[2]), *d, pbc)
         c = M.Config.defaults(nx=int(n[0]), ny=int(n[1]), nz=int(n[2]), dx=d[0], dy=d[1], dz=d[2],
                               pbc_x=int(pbc[0]), pbc_y=int(pbc[1]), pbc_z=int(pbc[2]), use_reference_pi=1)
-        assert np.array_equal(OL.tensor(c), k_ref)
-        assert np.abs(O.tensor(c) - k_ref).max() <= 5e-11 * np.abs(k_ref).max()
+        assert np.array_equal(OL.tensor(c.copy(tensor_sum=0)), k_ref)
+        for ts in (0, 1):  # both forms of the default build, within the sums' rounding
+            assert np.abs(O.tensor(c.copy(tensor_sum=ts)) - k_ref).max() <= 5e-11 * np.abs(k_ref).max()
 
 
 def test_live_reference_product_on_random_spectra(O, OL):
