@@ -438,14 +438,16 @@ def run_ours(args):
         }
         fam = dict(zip(["k_rows", "k_col_pass"], prof[:2]))
     else:
-        mc = {1: "k_mc_tile", 2: "k_mc_quad"}.get(shape[6], "k_mc_checker")  # tile: one launch, else one per colour
+        # tile / strip: both colours in one launch, else one launch per colour
+        mc = {1: "k_mc_tile", 2: "k_mc_quad", 4: "k_mc_strip"}.get(shape[6], "k_mc_checker")
+        col = "k_col_reg" if shape[8] == 2 else "k_col_pass"  # the film column pass held in registers
         kbytes = {
             "k_x_forward": R * (3 * s_ * n + 3 * 2 * s_ * nh),
-            "k_col_pass": R * 2 * (3 * 2 * s_ * nh) + 6 * 2 * s_ * nh,
+            col: R * 2 * (3 * 2 * s_ * nh) + 6 * 2 * s_ * nh,
             "k_x_inverse": R * (3 * 2 * s_ * nh + 3 * s_ * n),
             mc: R * n * 9 * s_,  # both colours: 36 B per trial
         }
-        fam = dict(zip(["k_x_forward", "k_col_pass", "k_x_inverse", mc], prof[:4]))
+        fam = dict(zip(["k_x_forward", col, "k_x_inverse", mc], prof[:4]))
     dom = max(fam, key=fam.get)
     launches = 2 if dom in ("k_mc_checker", "k_mc_quad") else 1
     per_launch_ms = fam[dom] / launches
@@ -461,7 +463,8 @@ def run_ours(args):
                           "(mmc_batch_profile_sweeps): serialised launches, an upper bound on each kernel's time "
                           "in the timed run, whose graphs overlap the kernels of the replica parts on "
                           f"{shape[9]} streams",
-                "bytes_model": "per replica: x passes 3*4*N real + 3*8*N_h complex; column pass 2*3*8*N_h "
+                "bytes_model": "per replica: x passes 3*4*N real + 3*8*N_h complex; column pass (k_col_pass or "
+                               "k_col_reg) 2*3*8*N_h "
                                "(+ 6*8*N_h shared tensor once); Metropolis 36 B per trial (both colours); row "
                                "kernel m in/out 2*3*4*N + spectrum rows in/out 2*3*8*N_h; N=65536, N_h=33024"}
     batch.close()
