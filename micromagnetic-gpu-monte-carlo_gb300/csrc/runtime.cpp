@@ -1299,6 +1299,10 @@ struct mmc_batch {
   cudaGraphExec_t gexec = nullptr;
   int graph_len = 0;
   bool graph_pt = false;
+  // tempering: the graph of one swap interval whose first sweep also makes the
+  // previous interval's swap (batch_sweep_lead)
+  cudaGraphExec_t gexec_lead = nullptr;
+  int lead_len = 0;
   std::vector<unsigned long long> acc_base;
   unsigned long long proposed = 0;
   double last_ms = 0;
@@ -1317,6 +1321,7 @@ void batch_free(mmc_batch* b) {
   if (!b) return;
   if (b->base) cudaSetDevice(b->base->device);
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  if (b->gexec_lead) cudaGraphExecDestroy(b->gexec_lead);
   if (b->fork) cudaEventDestroy(b->fork);
   for (int k = 0; k < 3; ++k) {
     if (b->joins[k]) cudaEventDestroy(b->joins[k]);
@@ -1503,12 +1508,41 @@ cudaError_t batch_sweep(mmc_batch* b, cudaEvent_t* ev, int slot, int parity) {
 // Sweep q reads counter slot q mod CTR_SLOTS; the counters advance after
 // every CTR_SLOTS sweeps and after the last one (one small launch per graph
 // of 32 sweeps instead of one per sweep).
-cudaError_t batch_sweeps(mmc_batch* b, long long k) {
+cudaError_t batch_swap(mmc_batch* b);
+cudaError_t batch_energy_kernels(mmc_batch* b, bool swap = false, bool with_demag = true);
+// The first sweep of a swap interval that also makes the previous interval's
+// swap: the demag field of m (which the sweep needs anyway) gives the
+// energies, the swap pass updates the temperatures, then the Metropolis
+// launches run -- one demag evaluation where a separate swap pass would need
+// its own.  The same energies, swaps and decisions as a swap pass followed by
+// a sweep.
+cudaError_t batch_sweep_lead(mmc_batch* b, int slot) {
+  mmc_handle* h = b->base;
+  cudaError_t e;
+  if (h->cfg.cal_demag_flag && (e = batch_demag(b)) != cudaSuccess) return e;
+  if ((e = batch_energy_kernels(b, true, false)) != cudaSuccess) return e;
+  if ((e = batch_swap(b)) != cudaSuccess) return e;
+  if (batch_strip(b))
+    return h->prec == 32 ? launch_mc_strip<float>(h->g, (const McCoef<float>*)b->coef, (const float*)b->m,
+                                                  (float*)b->m2, (const float*)b->h, b->ctr + slot, b->acc, h->st, b->R)
+                         : launch_mc_strip<double>(h->g, (const McCoef<double>*)b->coef, (const double*)b->m,
+                                                   (double*)b->m2, (const double*)b->h, b->ctr + slot, b->acc, h->st,
+                                                   b->R);
+  return h->prec == 32 ? launch_mc<float>(h->g, (const McCoef<float>*)b->coef, (float*)b->m, (const float*)b->h,
+                                          b->ctr + slot, -1, b->acc, h->st, b->R, b->tun.mc_form)
+                       : launch_mc<double>(h->g, (const McCoef<double>*)b->coef, (double*)b->m, (const double*)b->h,
+                                           b->ctr + slot, -1, b->acc, h->st, b->R, b->tun.mc_form);
+}
+
+// lead_swap: the first sweep makes the pending swap (batch_sweep_lead; the
+// pass kernels path only).
+cudaError_t batch_sweeps(mmc_batch* b, long long k, bool lead_swap = false) {
   cudaError_t e = cudaSuccess;
   for (long long q = 0; q < k && e == cudaSuccess; ++q) {
     const int slot = (int)(q % CTR_SLOTS);
-    e = b->rows_band > 0 ? batch_sweep_rows(b, (int)(q & 1), nullptr, slot)
-                         : batch_sweep(b, nullptr, slot, (int)(q & 1));
+    e = (q == 0 && lead_swap) ? batch_sweep_lead(b, slot)
+        : b->rows_band > 0    ? batch_sweep_rows(b, (int)(q & 1), nullptr, slot)
+                              : batch_sweep(b, nullptr, slot, (int)(q & 1));
     if (e == cudaSuccess && (slot == CTR_SLOTS - 1 || q == k - 1))
       e = launch_advance(b->ctr, (uint32_t)(slot + 1), b->base->st, CTR_SLOTS);
   }
@@ -1525,11 +1559,12 @@ cudaError_t batch_set_counters(mmc_batch* b, long long stage, long long sweep0) 
 
 // Energies (and <m> and the topological charge) of every replica into b->red;
 // swap = true: the energies a tempering swap needs (launch_energy, with_q = -1).
-cudaError_t batch_energy_kernels(mmc_batch* b, bool swap = false) {
+// with_demag = false: b->h already holds the demag field of b->m.
+cudaError_t batch_energy_kernels(mmc_batch* b, bool swap, bool with_demag) {
   const int with_q = swap ? -1 : 1;
   mmc_handle* h = b->base;
   cudaError_t e;
-  if (h->cfg.cal_demag_flag && (e = batch_demag(b)) != cudaSuccess) return e;
+  if (with_demag && h->cfg.cal_demag_flag && (e = batch_demag(b)) != cudaSuccess) return e;
   const bool dm = h->cfg.cal_demag_flag != 0;
   return h->prec == 32 ? launch_energy<float>(h->g, b->ecoef, (const float*)b->m, dm ? (const float*)b->h : nullptr,
                                               b->partials, h->npartials, b->red, h->st, b->R, with_q)
@@ -1545,6 +1580,37 @@ cudaError_t batch_swap(mmc_batch* b) {
 }
 
 // A graph of `len` sweeps, followed (pt) by an energy evaluation and a swap pass.
+// The graph of one swap interval of `len` sweeps whose first sweep makes the
+// pending swap (batch_sweep_lead).
+int batch_graph_lead(mmc_batch* b, int len) {
+  if (b->gexec_lead && b->lead_len == len) return MMC_OK;
+  if (b->gexec_lead) cudaGraphExecDestroy(b->gexec_lead);
+  b->gexec_lead = nullptr;
+  mmc_handle* h = b->base;
+  cudaGraph_t graph;
+  CU(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = batch_sweeps(b, len, true);
+  cudaError_t e2 = cudaStreamEndCapture(h->st, &graph);
+  if (e != cudaSuccess || e2 != cudaSuccess) cudaGetLastError();
+  if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("batch capture: ") + cudaGetErrorString(e));
+  if (e2 != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("batch capture end: ") + cudaGetErrorString(e2));
+  e = cudaGraphInstantiate(&b->gexec_lead, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(MMC_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+  b->lead_len = len;
+  return MMC_OK;
+}
+
+// Drops the captured graphs (launch shape, ladders or the state they bind changed).
+void batch_drop_graphs(mmc_batch* b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->graph_len = 0;
+  if (b->gexec_lead) cudaGraphExecDestroy(b->gexec_lead);
+  b->gexec_lead = nullptr;
+  b->lead_len = 0;
+}
+
 int batch_graph(mmc_batch* b, int len, bool pt) {
   if (b->gexec && b->graph_len == len && b->graph_pt == pt) return MMC_OK;
   if (b->gexec) cudaGraphExecDestroy(b->gexec);
@@ -1579,6 +1645,7 @@ int batch_sync_temperatures(mmc_batch* b) {
 struct BatchRun {
   long long stage = 0, sweep0 = 0, nsweeps = 0, done = 0;
   long long pieces = 0;
+  bool swap_pending = false;  // a swap interval ended; its swap not yet made
 };
 constexpr int BATCH_GRAPH_SWEEPS = 32;
 
@@ -1600,21 +1667,33 @@ int batch_run_piece(mmc_batch* b, BatchRun& r, bool* finished) {
   const int I = b->interval;
   if (r.done < r.nsweeps) {
     if (I > 0) {
-      // sweeps up to the next multiple of the swap interval, then a swap pass
+      // sweeps up to the next multiple of the swap interval, after which a
+      // swap is due; it is made by the next interval's first sweep
+      // (batch_sweep_lead, one demag evaluation less), or by a swap pass
+      // before direct sweeps or at the end of the run
       const long long s = r.sweep0 + r.done;
       const long long to_boundary = I - (s % I);
-      if (to_boundary <= r.nsweeps - r.done && to_boundary == I) {
-        TRY(batch_graph(b, I, true));
-        CU(cudaGraphLaunch(b->gexec, h->st));
+      const bool lead_ok = b->rows_band == 0;
+      if (to_boundary <= r.nsweeps - r.done && to_boundary == I && (!r.swap_pending || lead_ok)) {
+        if (r.swap_pending) {
+          TRY(batch_graph_lead(b, I));
+          CU(cudaGraphLaunch(b->gexec_lead, h->st));
+        } else {
+          TRY(batch_graph(b, I, false));
+          CU(cudaGraphLaunch(b->gexec, h->st));
+        }
         r.done += I;
+        r.swap_pending = true;
       } else {
+        if (r.swap_pending) {
+          CU(batch_energy_kernels(b, true));
+          CU(batch_swap(b));
+          r.swap_pending = false;
+        }
         const long long k = std::min(to_boundary, r.nsweeps - r.done);
         CU(batch_sweeps(b, k));
         r.done += k;
-        if (k == to_boundary) {
-          CU(batch_energy_kernels(b, true));
-          CU(batch_swap(b));
-        }
+        r.swap_pending = k == to_boundary;
       }
     } else if (r.nsweeps - r.done >= BATCH_GRAPH_SWEEPS) {
       CU(cudaGraphLaunch(b->gexec, h->st));
@@ -1629,8 +1708,13 @@ int batch_run_piece(mmc_batch* b, BatchRun& r, bool* finished) {
   return MMC_OK;
 }
 
-int batch_run_end(mmc_batch* b, const BatchRun& r) {
+int batch_run_end(mmc_batch* b, BatchRun& r) {
   mmc_handle* h = b->base;
+  if (r.swap_pending) {
+    CU(batch_energy_kernels(b, true));
+    CU(batch_swap(b));
+    r.swap_pending = false;
+  }
   CU(cudaEventRecord(h->ev[1], h->st));
   CU(cudaStreamSynchronize(h->st));
   float ms = 0;
@@ -1697,9 +1781,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     // timed the way runs execute: replays of a captured graph of
     // BATCH_GRAPH_SWEEPS sweeps with this shape
     if (e == cudaSuccess) {
-      if (b->gexec) cudaGraphExecDestroy(b->gexec);
-      b->gexec = nullptr;
-      b->graph_len = 0;
+      batch_drop_graphs(b);
       if ((status = batch_graph(b, BATCH_GRAPH_SWEEPS, false)) != MMC_OK) return;
     }
     const int reps = std::max(1, (sweeps + BATCH_GRAPH_SWEEPS - 1) / BATCH_GRAPH_SWEEPS);
@@ -1808,9 +1890,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
     e = cudaMemcpyAsync(b->acc, acc0.data(), b->R * sizeof(unsigned long long), cudaMemcpyHostToDevice, h->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
   cudaFree(saved);
-  if (b->gexec) cudaGraphExecDestroy(b->gexec);
-  b->gexec = nullptr;
-  b->graph_len = 0;
+  batch_drop_graphs(b);
   if (status != MMC_OK) return status;
   CU(e);
   if (best_ms) *best_ms = best_t;
@@ -2325,8 +2405,7 @@ int mmc_batch_set_ladders(mmc_batch* b, int nladders, int per_ladder, const int*
   b->pt.key0 = (uint32_t)((uint64_t)seed & 0xffffffffu);
   b->pt.key1 = (uint32_t)((uint64_t)seed >> 32);
   b->interval = swap_interval;
-  if (b->gexec) cudaGraphExecDestroy(b->gexec);
-  b->gexec = nullptr;
+  batch_drop_graphs(b);
   return MMC_OK;
 }
 
@@ -2433,9 +2512,7 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
   b->tun = t;
   b->rows_band = band;
   b->streams = streams;
-  if (b->gexec) cudaGraphExecDestroy(b->gexec);
-  b->gexec = nullptr;
-  b->graph_len = 0;
+  batch_drop_graphs(b);
   return MMC_OK;
 }
 

@@ -408,3 +408,34 @@ def test_parallel_tempering_fp32_swap_energies(M, O):
             assert swapped == (delta >= 0 or u < np.exp(delta)), k
             checked += 1
     assert checked >= 3 and int(cnt[0]) == K // 2
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("form", [2, 4])
+def test_tempering_swap_fused_into_next_sweep(M, prec, form):
+    """One call of 95 sweeps with swaps every 10 (graphs whose first sweep
+    makes the previous interval's swap from the demag field it computes
+    anyway) against the same sweeps in calls of 7 (separate swap passes before
+    direct sweeps): equal states, temperatures and swap counts, with the
+    vectorised (2) and strip (4) Metropolis forms."""
+    cfgs = cfgs_for(M, 6, prec, sweep_engine=1, nx=32, ny=32, pbc_x=1, pbc_y=1)
+    temps = np.array([[50.0, 80.0, 130.0, 210.0, 340.0, 550.0]])
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        for x in (a, b):
+            s = list(x.launch_shape())
+            s[6] = form
+            x.set_launch_shape(s)
+            x.set_ladders(np.arange(6).reshape(1, 6), temps, 10, 5)
+        a.run_sweeps(0, 0, 95)
+        s0 = 0
+        while s0 < 95:
+            k = min(7, 95 - s0)
+            b.run_sweeps(0, s0, k)
+            s0 += k
+        for r in range(6):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        assert np.array_equal(a.temperatures(), b.temperatures())
+        ra, ca = a.ladder_state()
+        rb, cb = b.ladder_state()
+        # 9 rounds: 5 even ones with 3 pairs, 4 odd ones with 2
+        assert np.array_equal(ra, rb) and np.array_equal(ca, cb) and int(ca[0]) == 5 * 3 + 4 * 2
