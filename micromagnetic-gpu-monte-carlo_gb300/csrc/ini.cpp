@@ -143,8 +143,8 @@ void config_defaults(mmc_config* c) {
 int config_validate(const mmc_config* c) {
   if (c->nx < 1 || c->ny < 1 || c->nz < 1)
     return fail(MMC_ERR_CONFIG, "nx, ny, nz must be >= 1");
-  if ((long long)c->nx * c->ny * c->nz > (1LL << 31))
-    return fail(MMC_ERR_CONFIG, "lattice larger than 2^31 cells");
+  if ((long long)c->nx * c->ny * c->nz >= (1LL << 31))
+    return fail(MMC_ERR_CONFIG, "lattice of 2^31 cells or more");
   if (!(c->dx > 0) || !(c->dy > 0) || !(c->dz > 0))
     return fail(MMC_ERR_CONFIG, "dx, dy, dz must be > 0");
   if (!(c->ms > 0)) return fail(MMC_ERR_CONFIG, "ms must be > 0");

@@ -1062,7 +1062,8 @@ __global__ void __launch_bounds__(256) k_mc_quad(Geom g, const McCoef<T>* __rest
   for (int u = 0; u < 2; ++u) {
     const int t = t0 + u * tstride;
     if (t < nseg * g.ny * g.nz) {
-      const int row = t / nseg, s = t - row * nseg;  // nseg is a power of two for the usual sizes; cheap either way
+      // t / (nx / 4) == (4 t) / nx: the multiply-shift divider by nx, no run-time division
+      const int row = g.dnx.div(4 * t), s = t - row * nseg;
       int z = 0, y = row;
       if constexpr (Z3) {
         z = g.dny.div(row);
@@ -1630,7 +1631,9 @@ __device__ __forceinline__ void energy_terms_at(const Geom& g, const EnCoef& e, 
   const T* mx = m;
   const T* my = m + n;
   const T* mz = m + 2 * n;
-  const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
+  // cell coordinates by the multiply-shift dividers (n < 2^31)
+  const int row = g.dnx.div((int)i), x = (int)i - row * g.nx;
+  const int z = g.dny.div(row), y = row - z * g.ny;
   const double ax = mx[i], ay = my[i], az = mz[i];
   for (int a = 0; a < 3; ++a) {
     const long long j = nbr_idx(g, x, y, z, a, 1);
@@ -1656,7 +1659,7 @@ __device__ __forceinline__ void energy_terms_at(const Geom& g, const EnCoef& e, 
   const long long i2 = nbr_idx(g, x, y, z, 0, 1);
   const long long i4 = nbr_idx(g, x, y, z, 1, 1);
   if (i2 >= 0 && i4 >= 0) {
-    const int x2 = (int)(i2 % g.nx);
+    const int x2 = (int)i2 - g.dnx.div((int)i2) * g.nx;
     const long long i3 = nbr_idx(g, x2, y, z, 1, 1);
     const long long tri[2][3] = {{i, i2, i3}, {i, i3, i4}};
     for (int t = 0; t < 2; ++t) {
@@ -1792,7 +1795,9 @@ __device__ __forceinline__ void field_at(const Geom& g, const HCoef& c, int term
   const T* mx = m;
   const T* my = m + n;
   const T* mz = m + 2 * n;
-  const int x = (int)(i % g.nx), y = (int)((i / g.nx) % g.ny), z = (int)(i / ((long long)g.nx * g.ny));
+  // cell coordinates by the multiply-shift dividers (n < 2^31)
+  const int row = g.dnx.div((int)i), x = (int)i - row * g.nx;
+  const int z = g.dny.div(row), y = row - z * g.ny;
   const double ax = mx[i], ay = my[i], az = mz[i];
   double f0 = 0, f1 = 0, f2 = 0;
   const bool all = term == 5;
