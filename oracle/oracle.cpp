@@ -4,20 +4,28 @@
 // tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg.  The
 // product (libmmc) never links, loads or calls it.
 //
-// Parity status: the reference ships no tests, golden vectors or fixtures and
-// cannot be built (its kernel bodies and helper headers are missing), so this
-// oracle is "parity unpinned" against reference outputs.  It is pinned instead
-// by: high-precision (mpmath) evaluations of the reference's Newell formulas
-// (tests/golden/), the Random123 known-answer vectors for Philox4x32-10, and
-// physics identities (self-tensor trace, local dE == global energy difference,
-// FFT convolution == direct sum).
+// Parity status: pinned to the reference's own code where the reference has
+// any.  Its complete demag arithmetic -- ktensorCPU, f, g and
+// calHexchangeKernel (src/demag_cu.cu, src/demag_cu.h) -- compiles unmodified
+// with stand-in headers (oracle/build_ref.py -> oracle/_ref); its outputs are
+// committed in tests/golden/ref_demag_golden.npz, and this file built with
+// -DORACLE_LIBM (C library functions, its own Philox) reproduces the tensor
+// and the product bit for bit (tests/test_ref_pin.py).  The reference's
+// Metropolis, energy and self-tensor kernels have no published bodies; for
+// those this file follows the physics contract below and is pinned by the
+// Random123 known-answer vectors for Philox4x32-10, high-precision (mpmath)
+// evaluations of the Newell formulas (tests/golden/) and physics identities
+// (self-tensor trace, local dE == global energy difference, FFT convolution
+// == direct sum).
 //
 // What follows the reference line by line:
 //  - newell_f / newell_g: src/demag_cu.h:43-71 (same expression order).
 //  - newell_tensor: ktensorCPU, src/demag_cu.cu:119-248 -- offset wrap
 //    (:149-151), image loops over [-max(pbc,0), max(pbc,0)] as the GPU
 //    orchestration src/main.cu:475-491 does, the 64-term parity-signed sum
-//    (:170-213) and the division by -4*pi*dx*dy*dz (:221-228).
+//    (:170-213) and the division by -4*pi*dx*dy*dz (:221-228); with
+//    tensor_sum = 1 each image's 64 terms grouped by lattice node
+//    (newell_point_nodes), the library's default form.
 //  - demag product: calHexchangeKernel, src/demag_cu.cu:68-116 (K^ . M^ / N).
 //  - padding: src/main.cu:254-263.
 // What follows the physics contract this project fixes for the missing
