@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(NT * NT) k_newell_nodes(int nxp, int nyp, int 
 
 cudaError_t launch_newell(const Geom& g, double dx, double dy, double dz, int Px, int Py, int Pz, double pi,
                           double* k6, int px0, int px1, int finalize, cudaStream_t st, double far_r2, int nodes) {
-  if (nodes) {
+  if (nodes && g.tzp <= 65535 && (g.typ + NT - 1) / NT <= 65535) {  // grid y and z limits; else the term form
     dim3 grid((unsigned)((g.txp + NT - 1) / NT), (unsigned)((g.typ + NT - 1) / NT), (unsigned)g.tzp);
     k_newell_nodes<<<grid, NT * NT, 0, st>>>(g.txp, g.typ, g.tzp, dx, dy, dz, Px, Py, Pz, px0, px1, finalize, pi,
                                              far_r2, k6, g.tnp);
