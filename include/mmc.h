@@ -86,7 +86,9 @@ typedef struct mmc_config {
   long long terminal_output_period;
   long long energy_output_period;
   long long ms_output_period;
-  int rand_block_size;                     /* accepted for compatibility; see DESIGN */
+  int rand_block_size;                     /* accepted and ignored: it sized the reference's pre-generated
+                                              random pools (src/main.cu:351-385), which counter-based
+                                              Philox proposals do not need */
   int cal_demag_flag;
   int Temperature_use_exp;                 /* 1: T *= step, 0: T -= step */
 
