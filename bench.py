@@ -526,6 +526,13 @@ def run_ours(args):
         "roofline": roofline,
         "clocks": clk.summary(),
         "gpu_launches": args.steps * launches_per_step(S, shape, R),
+        # the whole batched sweep of one rank against the same peak: every
+        # kernel's algorithmic bytes (roofline.bytes_model) over the timed
+        # region's time per sweep
+        "sweep_roofline": {"algorithmic_bytes_per_sweep": sum(kbytes.values()),
+                           "us_per_sweep": 1e6 * total / (args.steps * S),
+                           "achieved_gbs": sum(kbytes.values()) / (total / (args.steps * S)) / 1e9,
+                           "frac": sum(kbytes.values()) / (total / (args.steps * S)) / 1e9 / peak},
         "single_lattice_fp32": {"value": single_v, "unit": UNIT, "engine": single_engine,
                                 "film_engine_phase_us": phases},
         "fp64_plain": fp64_line,
