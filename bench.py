@@ -449,10 +449,25 @@ def run_ours(args):
         }
         fam = dict(zip(["k_x_forward", col, "k_x_inverse", mc], prof[:4]))
     dom = max(fam, key=fam.get)
+    # demag convolutions/s: the three pass kernels' time per batched sweep on
+    # one stream (the pass-kernel path), R convolutions per sweep; bytes per
+    # convolution in the model of the hot-path table: m in and h out
+    # (6 s N) and the half spectra of K^ . M^ (6 x 2 s N_h)
+    demag_line = None
+    if shape[5] == 0:
+        conv_ms = fam["k_x_forward"] + fam[col] + fam["k_x_inverse"]
+        conv_bytes = 6 * s_ * n + 6 * 2 * s_ * nh
+        conv_rate = R / (conv_ms * 1e-3)
+        demag_line = {"value": conv_rate, "unit": "demag convolutions/s", "replicas": R,
+                      "ms_per_batch": conv_ms, "bytes_per_convolution": conv_bytes,
+                      "achieved_gbs": conv_rate * conv_bytes / 1e9,
+                      "timing": "x forward + column + x inverse passes, CUDA events, one stream"}
     launches = 2 if dom in ("k_mc_checker", "k_mc_quad") else 1
     per_launch_ms = fam[dom] / launches
     bytes_launch = kbytes[dom] / launches
     peak, peak_kind = measured_peaks()
+    if demag_line is not None:
+        demag_line["frac"] = demag_line["achieved_gbs"] / peak
     traffic, tshape = ncu_traffic(dom, shape)
     achieved = bytes_launch / (per_launch_ms * 1e-3) / 1e9
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -526,6 +541,7 @@ def run_ours(args):
         "roofline": roofline,
         "clocks": clk.summary(),
         "gpu_launches": args.steps * launches_per_step(S, shape, R),
+        "demag_convolutions": demag_line,
         # the whole batched sweep of one rank against the same peak: every
         # kernel's algorithmic bytes (roofline.bytes_model) over the timed
         # region's time per sweep
