@@ -376,10 +376,13 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
  * pass), and the Metropolis form: 0 one launch per colour, 1 both colours of
  * a film in one tile launch, 2 one vectorised launch per colour (films with
  * nx a multiple of 4), 3 the same with each CTA's rows staged in shared
- * memory by asynchronous copies (nx also at most 1024), whether the pass kernels expand their transforms in
- * line (1) or call them out of line (0), and whether the column passes
- * transform in place reading the tensor from global memory (1), and the
- * number of streams (1-4) the batch's replicas are split over. */
+ * memory by asynchronous copies (nx also at most 1024), 4 both colours of a
+ * film in one launch over strips of rows (nx a multiple of 4, at most 2048,
+ * row kernel off), whether the pass kernels expand their transforms in
+ * line (1) or call them out of line (0), whether the column passes
+ * transform in place reading the tensor from global memory (1; 2 the same,
+ * with film y lines of length 64 or 256 held in registers, other lines as 1),
+ * and the number of streams (1-4) the batch's replicas are split over. */
 int mmc_batch_launch_shape(mmc_batch* b, int out[10]);
 /* Autotuner: times each launch shape this batch can run with (the film row
  * kernel with each band that fits; the pass kernels with 1-16 rows per x-pass
@@ -400,7 +403,8 @@ int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int*
  * of two dividing the column-pass thread count, 32-512 threads), tiles whose
  * shared memory fits 220 KB in the chosen column-pass form, a row-kernel band
  * this batch offers, a Metropolis form the lattice qualifies for, 0/1 for the
- * two transform flags and 1-4 streams; anything else is rejected.  Results do
+ * in-line transform flag, 0-2 for the column-pass form and 1-4 streams;
+ * anything else is rejected.  Results do
  * not depend on the shape.  No counterpart in the reference. */
 int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]);
 
