@@ -439,7 +439,8 @@ def run_ours(args):
         fam = dict(zip(["k_rows", "k_col_pass"], prof[:2]))
     else:
         # tile / strip: both colours in one launch, else one launch per colour
-        mc = {1: "k_mc_tile", 2: "k_mc_quad", 4: "k_mc_strip"}.get(shape[6], "k_mc_checker")
+        mc = {1: "k_mc_tile", 2: "k_mc_quad", 3: "k_mc_band", 4: "k_mc_strip", 5: "k_mc_pipe"}.get(shape[6],
+                                                                                                  "k_mc_checker")
         col = "k_col_reg" if shape[8] == 2 else "k_col_pass"  # the film column pass held in registers
         kbytes = {
             "k_x_forward": R * (3 * s_ * n + 3 * 2 * s_ * nh),
@@ -462,7 +463,7 @@ def run_ours(args):
                       "ms_per_batch": conv_ms, "bytes_per_convolution": conv_bytes,
                       "achieved_gbs": conv_rate * conv_bytes / 1e9,
                       "timing": "x forward + column + x inverse passes, CUDA events, one stream"}
-    launches = 2 if dom in ("k_mc_checker", "k_mc_quad") else 1
+    launches = 2 if dom in ("k_mc_checker", "k_mc_quad", "k_mc_band", "k_mc_pipe") else 1
     per_launch_ms = fam[dom] / launches
     bytes_launch = kbytes[dom] / launches
     peak, peak_kind = measured_peaks()

@@ -378,7 +378,9 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
  * nx a multiple of 4), 3 the same with each CTA's rows staged in shared
  * memory by asynchronous copies (nx also at most 1024), 4 both colours of a
  * film in one launch over strips of rows (nx a multiple of 4, at most 2048,
- * row kernel off), whether the pass kernels expand their transforms in
+ * row kernel off), 5 the staged form run by persistent CTAs with the rows
+ * fetched by bulk asynchronous copies (as 3; a run whose buffer wait runs out
+ * of its time limit returns MMC_ERR_TIMEOUT), whether the pass kernels expand their transforms in
  * line (1) or call them out of line (0), whether the column passes
  * transform in place reading the tensor from global memory (1; 2 the same,
  * with film y lines of length 64 or 256 held in registers, other lines as 1),
@@ -446,6 +448,16 @@ int mmc_ovf_write(const char* path, int nx, int ny, int nz, double dx, double dy
  * MMC_OK if the wait had completed).  The device stays usable afterwards --
  * this is how the film engine's barriers report MMC_ERR_TIMEOUT. */
 int mmc_selftest_barrier_timeout(int device, long long spin_limit, int* status);
+
+/* Test hook of failure detection (no counterpart in the reference): one
+ * thread waits on a shared-memory transaction barrier (mbarrier) that expects
+ * an arrival that never comes -- the wait the pipelined Metropolis form makes
+ * for its staged rows -- for at most limit_ns nanoseconds (1 .. 1e9) of the
+ * device's global timer; *status receives MMC_ERR_TIMEOUT when the wait gave
+ * up (MMC_OK if it had completed).  No copy is in flight, and the device stays
+ * usable afterwards.  A run whose pipelined buffer wait gives up returns
+ * MMC_ERR_TIMEOUT the same way. */
+int mmc_selftest_mbar_timeout(int device, long long limit_ns, int* status);
 
 /* Test hook (no counterpart in the reference, whose random pools came from
  * cuRAND's host API, src/main.cu:351-385): evaluates Philox4x32-10 on device

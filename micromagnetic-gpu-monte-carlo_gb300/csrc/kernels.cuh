@@ -1168,6 +1168,64 @@ inline int mc_band_rows(const Geom& g, int threads) {
   return band;
 }
 
+// The decisions of this colour on rows y0 .. y0+nb-1 of one replica from rows
+// staged in shared memory -- ms[slot][comp][x] with slot s = row y0-1+s, hs
+// [row][comp][x] (read when dm) -- the CTA's threads striding over the rows'
+// 4-cell segments (k_mc_quad's per-thread work, the same quad_cells); the
+// segments that changed are stored to m (this replica's), and accepts are
+// added to mine.
+template <typename T, bool ALLB>
+__device__ __forceinline__ void band_segments(const Geom& g, const McCoef<T>& c, const T* ms, const T* hs,
+                                              T* __restrict__ m, int y0, int nb, int color, bool dm,
+                                              const FastDiv& dseg, uint32_t stage, uint32_t sweep,
+                                              unsigned int& mine) {
+  const int nx = g.nx, ny = g.ny;
+  const long long n = g.n;
+  const int nseg = (int)dseg.d;
+  for (int t = threadIdx.x; t < nb * nseg; t += blockDim.x) {
+    const int rr = dseg.div(t), s = t - rr * nseg;
+    const int y = y0 + rr;
+    const int x0 = 4 * s;
+    bool hu = true, hd = true;
+    if (y + 1 >= ny && !g.per[1]) hu = false;
+    if (y - 1 < 0 && !g.per[1]) hd = false;
+    if (ny == 1) hu = hd = false;
+    int xl = x0 - 1, xr = x0 + 4;
+    bool hl = true, hr = true;
+    if (xl < 0) { if (g.per[0]) xl += nx; else hl = false; }
+    if (xr >= nx) { if (g.per[0]) xr -= nx; else hr = false; }
+    if constexpr (ALLB) hu = hd = hl = hr = true;
+    const int p0 = (color + y) & 1;
+    const T* own_r = ms + (size_t)(rr + 1) * 3 * nx;
+    const T* up_r = own_r + 3 * nx;
+    const T* dn_r = own_r - 3 * nx;
+    Vec4<T> own[3], up[3], dn[3], hh[3];
+    T lft[3], rgt[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      own[k] = ld4<T>(own_r + k * nx + x0);
+      up[k] = hu ? ld4<T>(up_r + k * nx + x0) : own[k];
+      dn[k] = hd ? ld4<T>(dn_r + k * nx + x0) : own[k];
+      lft[k] = (hl && p0 == 0) ? own_r[k * nx + xl] : (T)0;
+      rgt[k] = (hr && p0 == 1) ? own_r[k * nx + xr] : (T)0;
+      if (dm) hh[k] = ld4<T>(hs + ((size_t)rr * 3 + k) * nx + x0);
+      else hh[k].v[0] = hh[k].v[1] = hh[k].v[2] = hh[k].v[3] = (T)0;
+    }
+    const long long rowb = (long long)y * nx;
+    bool changed;
+    if (p0 == 0)
+      changed = quad_cells<T, 0, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), stage,
+                                       sweep, mine, own, own, false, false);
+    else
+      changed = quad_cells<T, 1, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), stage,
+                                       sweep, mine, own, own, false, false);
+    if (changed) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) st4<T>(m + k * n + rowb + x0, own[k]);
+    }
+  }
+}
+
 // (Three CTAs of 256 threads per SM in FP32 -- 80 registers, a few spilled
 // -- and two in FP64.)
 template <typename T, bool ALLB>
@@ -1208,54 +1266,218 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_mc_band(Geom g,
   }
   cp_async_wait_all();
   __syncthreads();
-  const int nseg = (int)dseg.d;
   unsigned int mine = 0;
-  for (int t = threadIdx.x; t < nb * nseg; t += blockDim.x) {
-    const int rr = dseg.div(t), s = t - rr * nseg;
-    const int y = y0 + rr;
-    const int x0 = 4 * s;
-    bool hu = true, hd = true;
-    if (y + 1 >= ny && !g.per[1]) hu = false;
-    if (y - 1 < 0 && !g.per[1]) hd = false;
-    if (ny == 1) hu = hd = false;
-    int xl = x0 - 1, xr = x0 + 4;
-    bool hl = true, hr = true;
-    if (xl < 0) { if (g.per[0]) xl += nx; else hl = false; }
-    if (xr >= nx) { if (g.per[0]) xr -= nx; else hr = false; }
-    if constexpr (ALLB) hu = hd = hl = hr = true;
-    const int p0 = (color + y) & 1;
-    const T* own_r = ms + (size_t)(rr + 1) * 3 * nx;
-    const T* up_r = own_r + 3 * nx;
-    const T* dn_r = own_r - 3 * nx;
-    Vec4<T> own[3], up[3], dn[3], hh[3];
-    T lft[3], rgt[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      own[k] = ld4<T>(own_r + k * nx + x0);
-      up[k] = hu ? ld4<T>(up_r + k * nx + x0) : own[k];
-      dn[k] = hd ? ld4<T>(dn_r + k * nx + x0) : own[k];
-      lft[k] = (hl && p0 == 0) ? own_r[k * nx + xl] : (T)0;
-      rgt[k] = (hr && p0 == 1) ? own_r[k * nx + xr] : (T)0;
-      if (dm) hh[k] = ld4<T>(hs + ((size_t)rr * 3 + k) * nx + x0);
-      else hh[k].v[0] = hh[k].v[1] = hh[k].v[2] = hh[k].v[3] = (T)0;
-    }
-    const long long rowb = (long long)y * nx;
-    bool changed;
-    if (p0 == 0)
-      changed = quad_cells<T, 0, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
-                                 ctr->sweep, mine, own, own, false, false);
-    else
-      changed = quad_cells<T, 1, ALLB>(c, own, up, dn, lft, rgt, hh, hl, hr, hd, hu, (uint32_t)(rowb + x0), ctr->stage,
-                                 ctr->sweep, mine, own, own, false, false);
-    if (changed) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) st4<T>(m + k * n + rowb + x0, own[k]);
-    }
-  }
+  band_segments<T, ALLB>(g, c, ms, hs, m, y0, nb, color, dm, dseg, ctr->stage, ctr->sweep, mine);
   unsigned int v = mine;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0 && v) atomicAdd(acc, (unsigned long long)v);
+}
+
+// ---------------------------------------------- pipelined staged Metropolis
+// One colour of a two-colour film sweep (the k_mc_band lattices) by
+// persistent CTAs.  Work items are (replica, band of rows); CTA b takes the
+// items [b chunk, (b + 1) chunk), consecutive bands of one replica, so its
+// coefficients change rarely.  A band's rows -- m rows y0-1 .. y0+nb (wrapped
+// on a periodic axis) and h rows y0 .. y0+nb-1, whole rows of one component
+// each -- are fetched by bulk asynchronous copies (cp.async.bulk, the TMA
+// engine) into one of nst (2-4) shared-memory buffers, their completion
+// counted by that buffer's mbarrier (transaction bytes).  Warp 0 issues the
+// copies of item i + nst as soon as item i's buffer is free (after the CTA
+// barrier that ends item i), so the loads of later bands land while the CTA
+// decides the current ones: no registers or issue slots spent on copying, and
+// none of the load latency on the decisions' critical path.  Every warp waits
+// on its buffer's mbarrier itself, so no warp waits for the producer's
+// issuing; the producer reads the next item's replica flag (demag on or off)
+// before the decisions, so its latency is hidden too.  The decisions are
+// band_segments', i.e. k_mc_band's and k_mc_quad's (same quad_cells on the
+// same inputs).  Measured at 32 x 256^2 in FP32: 49 us per batched sweep
+// against k_mc_quad's 30.7 -- 128 registers hold 2 CTAs (16 warps) per SM at
+// 36-39 % issue, against k_mc_quad's 24 warps at 54 %, the top stall being
+// the barrier that ends each item (ncu); taking the loads off the decisions'
+// path does not pay where the decisions themselves are latency- and
+// issue-bound and k_mc_quad's warps already hide its L2 loads.  Two segments
+// per thread unrolled together: 51 us.  It is an autotuner candidate.
+//
+// Every wait on a buffer is bounded (MCP_WAIT_NS of the global timer): a warp
+// whose wait runs out sets the CTA's abort flag and *err; after the item's
+// barrier the CTA skips the remaining items, thread 0 waits (bounded again)
+// for the copies still in flight, and the CTA returns; the host reads *err
+// after the run.
+constexpr int MCP_THREADS = 256;
+constexpr int MCP_MIN_STAGES = 2;
+constexpr int MCP_MAX_STAGES = 3;
+constexpr int MCP_HDR = 128;  // bytes ahead of the stage buffers: the mbarriers, the abort flag
+constexpr unsigned long long MCP_WAIT_NS = 2000000000ull;
+__host__ __device__ inline bool mc_pipe_ok(const Geom& g) { return mc_band_ok(g); }
+// rows per band: one 4-cell segment per thread (two, unrolled together so
+// that their decisions interleave, measured no faster and spilled)
+inline int mc_pipe_rows(const Geom& g) { return std::max(1, std::min(g.ny, 4 * MCP_THREADS / g.nx)); }
+// elements of one stage buffer: m rows y0-1 .. y0+band, h rows y0 .. y0+band-1
+__host__ __device__ inline size_t mc_pipe_stage_elems(const Geom& g, int band) {
+  return (size_t)(2 * band + 2) * 3 * g.nx;
+}
+template <typename T>
+inline size_t mc_pipe_smem(const Geom& g, int nst = MCP_MIN_STAGES) {
+  return MCP_HDR + nst * mc_pipe_stage_elems(g, mc_pipe_rows(g)) * sizeof(T);
+}
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+__device__ __forceinline__ unsigned long long mcp_now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+// Waits until the phase with the given parity has completed, at most limit_ns.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = mcp_now_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (mcp_now_ns() - t0 > limit_ns) return false;
+  return true;
+}
+// Bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned) from
+// global to shared memory, completing as transaction bytes on bar.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// Warp 0: the copies of item i into buffer `buf` (see k_mc_pipe); dm: the
+// item's replica has demag on (its h rows are needed).
+template <typename T>
+__device__ __forceinline__ void mc_pipe_issue(const Geom& g, const T* m, const T* h, int i, int band, int nbands,
+                                              bool dm, T* buf, uint64_t* bar) {
+  const int nx = g.nx, ny = g.ny;
+  const long long n = g.n;
+  const int r = i / nbands;
+  const int y0 = (i - r * nbands) * band;
+  const int nb = min(band, ny - y0);
+  const bool wrap = g.per[1] && ny > 1;
+  const int lo = (y0 > 0 || wrap) ? 0 : 1;             // first m slot present
+  const int hi = (y0 + nb < ny || wrap) ? nb + 1 : nb;  // last m slot present
+  const int nm = 3 * (hi - lo + 1), nh = dm ? 3 * nb : 0;
+  const unsigned rowb = (unsigned)(nx * sizeof(T));
+  const T* mr = m + (long long)r * 3 * n;
+  const T* hr = h + (long long)r * 3 * n;
+  T* hs = buf + (size_t)(band + 2) * 3 * nx;
+  const int lane = threadIdx.x & 31;
+  // the CTA's reads of this buffer (ordered before by a barrier) come before
+  // the copies that overwrite it
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (lane == 0) mbar_arrive_expect_tx(bar, (unsigned)(nm + nh) * rowb);
+  __syncwarp();
+  for (int q = lane; q < nm + nh; q += 32) {
+    if (q < nm) {
+      const int slot = lo + q / 3, comp = q - (q / 3) * 3;
+      int y = y0 - 1 + slot;
+      if (y < 0) y += ny;
+      else if (y >= ny) y -= ny;
+      bulk_g2s(buf + ((size_t)slot * 3 + comp) * nx, mr + comp * n + (long long)y * nx, rowb, bar);
+    } else {
+      const int j = q - nm, rr = j / 3, comp = j - rr * 3;
+      bulk_g2s(hs + ((size_t)rr * 3 + comp) * nx, hr + comp * n + (long long)(y0 + rr) * nx, rowb, bar);
+    }
+  }
+}
+
+__device__ __forceinline__ void flush_accepts(unsigned int& mine, unsigned long long* counter) {
+  unsigned int v = mine;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v) atomicAdd(counter, (unsigned long long)v);
+  mine = 0;
+}
+
+// m, h, acc and cp cover every replica (items = replicas x nbands); nst
+// buffers (MCP_MIN_STAGES .. MCP_MAX_STAGES).
+template <typename T, bool ALLB>
+__global__ void __launch_bounds__(MCP_THREADS, 2)
+    k_mc_pipe(Geom g, const McCoef<T>* __restrict__ cp, T* __restrict__ m, const T* __restrict__ h,
+              const SweepCounters* __restrict__ ctr, int color, int band, int nbands, int items, int chunk, int nst,
+              FastDiv dseg, unsigned long long* acc, int* err) {
+  // no static shared memory: the dynamic limit is raised to the device's whole
+  // opt-in size
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw);
+  volatile int& abort_s = *reinterpret_cast<int*>(smem_raw + 64);
+  T* buf0 = reinterpret_cast<T*>(smem_raw + MCP_HDR);
+  const size_t selems = mc_pipe_stage_elems(g, band);
+  const long long n = g.n;
+  const int i0 = blockIdx.x * chunk, i1 = min(items, i0 + chunk);
+  if (i0 >= i1) return;
+  const bool producer = threadIdx.x < 32;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < nst; ++s) mbar_init(&bars[s], 1);
+    abort_s = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  pdl_wait();  // m and h are the previous kernels' output
+  if (producer)
+    for (int k = 0; k < nst && i0 + k < i1; ++k)
+      mc_pipe_issue<T>(g, m, h, i0 + k, band, nbands, cp[(i0 + k) / nbands].cd != (T)0, buf0 + k * selems,
+                       &bars[k]);
+  const uint32_t stage = ctr->stage, sweep = ctr->sweep;
+  McCoef<T> c;
+  int rc = -1;
+  unsigned int mine = 0;
+  int failed = -1;  // the item whose wait ran out
+  for (int i = i0; i < i1; ++i) {
+    const int k = i - i0, s = k % nst;
+    const int inext = i + nst;
+    const bool dm_next = producer && inext < i1 && cp[inext / nbands].cd != (T)0;
+    // warp-uniform: every lane sees the phase complete, or the warp gives up
+    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bars[s], (unsigned)(k / nst) & 1u, MCP_WAIT_NS));
+    if (!ok) {
+      abort_s = 1;
+    } else {
+      const int r = i / nbands, y0 = (i - r * nbands) * band;
+      if (r != rc) {
+        if (rc >= 0) flush_accepts(mine, acc + rc);
+        rc = r;
+        c = cp[r];
+      }
+      const T* ms = buf0 + s * selems;
+      band_segments<T, ALLB>(g, c, ms, ms + (size_t)(band + 2) * 3 * g.nx, m + (long long)r * 3 * n, y0,
+                             min(band, g.ny - y0), color, c.cd != (T)0, dseg, stage, sweep, mine);
+    }
+    __syncthreads();  // buffer s is free; abort_s is final for this item
+    if (abort_s) {
+      failed = i;
+      break;
+    }
+    if (producer && inext < i1) mc_pipe_issue<T>(g, m, h, inext, band, nbands, dm_next, buf0 + s * selems, &bars[s]);
+  }
+  if (rc >= 0) flush_accepts(mine, acc + rc);
+  if (failed >= 0 && threadIdx.x == 0) {
+    atomicExch(err, 1);
+    // the copies still in flight: items failed .. failed + nst - 1
+    for (int i = failed; i < min(i1, failed + nst); ++i) {
+      const int k = i - i0;
+      mbar_wait_bounded(&bars[k % nst], (unsigned)(k / nst) & 1u, MCP_WAIT_NS);
+    }
+  }
 }
 
 // Both colours of a two-colour film sweep (nz = 1) in one launch.  A CTA owns
@@ -1970,6 +2192,12 @@ cudaError_t prepare_impl(int max_dyn_smem) {
                                     max_dyn_smem));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_strip<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     max_dyn_smem));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_pipe<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    max_dyn_smem));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_pipe<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    max_dyn_smem));
+  // the error word's address, looked up now rather than during a graph capture
+  if (!mc_pipe_err_word()) return cudaErrorInvalidDevice;
   return cudaSuccess;
 }
 
@@ -2105,6 +2333,38 @@ cudaError_t mc_impl(const Geom& g, const McCoef<T>* c, T* m, const T* h, const S
     }
     for (int col = 0; col < g.ncolors; ++col) MMC_TRY(mc_impl<T>(g, c, m, h, ctr, col, acc, st, nrep, form));
     return cudaSuccess;
+  }
+  if (form == MC_FORM_PIPE && mc_pipe_ok(g)) {
+    const int band = mc_pipe_rows(g);
+    const int nbands = (g.ny + band - 1) / band;
+    const long long items = (long long)nrep * nbands;
+    auto kern = mc_all_bonds(g) ? k_mc_pipe<T, true> : k_mc_pipe<T, false>;
+    int* err = mc_pipe_err_word();
+    // the bulk copies need 16-byte aligned rows: nx * sizeof(T) is a multiple
+    // of 16 (nx % 4 == 0), so aligned bases suffice
+    if (!err || items > INT_MAX || ((uintptr_t)m | (uintptr_t)h) % 16 != 0) return cudaErrorInvalidValue;
+    int dev = 0, nsm = 0, optin = 0, per_sm = 0;
+    MMC_TRY(cudaGetDevice(&dev));
+    MMC_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    MMC_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    // as many buffers as keep the CTAs per SM the registers allow (at most
+    // MCP_MAX_STAGES, at least MCP_MIN_STAGES)
+    int nst = MCP_MIN_STAGES;
+    MMC_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, MCP_THREADS, mc_pipe_smem<T>(g, nst)));
+    for (int k = nst + 1; k <= MCP_MAX_STAGES && mc_pipe_smem<T>(g, k) <= (size_t)optin; ++k) {
+      int q = 0;
+      MMC_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&q, kern, MCP_THREADS, mc_pipe_smem<T>(g, k)));
+      if (q < per_sm) break;
+      nst = k;
+    }
+    const size_t smem = mc_pipe_smem<T>(g, nst);
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    // a static chunk of consecutive items per CTA, every CTA resident at once
+    const long long ctas = (long long)nsm * per_sm;
+    const int chunk = (int)((items + ctas - 1) / ctas);
+    const int grid = (int)((items + chunk - 1) / chunk);
+    return launch_pdl(kern, dim3(grid), dim3(MCP_THREADS), smem, st, g, c, m, h, ctr, color, band, nbands,
+                      (int)items, chunk, nst, FastDiv((uint32_t)(g.nx / 4)), acc, err);
   }
   if (form == MC_FORM_BAND && mc_band_ok(g)) {
     const int band = mc_band_rows<T>(g, threads);

@@ -4,6 +4,8 @@
 // the CPU oracle built with -ffp-contract=off.
 #include <curand_kernel.h>
 
+#include <atomic>
+
 #include "coef.h"
 #include "fused2d.cuh"
 #include "grad.cuh"
@@ -18,6 +20,10 @@ bool mc_band_eligible(const Geom& g) { return mc_band_ok(g); }
 bool mc_strip_eligible(const Geom& g) { return mc_strip_ok(g); }
 size_t mc_strip_smem_bytes(const Geom& g, size_t real_size) {
   return real_size == 4 ? mc_strip_smem<float>(g) : mc_strip_smem<double>(g);
+}
+bool mc_pipe_eligible(const Geom& g) { return mc_pipe_ok(g); }
+size_t mc_pipe_smem_bytes(const Geom& g, size_t real_size) {
+  return real_size == 4 ? mc_pipe_smem<float>(g) : mc_pipe_smem<double>(g);
 }
 MMC_INSTANTIATE_FUSED(double)
 MMC_INSTANTIATE_GRAD(double)
@@ -40,6 +46,49 @@ static __global__ void k_barrier_timeout_selftest(GridBarrier* bar, unsigned lon
 cudaError_t launch_barrier_timeout_selftest(void* bar, unsigned long long spin_limit, int* ok_out) {
   k_barrier_timeout_selftest<<<1, 32>>>(reinterpret_cast<GridBarrier*>(bar), spin_limit, ok_out);
   return cudaGetLastError();
+}
+
+// Failure-detection self-test of k_mc_pipe's bounded buffer wait: an mbarrier
+// that expects one arrival that never comes (and no copy), so the wait can
+// only end by its time limit.
+static __global__ void k_mbar_timeout_selftest(unsigned long long limit_ns, int* timed_out) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    *timed_out = mbar_wait_bounded(&bar, 0u, limit_ns) ? 0 : 1;
+  }
+}
+
+cudaError_t launch_mbar_timeout_selftest(unsigned long long limit_ns, int* timed_out) {
+  k_mbar_timeout_selftest<<<1, 32>>>(limit_ns, timed_out);
+  return cudaGetLastError();
+}
+
+// k_mc_pipe's error word (one per device): set by a CTA whose buffer wait ran
+// out of its time limit.
+__device__ int g_mc_pipe_err;
+
+int* mc_pipe_err_word() {
+  static std::atomic<int*> words[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  int* p = words[dev].load();
+  if (!p) {
+    void* a = nullptr;
+    if (cudaGetSymbolAddress(&a, g_mc_pipe_err) != cudaSuccess) return nullptr;
+    p = static_cast<int*>(a);
+    words[dev].store(p);
+  }
+  return p;
+}
+
+int mc_pipe_error_take() {
+  int* p = mc_pipe_err_word();
+  int v = 0;
+  if (!p || cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+  if (v) cudaMemset(p, 0, sizeof(int));
+  return v;
 }
 
 // Forward transform of the six real tensor blocks k6[c][z][y][x] (padded

@@ -164,7 +164,17 @@ cudaError_t launch_demag(const Geom& g, const FftPlan& px, const FftPlan& py, co
 // memory by asynchronous copies.)  MC_FORM_STRIP: both colours of a film in
 // one launch by strips of rows, reading m from one buffer and writing the
 // other (launch_mc_strip; the batch alternates its two copies of m).
-enum : int { MC_FORM_SCALAR = 0, MC_FORM_TILE = 1, MC_FORM_QUAD = 2, MC_FORM_BAND = 3, MC_FORM_STRIP = 4 };
+// MC_FORM_PIPE: one colour per launch by persistent CTAs, each band's rows
+// staged by bulk asynchronous copies into a ring of shared-memory buffers
+// (k_mc_pipe).
+enum : int {
+  MC_FORM_SCALAR = 0,
+  MC_FORM_TILE = 1,
+  MC_FORM_QUAD = 2,
+  MC_FORM_BAND = 3,
+  MC_FORM_STRIP = 4,
+  MC_FORM_PIPE = 5
+};
 // color < 0: every colour of the sweep in the given form (falls back to the
 // scalar form where the lattice does not qualify).
 template <typename T>
@@ -176,6 +186,12 @@ bool mc_quad_eligible(const Geom& g);
 bool mc_band_eligible(const Geom& g);
 bool mc_strip_eligible(const Geom& g);
 size_t mc_strip_smem_bytes(const Geom& g, size_t real_size);
+bool mc_pipe_eligible(const Geom& g);
+size_t mc_pipe_smem_bytes(const Geom& g, size_t real_size);
+// k_mc_pipe's device error word on the current device (its address, cached),
+// and its value, cleared when set (synchronous).
+int* mc_pipe_err_word();
+int mc_pipe_error_take();
 // One sweep (both colours) in the strip form: m_in -> m_out (distinct buffers).
 template <typename T>
 cudaError_t launch_mc_strip(const Geom& g, const McCoef<T>* c, const T* m_in, T* m_out, const T* h,
@@ -302,5 +318,8 @@ cudaError_t launch_pt_swap(const PtDevice& pt, const McParams* params, McCoef<T>
 int grid_barrier_error(const GridBarrier* host_copy);
 // Test hook: a barrier wait that can only run out (see mmc_selftest_barrier_timeout).
 cudaError_t launch_barrier_timeout_selftest(void* bar, unsigned long long spin_limit, int* ok_out);
+// Test hook: k_mc_pipe's bounded buffer wait on an mbarrier that never
+// completes (see mmc_selftest_mbar_timeout).
+cudaError_t launch_mbar_timeout_selftest(unsigned long long limit_ns, int* timed_out);
 
 }  // namespace mmc

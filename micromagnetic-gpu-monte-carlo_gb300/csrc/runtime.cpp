@@ -1717,6 +1717,8 @@ int batch_run_end(mmc_batch* b, BatchRun& r) {
   }
   CU(cudaEventRecord(h->ev[1], h->st));
   CU(cudaStreamSynchronize(h->st));
+  if (b->tun.mc_form == MC_FORM_PIPE && mc_pipe_error_take())
+    return fail(MMC_ERR_TIMEOUT, "a pipelined Metropolis buffer wait ran out of its time limit");
   float ms = 0;
   CU(cudaEventElapsedTime(&ms, h->ev[0], h->ev[1]));
   b->last_ms = ms;
@@ -1853,6 +1855,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   {
     std::vector<int> forms;
     if (mc_strip_eligible(g) && mc_strip_smem_bytes(g, h->tsize) <= smem_limit()) forms.push_back(MC_FORM_STRIP);
+    if (mc_pipe_eligible(g) && mc_pipe_smem_bytes(g, h->tsize) <= smem_limit()) forms.push_back(MC_FORM_PIPE);
     if (mc_quad_eligible(g)) forms.push_back(MC_FORM_QUAD);
     if (mc_band_eligible(g)) forms.push_back(MC_FORM_BAND);
     if (mc_tile_eligible(g)) forms.push_back(MC_FORM_TILE);
@@ -1893,6 +1896,7 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
   batch_drop_graphs(b);
   if (status != MMC_OK) return status;
   CU(e);
+  if (mc_pipe_error_take()) return fail(MMC_ERR_TIMEOUT, "a pipelined Metropolis buffer wait ran out of its time limit");
   if (best_ms) *best_ms = best_t;
   if (ncand) *ncand = tried;
   return MMC_OK;
@@ -2216,6 +2220,22 @@ int mmc_selftest_barrier_timeout(int device, long long spin_limit, int* status) 
   return MMC_OK;
 }
 
+int mmc_selftest_mbar_timeout(int device, long long limit_ns, int* status) {
+  if (!status || limit_ns < 1 || limit_ns > 1000000000ll) return fail(MMC_ERR_INVALID, "bad argument");
+  CU(cudaSetDevice(device));
+  int* flag = nullptr;
+  CU(cudaMalloc(&flag, sizeof(int)));
+  cudaError_t e = cudaMemset(flag, 0xff, sizeof(int));
+  if (e == cudaSuccess) e = launch_mbar_timeout_selftest((unsigned long long)limit_ns, flag);
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  int v = -1;
+  if (e == cudaSuccess) e = cudaMemcpy(&v, flag, sizeof(int), cudaMemcpyDeviceToHost);
+  cudaFree(flag);
+  CU(e);
+  *status = v == 1 ? MMC_ERR_TIMEOUT : MMC_OK;
+  return MMC_OK;
+}
+
 int mmc_selftest_philox(int device, long long n, const uint32_t* ctr, uint32_t k0, uint32_t k1, uint32_t* out,
                         uint32_t* out_curand) {
   if (n < 0 || (n > 0 && !ctr)) return fail(MMC_ERR_INVALID, "bad argument");
@@ -2496,11 +2516,12 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
       t.col_threads % t.col_tx != 0 ||
       t.col_threads % t.col_tx_z != 0 ||
       (t.x_threads != 128 && t.x_threads != 256) || t.col_threads < 32 || t.col_threads > 512 ||
-      t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_STRIP ||
+      t.col_threads % 32 != 0 || t.mc_form < MC_FORM_SCALAR || t.mc_form > MC_FORM_PIPE ||
       (t.mc_form == MC_FORM_TILE && !mc_tile_eligible(g)) || (t.mc_form == MC_FORM_QUAD && !mc_quad_eligible(g)) ||
       (t.mc_form == MC_FORM_BAND && !mc_band_eligible(g)) ||
       (t.mc_form == MC_FORM_STRIP && (!mc_strip_eligible(g) || shape[5] != 0 ||
                                       mc_strip_smem_bytes(g, h->tsize) > smem_limit())) ||
+      (t.mc_form == MC_FORM_PIPE && (!mc_pipe_eligible(g) || mc_pipe_smem_bytes(g, h->tsize) > smem_limit())) ||
       (t.fft_inline != 0 && t.fft_inline != 1) || t.col_lean < 0 || t.col_lean > 2)
     return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
   if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())

@@ -187,6 +187,8 @@ def lib(path=None):
         "mmc_farm_request_stop": (None, [H]),
         "mmc_selftest_barrier_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong,
                                                         ctypes.POINTER(ctypes.c_int)]),
+        "mmc_selftest_mbar_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong,
+                                                     ctypes.POINTER(ctypes.c_int)]),
         "mmc_batch_request_stop": (None, [H]),
         "mmc_batch_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
         "mmc_batch_set_m": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),

@@ -83,12 +83,12 @@ TILE_GEOMS = [dict(nx=64, ny=64, pbc_x=1, pbc_y=1), dict(nx=96, ny=41, pbc_x=1, 
 
 
 def form_ok(geom, form):
-    """Eligibility of the tile (1), vector (2), staged vector (3) and strip (4)
-    forms for a two-colour film."""
+    """Eligibility of the tile (1), vector (2), staged vector (3), strip (4)
+    and pipelined staged (5) forms for a two-colour film."""
     nx, ny = geom["nx"], geom["ny"]
     if form in (2, 4):
         return nx % 4 == 0
-    if form == 3:
+    if form in (3, 5):
         return nx % 4 == 0 and nx <= 1024
     per_ok = lambda n, p: p == 0 or (n % 32 == 0 and n >= 64)
     return per_ok(nx, geom.get("pbc_x", 2)) and per_ok(ny, geom.get("pbc_y", 1))
@@ -96,14 +96,16 @@ def form_ok(geom, form):
 
 @pytest.mark.parametrize("prec", [32, 64])
 @pytest.mark.parametrize("geom", TILE_GEOMS)
-@pytest.mark.parametrize("form", [1, 2, 3, 4])
+@pytest.mark.parametrize("form", [1, 2, 3, 4, 5])
 def test_mc_forms_bitwise_equal_scalar_kernels(M, prec, geom, form):
     """Both colours in one tile launch (ring of colour-0 cells recomputed), the
     vectorised per-colour form, the same with the rows staged in shared
-    memory, or both colours in one launch by strips of rows (the rows next to
-    a strip recomputed; m read from one copy and written to the other), against
-    the scalar per-colour form.  37 + 32 sweeps: the strip form's odd run ends
-    in the second copy and is moved back."""
+    memory, both colours in one launch by strips of rows (the rows next to a
+    strip recomputed; m read from one copy and written to the other), or the
+    staged form by persistent CTAs with the rows fetched by bulk asynchronous
+    copies (a chunk of bands of several replicas per CTA), against the scalar
+    per-colour form.  37 + 32 sweeps: the strip form's odd run ends in the
+    second copy and is moved back."""
     if not form_ok(geom, form):
         pytest.skip("form not available for this lattice (checked in test_mc_forms_rejected_where_ineligible)")
     cfgs = cfgs_for(M, 3, prec, sweep_engine=1, **geom)
@@ -156,7 +158,7 @@ def test_vector_form_on_3d_lattices(M, O, prec, geom):
         assert np.array_equal(got, m)
 
 
-@pytest.mark.parametrize("form", [1, 2, 3])
+@pytest.mark.parametrize("form", [1, 2, 3, 5])
 def test_mc_forms_fp64_decisions_match_oracle(M, O, form):
     c = cfgs_for(M, 1, 64, sweep_engine=1, nx=64, ny=64, pbc_x=1, pbc_y=1)[0]
     with M.Batch([c]) as b:
@@ -226,7 +228,7 @@ def test_mc_forms_rejected_where_ineligible(M):
     with M.Batch(cfgs_for(M, 1, 32, nx=18, ny=8, pbc_x=1, pbc_y=1)) as b:
         s = list(b.launch_shape())
         assert s[6] == 0
-        for form in (2, 3):
+        for form in (2, 3, 5):
             s[6] = form
             with pytest.raises(M.MmcError):
                 b.set_launch_shape(s)
@@ -234,7 +236,14 @@ def test_mc_forms_rejected_where_ineligible(M):
         s = list(b.launch_shape())
         s[6] = 2
         b.set_launch_shape(s)
-        s[6] = 3
+        for form in (3, 5, 6):
+            s[6] = form
+            with pytest.raises(M.MmcError):
+                b.set_launch_shape(s)
+    # the staged forms are for films
+    with M.Batch(cfgs_for(M, 1, 32, nx=8, ny=6, nz=3, pbc_x=1, pbc_y=1, pbc_z=0)) as b:
+        s = list(b.launch_shape())
+        s[6] = 5
         with pytest.raises(M.MmcError):
             b.set_launch_shape(s)
 
@@ -411,7 +420,7 @@ def test_parallel_tempering_fp32_swap_energies(M, O):
 
 
 @pytest.mark.parametrize("prec", [32, 64])
-@pytest.mark.parametrize("form", [2, 4])
+@pytest.mark.parametrize("form", [2, 4, 5])
 def test_tempering_swap_fused_into_next_sweep(M, prec, form):
     """One call of 95 sweeps with swaps every 10 (graphs whose first sweep
     makes the previous interval's swap from the demag field it computes

@@ -511,6 +511,24 @@ def test_device_wait_timeout_is_reported_and_device_stays_usable(M):
         assert a.energy().accepted > 0
 
 
+def test_mbarrier_wait_timeout_is_reported_and_device_stays_usable(M):
+    """The pipelined Metropolis form's bounded wait on a transaction barrier
+    that nothing completes (no copy in flight) gives up after its time limit
+    (1 ms here), the host reads MMC_ERR_TIMEOUT, and the pipelined form then
+    runs and reports no error."""
+    import ctypes
+    st = ctypes.c_int(-1)
+    M.check(M.lib().mmc_selftest_mbar_timeout(0, 1000000, ctypes.byref(st)))
+    assert st.value == 8  # MMC_ERR_TIMEOUT
+    cfgs = [cfg(M, nx=64, ny=32, precision=32, randomseed=5 + r) for r in range(2)]
+    with M.Batch(cfgs) as b:
+        s = list(b.launch_shape())
+        s[6] = 5
+        b.set_launch_shape(s)
+        b.run_sweeps(0, 0, 40)
+        assert all(o.accepted > 0 for o in b.energy())
+
+
 @pytest.mark.parametrize("geom", [dict(nx=16, ny=12, pbc_x=2, pbc_y=1), dict(nx=10, ny=8, nz=3, pbc_x=3, pbc_y=0,
                                                                            pbc_z=0)])
 def test_far_radius_tensor_bitwise_equals_oracle(M, O, geom, tmp_path):
