@@ -441,7 +441,8 @@ def run_ours(args):
         # tile / strip: both colours in one launch, else one launch per colour
         mc = {1: "k_mc_tile", 2: "k_mc_quad", 3: "k_mc_band", 4: "k_mc_strip", 5: "k_mc_pipe"}.get(shape[6],
                                                                                                   "k_mc_checker")
-        col = "k_col_reg" if shape[8] == 2 else "k_col_pass"  # the film column pass held in registers
+        # the film column pass held in registers (three components or one per thread)
+        col = {2: "k_col_reg", 3: "k_col_reg3"}.get(shape[8], "k_col_pass")
         kbytes = {
             "k_x_forward": R * (3 * s_ * n + 3 * 2 * s_ * nh),
             col: R * 2 * (3 * 2 * s_ * nh) + 6 * 2 * s_ * nh,

@@ -383,7 +383,8 @@ int mmc_batch_profile_sweeps(mmc_batch* b, long long stage, long long sweep0, lo
  * of its time limit returns MMC_ERR_TIMEOUT), whether the pass kernels expand their transforms in
  * line (1) or call them out of line (0), whether the column passes
  * transform in place reading the tensor from global memory (1; 2 the same,
- * with film y lines of length 64 or 256 held in registers, other lines as 1),
+ * with film y lines of length 64 or 256 held in registers, other lines as 1;
+ * 3 as 2 with one component per thread),
  * and the number of streams (1-4) the batch's replicas are split over. */
 int mmc_batch_launch_shape(mmc_batch* b, int out[10]);
 /* Autotuner: times each launch shape this batch can run with (the film row
@@ -405,7 +406,7 @@ int mmc_batch_autotune(mmc_batch* b, int sweeps, double* best_ms_per_sweep, int*
  * of two dividing the column-pass thread count, 32-512 threads), tiles whose
  * shared memory fits 220 KB in the chosen column-pass form, a row-kernel band
  * this batch offers, a Metropolis form the lattice qualifies for, 0/1 for the
- * in-line transform flag, 0-2 for the column-pass form and 1-4 streams;
+ * in-line transform flag, 0-3 for the column-pass form and 1-4 streams;
  * anything else is rejected.  Results do
  * not depend on the shape.  No counterpart in the reference. */
 int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]);

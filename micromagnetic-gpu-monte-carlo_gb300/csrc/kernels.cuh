@@ -588,6 +588,95 @@ __global__ void __launch_bounds__(CR_TX * A) k_col_reg(FftPlan p, C<T>* __restri
     }
 }
 
+// The same column pass with each component held by threads of its own:
+// thread (c, t, b) of 3 CR_TX A holds component c of column t (k_col_reg's
+// values y = b + A a).  Each component is transformed by exactly k_col_reg's
+// arithmetic (col_reg_transform1, its own transpose buffer); for the K^
+// product every thread writes its frequencies into its buffer in the
+// transposes' layout and reads the other two components' from theirs, then
+// forms its own component of sum_b K_ab M_b with k_col_reg's expressions.
+// The results equal k_col_reg's (and k_col_pass's) bit for bit.  At 256^2
+// (A = 16) it holds 168 registers per thread -- 12 warps per SM against
+// k_col_reg's 8 -- and takes 31.1 us per batch of 32 replicas against 32.4;
+// capped at 80 registers for two CTAs per SM it spilled and took 36.7.  An
+// autotuner candidate (col_lean = 3).
+template <typename T, bool INV, int A>
+__device__ __forceinline__ void col_reg_transform1(C<T> (&v)[A], C<T>* tb, const C<T>* roots, int t, int b,
+                                                   bool first) {
+  using V = C<T>;
+  constexpr int RW = col_reg_row<A>();
+  RegDft<T, INV, A>::run(v);
+#pragma unroll
+  for (int ka = 1; ka < A; ++ka) {
+    const V w = roots[b * ka];
+    v[ka] = INV ? cmulc(v[ka], w) : cmul(v[ka], w);
+  }
+  if (!first) __syncthreads();
+#pragma unroll
+  for (int ka = 0; ka < A; ++ka) tb[ka * RW + b * CR_TX + t] = v[ka];
+  __syncthreads();
+#pragma unroll
+  for (int bb = 0; bb < A; ++bb) v[bb] = tb[b * RW + bb * CR_TX + t];
+  RegDft<T, INV, A>::run(v);
+}
+
+template <typename T, int A>
+__global__ void __launch_bounds__(3 * CR_TX * A)
+    k_col_reg3(FftPlan p, C<T>* __restrict__ S, long long nspec, const C<T>* __restrict__ khat, int hx, int pitch,
+               int load_lim, int store_lim, int flags, T inv_n, long long s_rstride) {
+  using V = C<T>;
+  constexpr int L = A * A, RW = col_reg_row<A>(), NT = CR_TX * A;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V* roots = reinterpret_cast<V*>(smem_raw);  // exp(-2 pi i j / L), j < L
+  V* tb = roots + L;                          // three buffers of A rows of RW
+  S += blockIdx.z * s_rstride;
+  const int c = threadIdx.x / NT, tt = threadIdx.x - c * NT;  // c is warp-uniform
+  const int t = tt % CR_TX, b = tt / CR_TX;
+  const int kx = blockIdx.x * CR_TX + t;
+  const bool ok = kx < hx;
+  {
+    const V* src = plan_tw<T>(p) + p.full_off;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) roots[i] = src[i];
+  }
+  pdl_wait();  // the spectrum is the x pass's output
+  V v[A];
+#pragma unroll
+  for (int a = 0; a < A; ++a) {
+    const int row = b + A * a;
+    v[a] = (ok && row < load_lim) ? S[c * nspec + (long long)row * pitch + kx] : cmk<V>(0, 0);
+  }
+  __syncthreads();  // roots
+  V* tbc = tb + (size_t)c * A * RW;
+  col_reg_transform1<T, false, A>(v, tbc, roots, t, b, true);
+  __syncthreads();  // every thread has read its transpose
+#pragma unroll
+  for (int kb = 0; kb < A; ++kb) tbc[kb * RW + b * CR_TX + t] = v[kb];
+  __syncthreads();
+  // row c of K^: (xx, xy, xz), (xy, yy, yz) or (xz, yz, zz) in the six blocks
+  // xx, xy, xz, yy, yz, zz
+  const int o0 = c, o1 = c == 0 ? 1 : c == 1 ? 3 : 4, o2 = c == 0 ? 2 : c == 1 ? 4 : 5;
+  // src/demag_cu.cu:98-111: real and imaginary parts of sum_b K_ab M_b, divided by N
+#pragma unroll
+  for (int kb = 0; kb < A; ++kb) {
+    const int pos = b + A * kb;
+    const V* kk = khat + (long long)pos * pitch + (ok ? kx : 0);
+    V k0 = kk[o0 * nspec], k1 = kk[o1 * nspec], k2 = kk[o2 * nspec];
+    if (flags & PASS_SYM) k0.y = k1.y = k2.y = (T)0;
+    const int q = kb * RW + b * CR_TX + t;
+    const V mx = tb[q], my = tb[A * RW + q], mz = tb[2 * A * RW + q];
+    const T hr = (mx.x * k0.x - mx.y * k0.y) + (my.x * k1.x - my.y * k1.y) + (mz.x * k2.x - mz.y * k2.y);
+    const T hi = (mx.x * k0.y + mx.y * k0.x) + (my.x * k1.y + my.y * k1.x) + (mz.x * k2.y + mz.y * k2.x);
+    v[kb] = cmk<V>(hr * inv_n, hi * inv_n);
+  }
+  col_reg_transform1<T, true, A>(v, tbc, roots, t, b, false);
+  if (!ok) return;
+#pragma unroll
+  for (int kb = 0; kb < A; ++kb) {
+    const int row = b + A * kb;
+    if (row < store_lim) S[c * nspec + (long long)row * pitch + kx] = v[kb];
+  }
+}
+
 // Column pass for short lines (n <= 16: the padded z axis of thin 3-D
 // lattices, short y axes): one thread per column (kx, plane) holding the three
 // component lines in registers, transformed by ThreadDft -- no shared-memory
@@ -2188,6 +2277,10 @@ cudaError_t prepare_impl(int max_dyn_smem) {
                                     (int)col_reg_smem<T, 16>()));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_col_reg<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)col_reg_smem<T, 8>()));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_col_reg3<T, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)col_reg_smem<T, 16>()));
+  MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_col_reg3<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)col_reg_smem<T, 8>()));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_strip<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     max_dyn_smem));
   MMC_TRY_ATTR(cudaFuncSetAttribute((const void*)k_mc_strip<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2227,11 +2320,14 @@ cudaError_t run_x_forward(const FftPlan& p, int ncomp, int xdata, int ydata, int
   return cudaGetLastError();
 }
 
+// The film column pass held in registers for a launch shape: 0 none, 1
+// k_col_reg (col_lean 2), 2 k_col_reg3 (col_lean 3).
+inline int col_regs(const DemagTuning& tun) { return tun.col_lean >= 2 ? tun.col_lean - 1 : 0; }
 template <typename T>
 cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, const C<T>* khat, int hx,
                          int planes, long long plane_stride, long long pos_stride, int load_lim, int store_lim,
                          int flags, T inv_n, int tx, int threads, cudaStream_t st, int nrep = 1,
-                         long long s_rstride = 0, bool inl = false, bool lean = false, bool regs = false) {
+                         long long s_rstride = 0, bool inl = false, bool lean = false, int regs = 0) {
   if (ncomp == 3 && p.n <= 16 && p.full_off > 0) {  // short lines: one thread per column
     const ColShortFn<T> ks = col_short_kernel<T>(p.n);
     if (ks) {
@@ -2243,6 +2339,13 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
   if (regs && ncomp == 3 && planes == 1 && (flags & ~PASS_SYM) == (PASS_FWD | PASS_MUL | PASS_INV) &&
       pos_stride < (1LL << 31) && p.warp_a == p.warp_b && (p.warp_a == 16 || p.warp_a == 8)) {
     dim3 grid((hx + CR_TX - 1) / CR_TX, 1, nrep);
+    if (regs == 2) {  // one component per thread
+      if (p.warp_a == 16)
+        return launch_pdl(k_col_reg3<T, 16>, grid, dim3(3 * CR_TX * 16), col_reg_smem<T, 16>(), st, p, S, nspec,
+                          khat, hx, (int)pos_stride, load_lim, store_lim, flags, inv_n, s_rstride);
+      return launch_pdl(k_col_reg3<T, 8>, grid, dim3(3 * CR_TX * 8), col_reg_smem<T, 8>(), st, p, S, nspec, khat,
+                        hx, (int)pos_stride, load_lim, store_lim, flags, inv_n, s_rstride);
+    }
     if (p.warp_a == 16)
       return launch_pdl(k_col_reg<T, 16>, grid, dim3(CR_TX * 16), col_reg_smem<T, 16>(), st, p, S, nspec, khat, hx,
                         (int)pos_stride, load_lim, store_lim, flags, inv_n, s_rstride);
@@ -2291,7 +2394,7 @@ cudaError_t demag_impl(const Geom& g, const FftPlan& px, const FftPlan& py, cons
   if (g.nzp == 1) {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, 1, yplane, ystride, g.ny, g.ny,
                             PASS_FWD | PASS_MUL | PASS_INV | mul_flags, inv_n, tun.col_tx, tun.col_threads, st, nrep,
-                            sr, tun.fft_inline != 0, tun.col_lean != 0, tun.col_lean == 2));
+                            sr, tun.fft_inline != 0, tun.col_lean != 0, col_regs(tun)));
   } else {
     MMC_TRY(run_col_pass<T>(py, 3, S, ns, K, g.hx, g.nz, yplane, ystride, g.ny, g.nyp, PASS_FWD, inv_n, tun.col_tx,
                             tun.col_threads, st, nrep, sr, tun.fft_inline != 0, tun.col_lean != 0));
@@ -2488,7 +2591,7 @@ cudaError_t launch_col_pass_2d(const Geom& g, const FftPlan& py, const DemagTuni
   return run_col_pass<T>(py, 3, reinterpret_cast<C<T>*>(spec), g.nspec, reinterpret_cast<const C<T>*>(khat), g.hx, 1,
                          (long long)g.nyp * g.hxp, g.hxp, g.ny, g.ny, PASS_FWD | PASS_MUL | PASS_INV, inv_n,
                          tun.col_tx, tun.col_threads, st, nrep, 3 * g.nspec, tun.fft_inline != 0,
-                         tun.col_lean != 0, tun.col_lean == 2);
+                         tun.col_lean != 0, col_regs(tun));
 }
 template <typename T>
 cudaError_t launch_prepare(int max_dyn_smem) {

@@ -139,7 +139,8 @@ struct DemagTuning {
   int mc_form;     // MC_FORM_*
   int fft_inline;  // 1: the pass kernels expand the warp-level transforms in line
   int col_lean;    // 1: column passes transform in place and read K^ from global memory; 2: as 1, and
-                   // film y passes of length 64 or 256 hold their lines in registers (k_col_reg)
+                   // film y passes of length 64 or 256 hold their lines in registers (k_col_reg); 3: as 2,
+                   // one component per thread (k_col_reg3)
 };
 
 // Device counters read by the sweep kernels: [stage, sweep].

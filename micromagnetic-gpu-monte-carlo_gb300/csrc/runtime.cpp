@@ -1845,12 +1845,16 @@ int batch_autotune(mmc_batch* b, int sweeps, double* best_ms, int* ncand) {
         }
     }
   }
-  // the column pass held in registers (col_lean = 2; films with y lengths 64 and 256)
+  // the column pass held in registers (films with y lengths 64 and 256):
+  // col_lean = 2 all three components per thread, 3 one component per thread
   if (h->cfg.cal_demag_flag && g.nzp == 1 && h->py.p.warp_a == h->py.p.warp_b &&
       (h->py.p.warp_a == 8 || h->py.p.warp_a == 16)) {
-    Cand c = best;
-    c.tun.col_lean = 2;
-    trial(c);
+    const Cand base = best;
+    for (int form = 2; form <= 3; ++form) {
+      Cand c = base;
+      c.tun.col_lean = form;
+      trial(c);
+    }
   }
   {
     std::vector<int> forms;
@@ -2522,7 +2526,7 @@ int mmc_batch_set_launch_shape(mmc_batch* b, const int shape[10]) {
       (t.mc_form == MC_FORM_STRIP && (!mc_strip_eligible(g) || shape[5] != 0 ||
                                       mc_strip_smem_bytes(g, h->tsize) > smem_limit())) ||
       (t.mc_form == MC_FORM_PIPE && (!mc_pipe_eligible(g) || mc_pipe_smem_bytes(g, h->tsize) > smem_limit())) ||
-      (t.fft_inline != 0 && t.fft_inline != 1) || t.col_lean < 0 || t.col_lean > 2)
+      (t.fft_inline != 0 && t.fft_inline != 1) || t.col_lean < 0 || t.col_lean > 3)
     return fail(MMC_ERR_INVALID, "launch shape outside the supported range");
   if (band != 0 && std::find(b->row_bands.begin(), b->row_bands.end(), band) == b->row_bands.end())
     return fail(MMC_ERR_UNSUPPORTED, "row-kernel band not available for this batch");

@@ -183,14 +183,14 @@ def test_mc_forms_fp64_decisions_match_oracle(M, O, form):
                                   dict(nx=16, ny=32, nz=2, pbc_x=1, pbc_y=1, pbc_z=0),
                                   dict(nx=12, ny=10, nz=3, pbc_x=0, pbc_y=0),
                                   dict(nx=40, ny=256, pbc_x=1, pbc_y=2), dict(nx=24, ny=100, pbc_x=2, pbc_y=0)])
-@pytest.mark.parametrize("variant", ["inline", "lean", "lean_half_threads", "two_streams", "regs"])
+@pytest.mark.parametrize("variant", ["inline", "lean", "lean_half_threads", "two_streams", "regs", "regs3"])
 def test_transform_variants_bitwise_equal(M, prec, geom, variant):
     """The pass kernels with the warp-level transforms in line or out of line,
     the in-place column passes that read K^ from global memory (with the full
-    or half thread count), and the film column pass held in registers
-    (k_col_reg: y lengths 64 and 256 -- ny = 256 periodic, and 100 open, its
-    199 padded to 256 -- the other lattices fall back to the in-place pass),
-    round identically."""
+    or half thread count), and the film column pass held in registers, all
+    three components per thread (k_col_reg) or one (k_col_reg3) -- y lengths
+    64 and 256: ny = 256 periodic, and 100 open, its 199 padded to 256; the
+    other lattices fall back to the in-place pass -- round identically."""
     cfgs = cfgs_for(M, 2, prec, sweep_engine=1, **geom)
     with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
         sa, sb = list(a.launch_shape()), list(b.launch_shape())
@@ -201,6 +201,8 @@ def test_transform_variants_bitwise_equal(M, prec, geom, variant):
             sb[9] = 2
         elif variant == "regs":
             sb[8] = 2
+        elif variant == "regs3":
+            sb[8] = 3
         else:
             sb[8] = 1
             if variant == "lean_half_threads":
