@@ -300,8 +300,19 @@ struct u32x4 {
   uint32_t x, y, z, w;
 };
 
+#if defined(__CUDACC__)
+// The multipliers in the constant bank on the device: a wide multiply takes a
+// constant-bank operand directly, where a literal would first be moved into a
+// register before each multiply (the sweep kernels have none to keep it in).
+static __constant__ uint32_t philox_mul_dev[2] = {0xD2511F53u, 0xCD9E8D57u};
+#endif
+
 MMC_HD u32x4 philox_round(u32x4 c, uint32_t k0, uint32_t k1) {
+#if defined(__CUDA_ARCH__)
+  const uint32_t M0 = philox_mul_dev[0], M1 = philox_mul_dev[1];
+#else
   const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+#endif
   // one 32 x 32 -> 64-bit product per multiplier (a single wide multiply-add
   // on the GPU); hi and lo are its halves
   const uint64_t p0 = (uint64_t)M0 * c.x, p1 = (uint64_t)M1 * c.z;
