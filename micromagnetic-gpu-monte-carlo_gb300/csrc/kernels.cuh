@@ -597,9 +597,11 @@ __global__ void __launch_bounds__(CR_TX * A) k_col_reg(FftPlan p, C<T>* __restri
 // forms its own component of sum_b K_ab M_b with k_col_reg's expressions.
 // The results equal k_col_reg's (and k_col_pass's) bit for bit.  At 256^2
 // (A = 16) it holds 168 registers per thread -- 12 warps per SM against
-// k_col_reg's 8 -- and takes 31.1 us per batch of 32 replicas against 32.4;
-// capped at 80 registers for two CTAs per SM it spilled and took 36.7.  An
-// autotuner candidate (col_lean = 3).
+// k_col_reg's 8 -- and takes 30.3-31.1 us per batch of 32 replicas against
+// 32.4; capped at 80 registers for two CTAs per SM it spilled and took 36.7,
+// and 4 columns per CTA (192 threads, two CTAs per SM at 168 registers, less
+// of the 129th column's tile wasted) took 30.6.  An autotuner candidate
+// (col_lean = 3).
 template <typename T, bool INV, int A>
 __device__ __forceinline__ void col_reg_transform1(C<T> (&v)[A], C<T>* tb, const C<T>* roots, int t, int b,
                                                    bool first) {
