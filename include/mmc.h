@@ -162,6 +162,18 @@ int mmc_transform_dims(const mmc_config* cfg, int out[3]);
 int mmc_create(const mmc_config* cfg, int device, mmc_handle** out);
 void mmc_destroy(mmc_handle* h);
 
+/* The CUDA stream the handle enqueues its work on.  A handle creates a
+ * non-blocking stream of its own; mmc_set_stream moves its work to `stream`
+ * (a cudaStream_t the caller created on the handle's device -- e.g. a
+ * framework's current stream -- and keeps alive while the handle uses it), and
+ * NULL moves it back.  The new stream first waits for the work already
+ * enqueued on the old one, so calls stay in order.  The legacy and per-thread
+ * default streams are refused (MMC_ERR_INVALID): the sweep graphs are captured
+ * on the handle's stream.  Calls that return results still synchronize that
+ * stream.  The reference ran everything on the default stream
+ * (src/main.cu:868-884, 1101-1120). */
+int mmc_set_stream(mmc_handle* h, void* stream);
+
 /* Replaces randInitMx (src/mx_init.h:21-97): every cell gets an independent
  * direction uniform on the sphere, from Philox4x32-10 keyed on the seed. */
 int mmc_init_random(mmc_handle* h, long long seed);
@@ -340,6 +352,9 @@ void mmc_request_stop(mmc_handle* h);
 typedef struct mmc_batch mmc_batch;
 int mmc_batch_create(const mmc_config* cfgs, int nrep, int device, mmc_batch** out);
 void mmc_batch_destroy(mmc_batch* b);
+/* As mmc_set_stream, for the batch's work (the replica parts of a launch
+ * shape with 2-4 streams fork from this stream and join it again). */
+int mmc_batch_set_stream(mmc_batch* b, void* stream);
 int mmc_batch_size(mmc_batch* b);
 int mmc_batch_build_demag(mmc_batch* b, const char* cache_dir);
 /* Per-replica temperatures (K); default Temperature_start of each config. */

@@ -287,7 +287,8 @@ struct mmc_handle {
   int prec = 32;
   size_t tsize = 4;
   Geom g{};
-  cudaStream_t st = nullptr;
+  cudaStream_t st = nullptr;      // where the handle's work is enqueued (st_own or the caller's)
+  cudaStream_t st_own = nullptr;  // created with the handle, destroyed with it
   PlanHost px, py, pz;
   DemagTuning tun{};
   void* m = nullptr;     // 3n T
@@ -973,7 +974,7 @@ void destroy_impl(mmc_handle* h) {
   free_plan(&h->px);
   free_plan(&h->py);
   free_plan(&h->pz);
-  if (h->st) cudaStreamDestroy(h->st);
+  if (h->st_own) cudaStreamDestroy(h->st_own);
   delete h;
 }
 
@@ -1026,8 +1027,9 @@ int create_impl(const mmc_config* cfg, int device, mmc_handle** out) {
   g.dhx = FastDiv((uint32_t)g.hx);
   g.dhxc = FastDiv((uint32_t)((g.nx + 1) / 2));
   int st;
-  if (cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&h->st_own, cudaStreamNonBlocking) != cudaSuccess)
     return bail(fail(MMC_ERR_CUDA, "stream creation failed"));
+  h->st = h->st_own;
   if ((st = make_plan(g.nxp, &h->px)) != MMC_OK) return bail(st);
   if ((st = make_plan(g.nyp, &h->py)) != MMC_OK) return bail(st);
   if ((st = make_plan(g.nzp, &h->pz)) != MMC_OK) return bail(st);
@@ -2101,6 +2103,33 @@ int mmc_create(const mmc_config* cfg, int device, mmc_handle** out) {
 
 void mmc_destroy(mmc_handle* h) { destroy_impl(h); }
 
+// The handle's work moves to `stream` (NULL: its own stream); the new stream
+// first waits for what the old one has enqueued.  Graphs are captured on the
+// handle's stream, so the legacy and per-thread default streams are refused.
+static int set_stream_impl(mmc_handle* h, void* stream) {
+  cudaStream_t ns = stream ? static_cast<cudaStream_t>(stream) : h->st_own;
+  if (ns == cudaStreamLegacy || ns == cudaStreamPerThread)
+    return fail(MMC_ERR_INVALID, "a default stream cannot carry the handle's work (graphs are captured on it)");
+  if (ns == h->st) return MMC_OK;
+  TRY(set_dev(h));
+  int dev = -1;
+  CU(cudaStreamGetDevice(ns, &dev));
+  if (dev != h->device) return fail(MMC_ERR_INVALID, "the stream belongs to another device");
+  cudaEvent_t e = nullptr;
+  CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  cudaError_t r = cudaEventRecord(e, h->st);
+  if (r == cudaSuccess) r = cudaStreamWaitEvent(ns, e, 0);
+  cudaEventDestroy(e);
+  CU(r);
+  h->st = ns;
+  return MMC_OK;
+}
+
+int mmc_set_stream(mmc_handle* h, void* stream) {
+  if (!h) return fail(MMC_ERR_INVALID, "null handle");
+  return set_stream_impl(h, stream);
+}
+
 int mmc_init_random(mmc_handle* h, long long seed) {
   if (!h) return fail(MMC_ERR_INVALID, "null handle");
   TRY(set_dev(h));
@@ -2561,6 +2590,11 @@ int mmc_batch_launch_shape(mmc_batch* b, int out[10]) {
   out[3] = b->tun.col_tx_z;
   out[4] = b->tun.col_threads;
   return MMC_OK;
+}
+
+int mmc_batch_set_stream(mmc_batch* b, void* stream) {
+  if (!b) return fail(MMC_ERR_INVALID, "null batch");
+  return set_stream_impl(b->base, stream);
 }
 
 int mmc_batch_last_run_ms(mmc_batch* b, double* ms) {

@@ -189,6 +189,8 @@ def lib(path=None):
                                                         ctypes.POINTER(ctypes.c_int)]),
         "mmc_selftest_mbar_timeout": (ctypes.c_int, [ctypes.c_int, ctypes.c_longlong,
                                                      ctypes.POINTER(ctypes.c_int)]),
+        "mmc_set_stream": (ctypes.c_int, [H, ctypes.c_void_p]),
+        "mmc_batch_set_stream": (ctypes.c_int, [H, ctypes.c_void_p]),
         "mmc_batch_request_stop": (None, [H]),
         "mmc_batch_energy": (ctypes.c_int, [H, ctypes.POINTER(Observables)]),
         "mmc_batch_set_m": (ctypes.c_int, [H, ctypes.c_int, _dp, _dp, _dp]),
@@ -306,6 +308,11 @@ class Lattice:
 
     def build_demag(self, cache_dir=""):
         check(lib().mmc_build_demag(self.h, cache_dir.encode() if cache_dir else None))
+
+    def set_stream(self, stream):
+        """Enqueue the lattice's work on a caller's cudaStream_t (an int
+        handle, e.g. torch.cuda.Stream().cuda_stream); None: its own stream."""
+        check(lib().mmc_set_stream(self.h, ctypes.c_void_p(stream) if stream else None))
 
     def tensor(self):
         np_ = self.pdims[0] * self.pdims[1] * self.pdims[2]
@@ -428,6 +435,10 @@ class Batch:
 
     def build_demag(self, cache_dir=""):
         check(lib().mmc_batch_build_demag(self.h, cache_dir.encode() if cache_dir else None))
+
+    def set_stream(self, stream):
+        """As Lattice.set_stream, for the batch's work."""
+        check(lib().mmc_batch_set_stream(self.h, ctypes.c_void_p(stream) if stream else None))
 
     def set_temperatures(self, T):
         T = np.ascontiguousarray(T, dtype=np.float64)

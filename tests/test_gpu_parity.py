@@ -599,3 +599,40 @@ def test_open_axis_with_large_prime_padding(M, O, prec):
         acc = O.sweeps(c, k, 150.0, 1, 0, 30, m, demag_mode=1)
         assert acc_gpu == acc
         assert np.array_equal(m_gpu, m)
+
+
+def test_caller_stream(M):
+    """A lattice's and a batch's work enqueued on a caller's stream (a torch
+    stream here) gives the results of their own streams, in order with the
+    work enqueued before the switch and after switching back; the default
+    streams are refused."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    s = torch.cuda.Stream()
+    c = cfg(M, nx=32, ny=32, precision=32)
+    with M.Lattice(c) as a, M.Lattice(c) as b:
+        a.run_sweeps(300.0, 0, 0, 10)
+        b.run_sweeps(300.0, 0, 0, 10)
+        b.set_stream(s.cuda_stream)
+        a.run_sweeps(300.0, 0, 10, 40)
+        b.run_sweeps(300.0, 0, 10, 40)
+        b.set_stream(None)
+        a.run_sweeps(300.0, 0, 50, 5)
+        b.run_sweeps(300.0, 0, 50, 5)
+        assert np.array_equal(a.get_m(), b.get_m())
+        assert a.energy().accepted == b.energy().accepted
+        for bad in (1, 2):  # cudaStreamLegacy, cudaStreamPerThread
+            with pytest.raises(M.MmcError):
+                M.check(M.lib().mmc_set_stream(b.h, ctypes.c_void_p(bad)))
+    cfgs = [cfg(M, nx=64, ny=32, precision=32, randomseed=40 + r) for r in range(3)]
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        sh = list(b.launch_shape())
+        sh[9] = 2  # replica parts on two streams, forked from the caller's
+        a.set_launch_shape(sh)
+        b.set_launch_shape(sh)
+        b.set_stream(s.cuda_stream)
+        a.run_sweeps(0, 0, 70)
+        b.run_sweeps(0, 0, 70)
+        for r in range(3):
+            assert np.array_equal(a.get_m(r), b.get_m(r))
+        b.set_stream(None)
