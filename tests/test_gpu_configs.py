@@ -8,7 +8,7 @@ T from 1400 K down by x0.90 per stage.
 - FP64 accept/reject decisions bit-identical to the oracle's for 100 sweeps
   at 64x64x1 (seed 256) and at 256x256x1, at the first stage's temperature
   and at the last stage's;
-- the batched FP32 vectorised Metropolis form at 256x256x1 (32 replicas, the
+- the batched FP32 vectorised Metropolis form at 256x256x1 (64 replicas, the
   benchmark's batch) against batched FP64 from the same states;
 - the stage loop's energy.txt lines and final state against the oracle's.
 
@@ -59,12 +59,12 @@ def test_fp64_decisions_bitwise_at_benchmark_configs(M, O, cache, side, seed, T,
 
 
 def test_batched_fp32_vector_form_tracks_fp64_at_256(M, cache):
-    """32 replicas of 256x256x1 (seeds 256..287) through the vectorised FP32
-    Metropolis form, against 32 FP64 replicas from the same FP32-representable
+    """64 replicas of 256x256x1 (seeds 256..319) through the vectorised FP32
+    Metropolis form, against 64 FP64 replicas from the same FP32-representable
     states: both use the same Philox stream, so they make the same decisions
     until a near-tie; after 3 sweeps nearly every spin agrees to FP32 rounding
     and the energies agree to 1e-4 relative."""
-    R = 32
+    R = 64
     c32 = [config(M, 256, 32, 256 + r) for r in range(R)]
     c64 = [config(M, 256, 64, 256 + r) for r in range(R)]
     with M.Batch(c32) as a, M.Batch(c64) as b:
