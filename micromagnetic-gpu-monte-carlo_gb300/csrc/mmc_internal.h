@@ -81,9 +81,10 @@ struct Geom {
   FastDiv dnx, dny, dhx, dhxc;  // nx, ny, hx, (nx + 1) / 2
 };
 
-// Metropolis coefficients, all in units of kT (see the sweep kernel).
+// Metropolis coefficients, all in units of kT (see the sweep kernel).  16-byte
+// aligned: a sweep thread copies its replica's set with 16-byte loads.
 template <typename T>
-struct McCoef {
+struct alignas(16) McCoef {
   T wex[3];   // 2 Aex V / (d_a^2 kT)
   T wdm[2];   // Dind V / (d_a kT), a = x, y
   T can;      // Ku1 V / kT
