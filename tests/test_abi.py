@@ -34,6 +34,14 @@ def test_null_arguments_are_rejected(M):
     assert L.mmc_create(None, 0, None) == M.ERR_INVALID
     assert b"null" in L.mmc_last_error()
     assert L.mmc_get_m(None, None, None, None) == M.ERR_INVALID
+    assert L.mmc_set_stream(None, None) == M.ERR_INVALID
+    assert L.mmc_batch_set_stream(None, None) == M.ERR_INVALID
+    st = ctypes.c_int(-1)
+    # the self-tests check their arguments before touching a device
+    assert L.mmc_selftest_mbar_timeout(0, 0, ctypes.byref(st)) == M.ERR_INVALID
+    assert L.mmc_selftest_mbar_timeout(0, 2_000_000_000, ctypes.byref(st)) == M.ERR_INVALID
+    assert L.mmc_selftest_mbar_timeout(0, 1000, None) == M.ERR_INVALID
+    assert st.value == -1
 
 
 def test_create_validates_config_before_touching_a_device(M):
