@@ -62,7 +62,7 @@ def ncu_traffic(kernel, shape, R):
     (the autotuner's pick varies between runs), then a capture with another
     replica count scaled by the replicas (a launch's traffic is one pass over
     its replicas' data); else (None, None)."""
-    p = os.path.join(ROOT, "profiles", "batch32_256x256_kernels.md")
+    p = os.path.join(ROOT, "profiles", "batched_256x256_kernels.md")
     if not os.path.exists(p):
         return None, None
     want = ",".join(str(v) for v in shape)
