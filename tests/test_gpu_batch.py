@@ -345,6 +345,29 @@ def test_streams_with_tempering_and_odd_batch(M, streams):
 
 
 @pytest.mark.parametrize("prec", [32, 64])
+@pytest.mark.parametrize("geom", [dict(nx=1024, ny=6, pbc_x=1, pbc_y=1), dict(nx=512, ny=9, pbc_x=1, pbc_y=0),
+                                  dict(nx=8, ny=300, pbc_x=0, pbc_y=1)])
+def test_pipelined_form_wide_and_tall_films(M, prec, geom):
+    """The pipelined staged form where its buffers are largest (one row per
+    band at nx = 1024: 96 KB per buffer in FP64) or hold many rows (nx = 8:
+    bands of 128 rows), with open and periodic y edges and replicas spread
+    over two streams, against the scalar per-colour form."""
+    cfgs = cfgs_for(M, 5, prec, sweep_engine=1, **geom)
+    with M.Batch(cfgs) as a, M.Batch(cfgs) as b:
+        sa, sb = list(a.launch_shape()), list(b.launch_shape())
+        sa[6], sb[6] = 0, 5
+        sb[9] = 2
+        a.set_launch_shape(sa)
+        b.set_launch_shape(sb)
+        for s0, n in ((0, 7), (7, 32)):
+            a.run_sweeps(2, s0, n)
+            b.run_sweeps(2, s0, n)
+        for r in range(5):
+            assert np.array_equal(a.get_m(r), b.get_m(r)), r
+        assert [o.accepted for o in a.energy()] == [o.accepted for o in b.energy()]
+
+
+@pytest.mark.parametrize("prec", [32, 64])
 @pytest.mark.parametrize("streams", [1, 3])
 def test_strip_form_with_streams_tempering_and_profile(M, prec, streams):
     """The strip form (form 4: both colours in one launch, m alternating
