@@ -60,16 +60,16 @@ def test_full_anneal_statistics_fp32_vs_fp64(M, tmp_path_factory):
 
 
 STATS_SWEEPS_256 = int(os.environ.get("MMC_STATS_SWEEPS_256", "1000"))
-SEEDS_256 = list(range(1, 17))
+SEEDS_256 = list(range(1, 33))
 
 
 def test_full_anneal_statistics_256_fp32_vs_fp64(M, tmp_path_factory):
     """The 256x256x1 film with PBC 20 images and the same material and
-    schedule (34 stages, 1400 K -> 40 K by x0.90): 16 batched FP32 anneals
-    against 16 batched FP64 anneals (seeds 1..16).  Sweeps per stage: 1000 by
-    default (the FP64 batch takes ~1 ms per sweep on GB300, whose FP64 rate is
+    schedule (34 stages, 1400 K -> 40 K by x0.90): 32 batched FP32 anneals
+    against 32 batched FP64 anneals (seeds 1..32).  Sweeps per stage: 1000 by
+    default (the FP64 batch takes ~2 ms per sweep on GB300, whose FP64 rate is
     a small fraction of its FP32 rate); MMC_STATS_SWEEPS_256=10000 runs the
-    benchmark schedule itself (~6 minutes).
+    benchmark schedule itself (~13 minutes).
     Checked: (1) final energy density, <m_z> and Q agree within 4 standard
     errors of the difference of the means; (2) the FP32 path's energy of each
     final FP32 state is within 1e-4 relative of the FP64 evaluation of the same
