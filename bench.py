@@ -262,11 +262,11 @@ SLAB = dict(nx=512, ny=512, nz=8, dx=2e-9, dy=2e-9, dz=1e-9, ms=1.1e6, Aex=15e-1
 def launches_per_step(S, shape, R, graph_sweeps=32):
     """Kernel launches of one timed step of S sweeps with a launch shape: per
     sweep the row kernel and the column pass (row path), or the x, column and
-    inverse x passes and the Metropolis launches (one tile launch, or one per
-    colour), once per replica part inside the 32-sweep graphs and on one stream
-    for the sweeps left over; one counter advance per graph and after the
-    left-over sweeps."""
-    per = 2 if shape[5] > 0 else 4 if shape[6] == 1 else 5
+    inverse x passes and the Metropolis launches (one tile or strip launch for
+    both colours, or one per colour), once per replica part inside the
+    32-sweep graphs and on one stream for the sweeps left over; one counter
+    advance per graph and after the left-over sweeps."""
+    per = 2 if shape[5] > 0 else 4 if shape[6] in (1, 4) else 5
     parts = 1 if shape[5] > 0 else min(shape[9], R)
     graphs, rem = divmod(S, graph_sweeps)
     return graphs * graph_sweeps * per * parts + rem * per + graphs + (1 if rem else 0)
