@@ -1,6 +1,7 @@
 // mmc_main.cpp -- command-line driver, a drop-in for the reference binary.
 //
 //   mmc <cfg.ini> [-gpu=N] [-tensorcache="/path/"] [-farm-Bz=b1,b2,...] [-farm-D=d1,d2,...]
+//       [-farm-seeds=N]
 //
 // Argument handling follows src/main.cu:97-105 and src/GPU_selector.h:11-76:
 // the first argument not starting with '-' is the ini file, -gpu=N picks the
@@ -8,10 +9,12 @@
 // Outputs go to <ini dir>/<ini stem>.output/ (src/main.cu:193-231): energy.txt
 // and the OVF snapshots.  Ctrl-C stops the anneal at the next sweep boundary.
 //
-// -farm-Bz= / -farm-D= (not in the reference) anneal a parameter sweep from the
-// same ini: one replica per (B_z, D) pair, replica k seeded randomseed + k,
-// all in one batch on the GPU; replica k writes into replica_<kkk>/ of the
-// output folder and farm.txt lists k, B_z, D and the seed.
+// -farm-Bz= / -farm-D= / -farm-seeds= (not in the reference) anneal a parameter
+// sweep or a seed ensemble from the same ini: N replicas (-farm-seeds, default
+// 1) per (B_z, D) pair, replica k seeded randomseed + k, all in one batch on
+// the GPU; replica k writes into replica_<kkk>/ of the output folder and
+// farm.txt lists k, B_z, D and the seed.
+#include <algorithm>
 #include <csignal>
 #include <cstdio>
 #include <cstdlib>
@@ -49,16 +52,17 @@ static bool parse_list(const std::string& s, std::vector<double>& out) {
 
 // The parameter sweep: one batch of replicas, the stage loop for all of them.
 static int run_farm(const mmc_config& cfg, int gpu, const std::vector<double>& bz, const std::vector<double>& dm,
-                    const std::string& out) {
+                    int seeds, const std::string& out) {
   std::vector<mmc_config> cfgs;
   for (double b : bz)
-    for (double d : dm) {
-      mmc_config c = cfg;
-      c.Bextz = b;
-      c.Dind = d;
-      if (cfg.randomseed >= 0) c.randomseed = cfg.randomseed + (long long)cfgs.size();
-      cfgs.push_back(c);
-    }
+    for (double d : dm)
+      for (int s = 0; s < seeds; ++s) {
+        mmc_config c = cfg;
+        c.Bextz = b;
+        c.Dind = d;
+        if (cfg.randomseed >= 0) c.randomseed = cfg.randomseed + (long long)cfgs.size();
+        cfgs.push_back(c);
+      }
   std::printf("farm: %zu replicas\n", cfgs.size());
   int st = mmc_batch_create(cfgs.data(), (int)cfgs.size(), gpu, &g_batch);
   if (st != MMC_OK) return st;
@@ -100,6 +104,7 @@ int main(int argc, char** argv) {
   std::string cfg_path, cache;
   int gpu = 0;
   std::vector<double> farm_bz, farm_d;
+  int farm_seeds = 0;
   for (int i = 1; i < argc; ++i) {
     std::string a = argv[i];
     if (a.empty()) continue;
@@ -127,6 +132,14 @@ int main(int argc, char** argv) {
         std::printf("Invalid command line parameter: -farm-D=\n");
         return 1;
       }
+    } else if (key.rfind("farm-seeds=", 0) == 0) {
+      char* end = nullptr;
+      const long v = std::strtol(key.c_str() + 11, &end, 10);
+      if (key.size() == 11 || *end != '\0' || v < 1 || v > 65535) {
+        std::printf("Invalid command line parameter: -farm-seeds=\n");
+        return 1;
+      }
+      farm_seeds = (int)v;
     }
   }
   cfg_path = abspath(cfg_path);
@@ -151,10 +164,14 @@ int main(int argc, char** argv) {
   std::string out = dir + "/" + stem + ".output";
   std::printf("output_path: %s\n", out.c_str());
 
-  if (!farm_bz.empty() || !farm_d.empty()) {
+  if (!farm_bz.empty() || !farm_d.empty() || farm_seeds > 0) {
     if (farm_bz.empty()) farm_bz.push_back(cfg.Bextz);
     if (farm_d.empty()) farm_d.push_back(cfg.Dind);
-    st = run_farm(cfg, gpu, farm_bz, farm_d, out);
+    if ((long long)farm_bz.size() * (long long)farm_d.size() * std::max(farm_seeds, 1) > 65535) {
+      std::printf("Invalid command line parameters: more than 65535 farm replicas\n");
+      return 1;
+    }
+    st = run_farm(cfg, gpu, farm_bz, farm_d, std::max(farm_seeds, 1), out);
     int rc = 0;
     if (st == MMC_ERR_INTERRUPTED) {
       std::printf("interrupted\n");

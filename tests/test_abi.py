@@ -69,7 +69,8 @@ def test_cli_bad_farm_list(M, tmp_path):
     cli = os.path.join(M.HERE, "bin", "mmc")
     p = tmp_path / "x.ini"
     p.write_text("nx = 1\n")
-    for arg in ("-farm-Bz=0.1,abc", "-farm-D=", "-farm-Bz=0.1,,0.2"):
+    for arg in ("-farm-Bz=0.1,abc", "-farm-D=", "-farm-Bz=0.1,,0.2", "-farm-seeds=0", "-farm-seeds=",
+                "-farm-seeds=3x", "-farm-seeds=70000"):
         r = subprocess.run([cli, str(p), arg], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True,
                            timeout=60)
         assert r.returncode == 1 and "Invalid command line parameter" in r.stdout, arg

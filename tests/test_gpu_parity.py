@@ -377,10 +377,13 @@ def test_cli_end_to_end(M, tmp_path):
     assert len(list(out.glob("*.ovf"))) == 3
 
 
-def test_cli_parameter_farm_equals_single_runs(M, tmp_path):
-    """-farm-Bz= / -farm-D= anneal every (B_z, D) pair as a replica of one
-    batch; each replica's energy.txt and snapshots equal those of a single CLI
-    run of the ini with that B_z, D and seed."""
+@pytest.mark.parametrize("args,count", [(("-farm-Bz=0.1,0.4", "-farm-D=3e-3,5e-3"), 4),
+                                        (("-farm-Bz=0.2", "-farm-seeds=3"), 3)])
+def test_cli_parameter_farm_equals_single_runs(M, tmp_path, args, count):
+    """-farm-Bz= / -farm-D= / -farm-seeds= anneal every (B_z, D) pair, as many
+    seeds of each as asked, as replicas of one batch; each replica's
+    energy.txt and snapshots equal those of a single CLI run of the ini with
+    that B_z, D and seed."""
     import shutil
     import subprocess
     text = open(os.path.join(os.path.dirname(__file__), "test_host_io.py")).read()
@@ -393,12 +396,12 @@ def test_cli_parameter_farm_equals_single_runs(M, tmp_path):
     farm_dir = tmp_path / "farm"
     farm_dir.mkdir()
     (farm_dir / "f.ini").write_text(body)
-    r = subprocess.run([cli, str(farm_dir / "f.ini"), "-farm-Bz=0.1,0.4", "-farm-D=3e-3,5e-3"],
+    r = subprocess.run([cli, str(farm_dir / "f.ini"), *args],
                        stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     out = farm_dir / "f.output"
     rows = [l.split() for l in (out / "farm.txt").read_text().splitlines()]
-    assert len(rows) == 4
+    assert len(rows) == count
     base_seed = int(M.load_ini(str(farm_dir / "f.ini")).randomseed)
     for k, bz, dm, seed in rows:
         assert int(seed) == base_seed + int(k)
