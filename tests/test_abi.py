@@ -48,6 +48,11 @@ def test_create_validates_config_before_touching_a_device(M):
     c = M.Config.defaults(nx=0)
     h = ctypes.c_void_p()
     assert M.lib().mmc_create(ctypes.byref(c), 0, ctypes.byref(h)) == M.ERR_CONFIG
+    # 2^31 cells or more: indices are 32-bit inside the kernels
+    for dims in ((65536, 32768, 1), (2048, 2048, 512)):
+        c = M.Config.defaults(nx=dims[0], ny=dims[1], nz=dims[2])
+        assert M.lib().mmc_create(ctypes.byref(c), 0, ctypes.byref(h)) == M.ERR_CONFIG, dims
+        assert b"2^31" in M.lib().mmc_last_error() or b"cells" in M.lib().mmc_last_error()
 
 
 def test_cli_usage(M):
