@@ -341,11 +341,12 @@ __device__ __forceinline__ void col_pass_body(const FftPlan& p, int ncomp, C<T>*
   const int ntx = min(tx, hx - kx0);
   const long long pbase = (long long)blockIdx.y * plane_stride + kx0;
   const int nlines = ncomp * ntx;
-  // lean (warp-level transforms only): one buffer, transformed in place, and
-  // the tensor read from global memory in the product -- a third of the
-  // shared memory, so more CTAs fit on an SM
+  // lean 1 (warp-level transforms only): one buffer, transformed in place,
+  // and the tensor read from global memory in the product -- a third of the
+  // shared memory, so more CTAs fit on an SM.  lean 2: two buffers, the tensor
+  // read from global memory (lines too long for the staged tensor tile).
   V* bufA = tw + ((p.tw_total + 1) & ~1);
-  V* bufB = lean ? bufA : bufA + (long long)ncomp * tx * stride;
+  V* bufB = lean == 1 ? bufA : bufA + (long long)ncomp * tx * stride;
   V* ktile = bufB + (long long)ncomp * tx * stride;  // [comp][pos][t] when PASS_MUL and not lean
   load_twiddles<T>(p, tw);
   // the tensor tile goes to shared memory asynchronously while the forward
@@ -2222,6 +2223,10 @@ inline size_t col_pass_smem(const FftPlan& p, int ncomp, int tx, size_t csize, b
           (mul ? 6 * (size_t)p.n * tx : 0)) *
          csize;
 }
+// Two line buffers and no tensor tile (the tensor read from global memory).
+inline size_t col_pass_smem_kglobal(const FftPlan& p, int ncomp, int tx, size_t csize) {
+  return col_pass_smem(p, ncomp, tx, csize, false);
+}
 
 // The warp-shaped x-pass kernels for the plan's (A, B), or null.
 template <typename T>
@@ -2355,9 +2360,21 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
                       (int)pos_stride, load_lim, store_lim, flags, inv_n, s_rstride);
   }
   if (tx < 1 || (tx & (tx - 1)) != 0 || threads % tx != 0) return cudaErrorInvalidValue;  // see k_col_pass
-  lean = lean && p.warp_a != 0;  // in-place transforms exist for the warp path only
-  size_t sm = lean ? col_pass_smem_lean(p, ncomp, tx, sizeof(C<T>))
-                   : col_pass_smem(p, ncomp, tx, sizeof(C<T>), (flags & PASS_MUL) != 0);
+  // in-place transforms exist for the warp path only
+  int lmode = lean && p.warp_a != 0 ? 1 : 0;
+  size_t sm = lmode ? col_pass_smem_lean(p, ncomp, tx, sizeof(C<T>))
+                    : col_pass_smem(p, ncomp, tx, sizeof(C<T>), (flags & PASS_MUL) != 0);
+  if (!lmode && (flags & PASS_MUL) && sm > 48 * 1024) {
+    // a tensor tile that does not fit beside the two line buffers is read from
+    // global memory in the product instead (the same values, so the same results)
+    int dev = 0, optin = 0;
+    MMC_TRY_ATTR(cudaGetDevice(&dev));
+    MMC_TRY_ATTR(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    if (sm > (size_t)optin) {
+      lmode = 2;
+      sm = col_pass_smem_kglobal(p, ncomp, tx, sizeof(C<T>));
+    }
+  }
   dim3 grid((hx + tx - 1) / tx, planes, nrep);
   auto kern = p.warp_a == 32 ? (inl ? k_col_pass_wide<T, true> : k_col_pass_wide<T, false>)
                              : (inl ? k_col_pass<T, true> : k_col_pass<T, false>);
@@ -2369,7 +2386,7 @@ cudaError_t run_col_pass(const FftPlan& p, int ncomp, C<T>* S, long long nspec, 
   threads -= threads % std::max(tx, 32);
   if (threads < 32) return cudaErrorInvalidValue;
   return launch_pdl(kern, grid, dim3(threads), sm, st, p, ncomp, S, nspec, khat, hx, plane_stride, pos_stride,
-                    load_lim, store_lim, flags, inv_n, tx, s_rstride, lean ? 1 : 0);
+                    load_lim, store_lim, flags, inv_n, tx, s_rstride, lmode);
 }
 
 #define MMC_TRY(x)                       \

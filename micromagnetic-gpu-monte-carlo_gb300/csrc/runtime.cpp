@@ -208,7 +208,9 @@ size_t x_pass_smem(const FftPlan& px, int r, size_t csize) {
 size_t col_pass_smem(const FftPlan& p, int tx, size_t csize, bool lean = false) {
   const size_t tw = (size_t)((p.tw_total + 1) & ~1), lines = (size_t)3 * tx * col_line_stride(p, csize);
   if (lean && p.warp_a) return (tw + lines) * csize;
-  return (tw + 2 * lines + 6 * (size_t)p.n * tx) * csize;
+  // the pass reads K^ from global memory when its tile would not fit
+  const size_t staged = (tw + 2 * lines + 6 * (size_t)p.n * tx) * csize;
+  return staged <= smem_limit() ? staged : (tw + 2 * lines) * csize;
 }
 
 // Launch shapes for `nrep` replicas.  The warp-level FFT gives each warp
@@ -253,7 +255,8 @@ DemagTuning choose_tuning(const Geom& g, const FftPlan& px, const FftPlan& py, c
   auto csm = [&](const FftPlan& p, int tx, bool mul) {
     const size_t tw = (size_t)((p.tw_total + 1) & ~1), lines = (size_t)3 * tx * col_line_stride(p, csize);
     if (t.col_lean && p.warp_a) return (tw + lines) * csize;
-    return (tw + 2 * lines + (mul ? 6 * (size_t)p.n * tx : 0)) * csize;
+    const size_t staged = (tw + 2 * lines + (mul ? 6 * (size_t)p.n * tx : 0)) * csize;
+    return staged <= smem_limit() ? staged : (tw + 2 * lines) * csize;  // K^ from global memory
   };
   auto pick = [&](const FftPlan& p, int planes, bool mul) {
     // short lines (a few padded z layers) take wider tiles, up to 64 columns

@@ -80,3 +80,31 @@ def test_slab_fp32_sweeps_energy_matches_fp64_evaluation(M, cache):
     assert abs(o32.e_total - o64.e_total) <= 1e-4 * abs(o64.e_total)
     assert np.abs(t32 - t64).max() <= 1e-4 * np.abs(t64).sum()
     assert np.abs(np.array(o32.m) - np.array(o64.m)).max() <= 1e-6
+
+
+def test_large_film_beyond_the_warp_transforms(M, tmp_path):
+    """A 1500 x 1500 periodic film (one image per side): transforms of length
+    1500 = 2^2 3 5^3 have no warp-level plan and run on the general mixed-radix
+    path, and in FP64 the column pass's tensor tile does not fit beside its
+    line buffers, so the pass reads the tensor from global memory.  FP64
+    linearity (1e-12) and the FP32 field against the FP64 field of the same
+    state (1e-5).  (Sides whose transform needs more shared memory than a CTA
+    has -- 2048 periodic, 600 open -- are refused at creation.)"""
+    geom = dict(nx=1500, ny=1500, nz=1, dx=2e-9, dy=2e-9, dz=1e-9, pbc_x=1, pbc_y=1, pbc_z=0, cal_demag_flag=1,
+                randomseed=3, sweep_engine=1)
+    cache = str(tmp_path)
+    with M.Lattice(M.Config.defaults(precision=64, **geom)) as lat:
+        lat.build_demag(cache)
+        m1 = lat.get_m().astype(np.float32).astype(np.float64)
+        m2 = np.roll(m1, 7, axis=1)
+        h1 = demag(lat, M, m1)
+        h2 = demag(lat, M, m2)
+        h12 = demag(lat, M, m1 - 0.5 * m2)
+        assert rel(h12, h1 - 0.5 * h2) <= 1e-12
+    with M.Lattice(M.Config.defaults(precision=32, **geom)) as lat:
+        lat.build_demag(cache)
+        h32 = demag(lat, M, m1)
+    assert rel(h32, h1) <= 1e-5
+    with pytest.raises(M.MmcError) as ei:
+        M.Lattice(M.Config.defaults(precision=32, **dict(geom, nx=2048, ny=2048)))
+    assert ei.value.status == M.ERR_UNSUPPORTED
